@@ -1,0 +1,192 @@
+"""GB300 collision-integral library: Python view of the C ABI in include/gpu_determ.h.
+
+The compute path is libgpu_determ.so (hand-written sm_103a kernels) built in
+tree by ``gpu_determ_gb300.build``.  There is no CPU fallback: if the library
+is missing or cannot be loaded, importing the bindings raises.
+
+Arrays passed to the operator are CUDA tensors (torch) or raw device
+pointers (int); distributions are laid out [node][cell] with the compact
+in-sphere node index and leading dimension ``ld``.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+__all__ = ["GDError", "GridSpec", "Context", "lib", "library_path", "DT_COURANT", "DT_FIXED"]
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(_HERE, "libgpu_determ.so")
+_lib = None
+
+DT_COURANT = 0
+DT_FIXED = 1
+
+_ERRORS = {1: "invalid argument", 2: "CUDA error", 3: "out of memory", 4: "unsupported",
+           5: "singular system", 6: "I/O error"}
+
+
+class GDError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"gpu_determ error {code} ({_ERRORS.get(code, '?')}): {msg}")
+        self.code = code
+
+
+class _Spec(C.Structure):
+    _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int),
+                ("vmin", C.c_float * 3), ("vmax", C.c_float * 3), ("R", C.c_float)]
+
+
+class _Info(C.Structure):
+    _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int), ("n_pnt", C.c_int),
+                ("du", C.c_float), ("dv", C.c_float), ("dw", C.c_float), ("d3v", C.c_float),
+                ("nonzero_weights", C.c_int64), ("table_a_elems", C.c_int64),
+                ("pair_products", C.c_int64), ("contraction_terms", C.c_int64),
+                ("scatter_terms", C.c_int64)]
+
+
+def library_path() -> str:
+    return _LIB_PATH
+
+
+def lib():
+    """Load libgpu_determ.so (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(_LIB_PATH):
+        raise ImportError(
+            f"{_LIB_PATH} is missing: build it with `python -m gpu_determ_gb300.build` "
+            "(there is no CPU fallback)")
+    L = C.CDLL(_LIB_PATH)
+    vp, i, f, P = C.c_void_p, C.c_int, C.c_float, C.POINTER
+    L.gd_version.restype = i
+    L.gd_last_error.restype = C.c_char_p
+    L.gd_grid_count.argtypes = [P(_Spec), P(i)]
+    L.gd_grid_fill.argtypes = [P(_Spec), vp, vp, vp, vp, vp, vp, vp]
+    L.gd_ctx_create.argtypes = [P(_Spec), i, P(vp)]
+    L.gd_ctx_destroy.argtypes = [vp]
+    L.gd_ctx_info.argtypes = [vp, P(_Info)]
+    L.gd_export_tables.argtypes = [vp, vp, vp, vp]
+    L.gd_correction_basis.argtypes = [vp, vp, vp]
+    L.gd_collision.argtypes = [vp, vp, i, i, vp, vp, vp]
+    L.gd_project.argtypes = [vp, vp, vp, vp, i, i, vp, vp, vp, vp]
+    L.gd_relax.argtypes = [vp, vp, vp, vp, i, i, i, f, vp, vp, vp]
+    L.gd_step.argtypes = [vp, vp, i, i, i, f, vp, vp, vp, vp, vp, vp, vp]
+    L.gd_moments.argtypes = [vp, vp, i, i, vp, vp]
+    for name in ("gd_grid_count", "gd_grid_fill", "gd_ctx_create", "gd_ctx_destroy", "gd_ctx_info",
+                 "gd_export_tables", "gd_correction_basis", "gd_collision", "gd_project",
+                 "gd_relax", "gd_step", "gd_moments"):
+        getattr(L, name).restype = i
+    _lib = L
+    return L
+
+
+def _check(rc: int):
+    if rc != 0:
+        raise GDError(rc, lib().gd_last_error().decode(errors="replace"))
+
+
+def _ptr(x):
+    """Device pointer of a tensor (or an int / None)."""
+    if x is None:
+        return None
+    if isinstance(x, int):
+        return x
+    return x.data_ptr()
+
+
+def _stream(s):
+    if s is None:
+        return None
+    if isinstance(s, int):
+        return s
+    return s.cuda_stream
+
+
+class GridSpec:
+    """Velocity lattice [vmin, vmax]^3 with n points per axis, cut to |xi| < R."""
+
+    def __init__(self, nx, ny=None, nz=None, vmin=(-5.0, -5.0, -5.0), vmax=(5.0, 5.0, 5.0), R=16.5):
+        self.nx, self.ny, self.nz = nx, (nx if ny is None else ny), (nx if nz is None else nz)
+        self.vmin = tuple(float(v) for v in vmin)
+        self.vmax = tuple(float(v) for v in vmax)
+        self.R = float(R)
+
+    def _c(self) -> _Spec:
+        return _Spec(self.nx, self.ny, self.nz, (C.c_float * 3)(*self.vmin),
+                     (C.c_float * 3)(*self.vmax), self.R)
+
+    def count(self) -> int:
+        n = C.c_int(0)
+        _check(lib().gd_grid_count(C.byref(self._c()), C.byref(n)))
+        return n.value
+
+    def fill(self):
+        """Host grid: dict of numpy arrays u, v, w, ui, vi, wi, steps."""
+        import numpy as np
+        n = self.count()
+        out = {"u": np.zeros(self.nx, np.float32), "v": np.zeros(self.ny, np.float32),
+               "w": np.zeros(self.nz, np.float32), "ui": np.zeros(n, np.int32),
+               "vi": np.zeros(n, np.int32), "wi": np.zeros(n, np.int32),
+               "steps": np.zeros(4, np.float32)}
+        _check(lib().gd_grid_fill(C.byref(self._c()), *(out[k].ctypes.data for k in
+                                                        ("u", "v", "w", "ui", "vi", "wi", "steps"))))
+        return out
+
+
+class Context:
+    """Device tables for one velocity grid and the collision operator on it."""
+
+    def __init__(self, spec: GridSpec, device: int = 0):
+        self.spec = spec
+        self._h = C.c_void_p()
+        _check(lib().gd_ctx_create(C.byref(spec._c()), int(device), C.byref(self._h)))
+        self.device = device
+        self.info = self._info()
+        self.n_pnt = self.info["n_pnt"]
+
+    def _info(self) -> dict:
+        inf = _Info()
+        _check(lib().gd_ctx_info(self._h, C.byref(inf)))
+        return {k: getattr(inf, k) for k, _ in _Info._fields_}
+
+    def close(self):
+        if self._h:
+            lib().gd_ctx_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # tables -----------------------------------------------------------------
+    def export_tables(self, b=None, a=None, stream=None):
+        _check(lib().gd_export_tables(self._h, _ptr(b), _ptr(a), _stream(stream)))
+
+    def correction_basis(self, basis, stream=None):
+        _check(lib().gd_correction_basis(self._h, _ptr(basis), _stream(stream)))
+
+    # operator ---------------------------------------------------------------
+    def collision(self, f, ncells, ld, nu=None, gain=None, stream=None):
+        _check(lib().gd_collision(self._h, _ptr(f), int(ncells), int(ld), _ptr(nu), _ptr(gain),
+                                  _stream(stream)))
+
+    def project(self, f, nu, gain, ncells, ld, nu_corr=None, q=None, x=None, stream=None):
+        _check(lib().gd_project(self._h, _ptr(f), _ptr(nu), _ptr(gain), int(ncells), int(ld),
+                                _ptr(nu_corr), _ptr(q), _ptr(x), _stream(stream)))
+
+    def relax(self, f, nu_corr, gain, ncells, ld, mode, param, time=None, dt=None, stream=None):
+        _check(lib().gd_relax(self._h, _ptr(f), _ptr(nu_corr), _ptr(gain), int(ncells), int(ld),
+                              int(mode), float(param), _ptr(time), _ptr(dt), _stream(stream)))
+
+    def step(self, f, ncells, ld, mode, param, nu=None, gain=None, q=None, m5=None, time=None,
+             dt=None, stream=None):
+        _check(lib().gd_step(self._h, _ptr(f), int(ncells), int(ld), int(mode), float(param),
+                             _ptr(nu), _ptr(gain), _ptr(q), _ptr(m5), _ptr(time), _ptr(dt),
+                             _stream(stream)))
+
+    def moments(self, f, ncells, ld, m5, stream=None):
+        _check(lib().gd_moments(self._h, _ptr(f), int(ncells), int(ld), _ptr(m5), _stream(stream)))

@@ -1,0 +1,470 @@
+// gd_capi.cu -- the extern "C" boundary (include/gpu_determ.h).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "gd_internal.h"
+
+struct gd_ctx {
+    gd::Context c;
+};
+
+namespace gd {
+
+namespace {
+thread_local std::string g_last_error;
+
+// Makes the context's device current for the duration of a call and restores
+// the caller's device afterwards.
+struct DeviceGuard {
+    int prev = -1;
+    bool ok = true;
+    explicit DeviceGuard(int dev)
+    {
+        if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+        if (prev != dev) ok = cudaSetDevice(dev) == cudaSuccess;
+    }
+    ~DeviceGuard()
+    {
+        int cur = -1;
+        if (prev >= 0 && cudaGetDevice(&cur) == cudaSuccess && cur != prev) cudaSetDevice(prev);
+    }
+};
+
+int check_spec(const gd_grid_spec *s)
+{
+    if (!s) return set_error(GD_ERR_INVALID_ARG, "grid spec is NULL");
+    const int n[3] = {s->nx, s->ny, s->nz};
+    for (int a = 0; a < 3; a++) {
+        if (n[a] < 2 || (n[a] & 1)) return set_error(GD_ERR_INVALID_ARG, "grid sizes must be even and >= 2");
+        if (n[a] > 64) return set_error(GD_ERR_UNSUPPORTED, "grid sizes above 64 per axis are not supported");
+        if (!(s->vmax[a] > s->vmin[a]) || !std::isfinite(s->vmin[a]) || !std::isfinite(s->vmax[a]))
+            return set_error(GD_ERR_INVALID_ARG, "velocity bounds must be finite with vmin < vmax");
+    }
+    if (!std::isfinite(s->R)) return set_error(GD_ERR_INVALID_ARG, "sphere radius must be finite");
+    return GD_OK;
+}
+
+int check_batch(const gd_ctx *ctx, const void *f, int ncells, int ld)
+{
+    if (!ctx) return set_error(GD_ERR_INVALID_ARG, "context is NULL");
+    if (!f) return set_error(GD_ERR_INVALID_ARG, "distribution pointer is NULL");
+    if (ncells < 1) return set_error(GD_ERR_INVALID_ARG, "ncells must be >= 1");
+    if (ld < ncells) return set_error(GD_ERR_INVALID_ARG, "ld must be >= ncells");
+    if ((int64_t)ld * ctx->c.d.n_pnt > ((int64_t)1 << 40))
+        return set_error(GD_ERR_UNSUPPORTED, "batch too large");
+    return GD_OK;
+}
+
+// Cumulative per-s work estimate (pair products, weight-row visits, scatter)
+// in linear s order; used to cut s into chunks of equal work.
+void build_s_schedule(Context &c, const std::vector<int> &row_off)
+{
+    const Dims &d = c.d;
+    // per parity class: inclusive 3-D prefix sums of row lengths over the class box
+    std::vector<int64_t> pref((size_t)8 * d.nclass, 0);
+    for (int p = 0; p < 8; p++) {
+        const int px = p & 1, py = (p >> 1) & 1, pz = (p >> 2) & 1;
+        int64_t *P = pref.data() + (size_t)p * d.nclass;
+        for (int a2 = 0; a2 < d.hx; a2++)
+            for (int b2 = 0; b2 < d.hy; b2++)
+                for (int c2 = 0; c2 < d.hz; c2++) {
+                    const int gx = 2 * a2 + px, gy = 2 * b2 + py, gz = 2 * c2 + pz;
+                    const int gbox = (gx * d.ny + gy) * d.nz + gz;
+                    int64_t v = row_off[gbox + 1] - row_off[gbox];
+                    auto at = [&](int x, int y, int z) -> int64_t {
+                        return (x < 0 || y < 0 || z < 0) ? 0 : P[(x * d.hy + y) * d.hz + z];
+                    };
+                    v += at(a2 - 1, b2, c2) + at(a2, b2 - 1, c2) + at(a2, b2, c2 - 1) -
+                         at(a2 - 1, b2 - 1, c2) - at(a2 - 1, b2, c2 - 1) - at(a2, b2 - 1, c2 - 1) +
+                         at(a2 - 1, b2 - 1, c2 - 1);
+                    P[(a2 * d.hy + b2) * d.hz + c2] = v;
+                }
+    }
+    c.s_work_prefix.assign(d.ns + 1, 0);
+    int64_t acc = 0, pairs = 0, visits = 0;
+    for (int sx = 0; sx < d.sx; sx++)
+        for (int sy = 0; sy < d.sy; sy++)
+            for (int sz = 0; sz < d.sz; sz++) {
+                const int64_t sl = ((int64_t)sx * d.sy + sy) * d.sz + sz;
+                const int Dx = std::min(sx, 2 * d.nx - 2 - sx), Dy = std::min(sy, 2 * d.ny - 2 - sy),
+                          Dz = std::min(sz, 2 * d.nz - 2 - sz);
+                const int64_t nB = (int64_t)((Dx >> 1) + 1) * ((Dy >> 1) + 1) * ((Dz >> 1) + 1);
+                const int p = (sx & 1) | ((sy & 1) << 1) | ((sz & 1) << 2);
+                const int64_t rows =
+                    pref[(size_t)p * d.nclass + ((Dx >> 1) * d.hy + (Dy >> 1)) * d.hz + (Dz >> 1)];
+                c.s_work_prefix[sl] = acc;
+                acc += 12 * nB + rows;
+                pairs += nB;
+                visits += rows;
+            }
+    c.s_work_prefix[d.ns] = acc;
+    c.pair_products = pairs;
+    c.contraction_terms = visits;
+}
+
+// Exact number of (weight, pair product) terms per cell-eval: for every s the
+// entries of the rows g in B(D(s)) whose n also lies in B(D(s)).  Depends on s
+// only through D(s); each D stands for prod_a (D_a == n_a - 1 ? 1 : 2) sums s.
+int exact_contraction_terms(Context &c, int64_t *out)
+{
+    const Dims &d = c.d;
+    std::vector<int> off(d.nxyz + 1);
+    std::vector<WEntry> rows(c.n_entries + 1);
+    GD_CUDA(cudaMemcpy(off.data(), c.d_list_off, sizeof(int) * (d.nxyz + 1), cudaMemcpyDeviceToHost));
+    GD_CUDA(cudaMemcpy(rows.data(), c.d_list, sizeof(WEntry) * c.n_entries, cudaMemcpyDeviceToHost));
+    int64_t total = 0;
+    for (int Dx = 0; Dx < d.nx; Dx++)
+        for (int Dy = 0; Dy < d.ny; Dy++)
+            for (int Dz = 0; Dz < d.nz; Dz++) {
+                const int mult = (Dx == d.nx - 1 ? 1 : 2) * (Dy == d.ny - 1 ? 1 : 2) * (Dz == d.nz - 1 ? 1 : 2);
+                const uint32_t hx2 = Dx >> 1, hy2 = Dy >> 1, hz2 = Dz >> 1;
+                int64_t t = 0;
+                for (int gx = Dx & 1; gx <= Dx; gx += 2)
+                    for (int gy = Dy & 1; gy <= Dy; gy += 2)
+                        for (int gz = Dz & 1; gz <= Dz; gz += 2) {
+                            const int gbox = (gx * d.ny + gy) * d.nz + gz;
+                            for (int e = off[gbox]; e < off[gbox + 1]; e++) {
+                                const uint32_t m = rows[e].meta;
+                                t += ((m >> 15) & 31) <= hx2 && ((m >> 20) & 31) <= hy2 && ((m >> 25) & 31) <= hz2;
+                            }
+                        }
+                total += t * mult;
+            }
+    *out = total;
+    return GD_OK;
+}
+
+}  // namespace
+
+int set_error(int code, const std::string &msg)
+{
+    g_last_error = msg;
+    return code;
+}
+
+int cuda_error(cudaError_t e, const char *what)
+{
+    std::string m = std::string(what) + ": " + cudaGetErrorName(e) + " (" + cudaGetErrorString(e) + ")";
+    return set_error(e == cudaErrorMemoryAllocation ? GD_ERR_OUT_OF_MEMORY : GD_ERR_CUDA, m);
+}
+
+int ensure_scratch(Context &c, size_t bytes)
+{
+    if (c.scratch.bytes >= bytes) return GD_OK;
+    if (c.scratch.ptr) {
+        GD_CUDA(cudaDeviceSynchronize());
+        GD_CUDA(cudaFree(c.scratch.ptr));
+        c.scratch.ptr = nullptr;
+        c.scratch.bytes = 0;
+    }
+    const size_t grow = bytes + bytes / 8;
+    cudaError_t e = cudaMalloc(&c.scratch.ptr, grow);
+    if (e != cudaSuccess) {
+        c.scratch.ptr = nullptr;
+        return cuda_error(e, "scratch allocation");
+    }
+    c.scratch.bytes = grow;
+    return GD_OK;
+}
+
+static void destroy_context(Context &c)
+{
+    cudaFree(c.d_cmap);
+    cudaFree(c.d_nodes);
+    cudaFree(c.d_b);
+    cudaFree(c.d_phi);
+    cudaFree(c.d_list_off);
+    cudaFree(c.d_list);
+    cudaFree(c.d_s_bounds);
+    cudaFree(c.d_reduce);
+    cudaFree(c.scratch.ptr);
+}
+
+static int create_context(Context &c, const gd_grid_spec &spec, int device)
+{
+    c.spec = spec;
+    c.device = device;
+    Dims &d = c.d;
+    d.nx = spec.nx;
+    d.ny = spec.ny;
+    d.nz = spec.nz;
+    d.nyz = d.ny * d.nz;
+    d.nxyz = d.nx * d.nyz;
+    d.hx = d.nx / 2;
+    d.hy = d.ny / 2;
+    d.hz = d.nz / 2;
+    d.nclass = d.hx * d.hy * d.hz;
+    d.sx = 2 * d.nx - 1;
+    d.sy = 2 * d.ny - 1;
+    d.sz = 2 * d.nz - 1;
+    d.ns = (int64_t)d.sx * d.sy * d.sz;
+    const int np = grid_count(spec);
+    if (np < 1) return set_error(GD_ERR_INVALID_ARG, "no lattice node lies inside the sphere");
+    if (np > 32767) return set_error(GD_ERR_UNSUPPORTED, "more than 32767 in-sphere nodes");
+    c.u.resize(d.nx);
+    c.v.resize(d.ny);
+    c.w.resize(d.nz);
+    c.ui.resize(np);
+    c.vi.resize(np);
+    c.wi.resize(np);
+    float steps[4];
+    d.n_pnt = grid_fill(spec, c.u.data(), c.v.data(), c.w.data(), c.ui.data(), c.vi.data(), c.wi.data(), steps);
+    d.du = steps[0];
+    d.dv = steps[1];
+    d.dw = steps[2];
+    d.d3v = steps[3];
+
+    c.cmap.assign(d.nxyz, -1);
+    std::vector<int16_t> cmap16(d.nxyz, -1);
+    std::vector<uint32_t> nodes(d.n_pnt);
+    std::vector<double> phi((size_t)5 * d.n_pnt);
+    for (int p = 0; p < d.n_pnt; p++) {
+        const int bi = (c.ui[p] * d.ny + c.vi[p]) * d.nz + c.wi[p];
+        c.cmap[bi] = p;
+        cmap16[bi] = (int16_t)p;
+        nodes[p] = (uint32_t)c.ui[p] | ((uint32_t)c.vi[p] << 10) | ((uint32_t)c.wi[p] << 20);
+        const double xu = c.u[c.ui[p]], xv = c.v[c.vi[p]], xw = c.w[c.wi[p]];
+        phi[p] = 1.0;
+        phi[(size_t)d.n_pnt + p] = xu;
+        phi[(size_t)2 * d.n_pnt + p] = xv;
+        phi[(size_t)3 * d.n_pnt + p] = xw;
+        phi[(size_t)4 * d.n_pnt + p] = xu * xu + xv * xv + xw * xw;
+    }
+
+    int ndev = 0;
+    GD_CUDA(cudaGetDeviceCount(&ndev));
+    if (device < 0 || device >= ndev) return set_error(GD_ERR_INVALID_ARG, "no such CUDA device");
+    DeviceGuard guard(device);
+    if (!guard.ok) return set_error(GD_ERR_CUDA, "cudaSetDevice failed");
+    GD_CUDA(cudaDeviceGetAttribute(&c.sm_count, cudaDevAttrMultiProcessorCount, device));
+    cudaStream_t st = nullptr;
+    GD_CUDA(cudaMalloc(&c.d_cmap, sizeof(int16_t) * d.nxyz));
+    GD_CUDA(cudaMalloc(&c.d_nodes, sizeof(uint32_t) * d.n_pnt));
+    GD_CUDA(cudaMalloc(&c.d_phi, sizeof(double) * 5 * d.n_pnt));
+    GD_CUDA(cudaMalloc(&c.d_b, sizeof(float) * d.nxyz));
+    GD_CUDA(cudaMalloc(&c.d_reduce, sizeof(float) * 512));
+    GD_CUDA(cudaMemcpy(c.d_cmap, cmap16.data(), sizeof(int16_t) * d.nxyz, cudaMemcpyHostToDevice));
+    GD_CUDA(cudaMemcpy(c.d_nodes, nodes.data(), sizeof(uint32_t) * d.n_pnt, cudaMemcpyHostToDevice));
+    GD_CUDA(cudaMemcpy(c.d_phi, phi.data(), sizeof(double) * 5 * d.n_pnt, cudaMemcpyHostToDevice));
+
+    // analytic weights: dense FP64-built table (transient), compacted to rows
+    const size_t na = (size_t)d.hx * d.nx * d.hy * d.hz * d.nyz;
+    float *a_dense = nullptr;
+    GD_CUDA(cudaMalloc(&a_dense, sizeof(float) * na));
+    int rc = launch_dense_tables(d, c.d_b, a_dense, st);
+    if (!rc) rc = build_weight_rows(c, a_dense, st);
+    cudaFree(a_dense);
+    if (rc) return rc;
+    std::vector<int> row_off(d.nxyz + 1);
+    GD_CUDA(cudaMemcpy(row_off.data(), c.d_list_off, sizeof(int) * (d.nxyz + 1), cudaMemcpyDeviceToHost));
+    build_s_schedule(c, row_off);
+    // scatter updates: distinct sign patterns of g whose target lies in the sphere
+    int64_t sc = 0;
+    for (int sx = 0; sx < d.sx; sx++)
+        for (int sy = 0; sy < d.sy; sy++)
+            for (int sz = 0; sz < d.sz; sz++) {
+                const int Dx = std::min(sx, 2 * d.nx - 2 - sx), Dy = std::min(sy, 2 * d.ny - 2 - sy),
+                          Dz = std::min(sz, 2 * d.nz - 2 - sz);
+                for (int gx = sx & 1; gx <= Dx; gx += 2)
+                    for (int gy = sy & 1; gy <= Dy; gy += 2)
+                        for (int gz = sz & 1; gz <= Dz; gz += 2)
+                            for (int sg = 0; sg < 8; sg++) {
+                                if (((sg & 1) && gx == 0) || ((sg & 2) && gy == 0) || ((sg & 4) && gz == 0)) continue;
+                                const int ix = (sx + ((sg & 1) ? -gx : gx)) >> 1;
+                                const int iy = (sy + ((sg & 2) ? -gy : gy)) >> 1;
+                                const int iz = (sz + ((sg & 4) ? -gz : gz)) >> 1;
+                                sc += c.cmap[(ix * d.ny + iy) * d.nz + iz] >= 0;
+                            }
+            }
+    c.scatter_terms = sc;
+    GD_CUDA(cudaDeviceSynchronize());
+    return GD_OK;
+}
+
+}  // namespace gd
+
+using gd::set_error;
+
+extern "C" {
+
+int gd_version(void) { return 100; }
+
+const char *gd_last_error(void) { return gd::g_last_error.c_str(); }
+
+int gd_grid_count(const gd_grid_spec *spec, int *n_pnt)
+{
+    int rc = gd::check_spec(spec);
+    if (rc) return rc;
+    if (!n_pnt) return set_error(GD_ERR_INVALID_ARG, "n_pnt is NULL");
+    *n_pnt = gd::grid_count(*spec);
+    return GD_OK;
+}
+
+int gd_grid_fill(const gd_grid_spec *spec, float *u, float *v, float *w, int *ui, int *vi, int *wi,
+                 float *steps)
+{
+    int rc = gd::check_spec(spec);
+    if (rc) return rc;
+    gd::grid_fill(*spec, u, v, w, ui, vi, wi, steps);
+    return GD_OK;
+}
+
+int gd_ctx_create(const gd_grid_spec *spec, int device, gd_ctx **out)
+{
+    if (!out) return set_error(GD_ERR_INVALID_ARG, "out is NULL");
+    *out = nullptr;
+    int rc = gd::check_spec(spec);
+    if (rc) return rc;
+    gd_ctx *ctx = new (std::nothrow) gd_ctx();
+    if (!ctx) return set_error(GD_ERR_OUT_OF_MEMORY, "host allocation failed");
+    rc = gd::create_context(ctx->c, *spec, device);
+    if (rc) {
+        gd::DeviceGuard g(device);
+        gd::destroy_context(ctx->c);
+        delete ctx;
+        return rc;
+    }
+    *out = ctx;
+    return GD_OK;
+}
+
+int gd_ctx_destroy(gd_ctx *ctx)
+{
+    if (!ctx) return GD_OK;
+    {
+        gd::DeviceGuard g(ctx->c.device);
+        gd::destroy_context(ctx->c);
+    }
+    delete ctx;
+    return GD_OK;
+}
+
+int gd_ctx_info(const gd_ctx *ctx, gd_info *out)
+{
+    if (!ctx || !out) return set_error(GD_ERR_INVALID_ARG, "NULL argument");
+    if (!ctx->c.contraction_exact) {
+        gd::DeviceGuard g(ctx->c.device);
+        gd::Context &mc = const_cast<gd_ctx *>(ctx)->c;
+        int rc = gd::exact_contraction_terms(mc, &mc.contraction_terms);
+        if (rc) return rc;
+        mc.contraction_exact = true;
+    }
+    const gd::Dims &d = ctx->c.d;
+    out->nx = d.nx;
+    out->ny = d.ny;
+    out->nz = d.nz;
+    out->n_pnt = d.n_pnt;
+    out->du = d.du;
+    out->dv = d.dv;
+    out->dw = d.dw;
+    out->d3v = d.d3v;
+    out->nonzero_weights = ctx->c.n_entries;
+    out->table_a_elems = (int64_t)d.hx * d.nx * d.hy * d.hz * d.nyz;
+    out->pair_products = ctx->c.pair_products;
+    out->contraction_terms = ctx->c.contraction_terms;
+    out->scatter_terms = ctx->c.scatter_terms;
+    return GD_OK;
+}
+
+int gd_export_tables(gd_ctx *ctx, float *b, float *a, gd_stream stream)
+{
+    if (!ctx) return set_error(GD_ERR_INVALID_ARG, "context is NULL");
+    gd::DeviceGuard g(ctx->c.device);
+    return gd::launch_dense_tables(ctx->c.d, b, a, (cudaStream_t)stream);
+}
+
+int gd_correction_basis(gd_ctx *ctx, float *basis, gd_stream stream)
+{
+    if (!ctx || !basis) return set_error(GD_ERR_INVALID_ARG, "NULL argument");
+    gd::DeviceGuard g(ctx->c.device);
+    return gd::run_basis(ctx->c, basis, (cudaStream_t)stream);
+}
+
+int gd_collision(gd_ctx *ctx, const float *f, int ncells, int ld, float *nu, float *gain, gd_stream stream)
+{
+    int rc = gd::check_batch(ctx, f, ncells, ld);
+    if (rc) return rc;
+    gd::DeviceGuard g(ctx->c.device);
+    cudaStream_t st = (cudaStream_t)stream;
+    if (nu && (rc = gd::run_loss(ctx->c, f, ncells, ld, nu, st))) return rc;
+    if (gain && (rc = gd::run_gain(ctx->c, f, ncells, ld, gain, st))) return rc;
+    return GD_OK;
+}
+
+int gd_project(gd_ctx *ctx, const float *f, const float *nu, const float *gain, int ncells, int ld,
+               float *nu_corr, double *q, double *x, gd_stream stream)
+{
+    int rc = gd::check_batch(ctx, f, ncells, ld);
+    if (rc) return rc;
+    if (!nu || !gain) return set_error(GD_ERR_INVALID_ARG, "nu and gain are required");
+    gd::DeviceGuard g(ctx->c.device);
+    return gd::run_project(ctx->c, f, nu, gain, ncells, ld, nu_corr, q, x, 0, 0.f, nullptr, nullptr,
+                           (cudaStream_t)stream);
+}
+
+int gd_relax(gd_ctx *ctx, float *f, const float *nu_corr, const float *gain, int ncells, int ld, int mode,
+             float param, float *time_dev, float *dt_dev, gd_stream stream)
+{
+    int rc = gd::check_batch(ctx, f, ncells, ld);
+    if (rc) return rc;
+    if (!nu_corr || !gain) return set_error(GD_ERR_INVALID_ARG, "nu and gain are required");
+    if (mode != GD_DT_COURANT && mode != GD_DT_FIXED) return set_error(GD_ERR_INVALID_ARG, "unknown dt mode");
+    if (!(param > 0.f) || !std::isfinite(param)) return set_error(GD_ERR_INVALID_ARG, "dt parameter must be > 0");
+    gd::DeviceGuard g(ctx->c.device);
+    return gd::run_relax(ctx->c, f, nu_corr, gain, ncells, ld, mode, param, time_dev, dt_dev,
+                         (cudaStream_t)stream);
+}
+
+int gd_step(gd_ctx *ctx, float *f, int ncells, int ld, int mode, float param, float *nu, float *gain,
+            double *q, double *m5, float *time_dev, float *dt_dev, gd_stream stream)
+{
+    int rc = gd::check_batch(ctx, f, ncells, ld);
+    if (rc) return rc;
+    if (mode != GD_DT_COURANT && mode != GD_DT_FIXED) return set_error(GD_ERR_INVALID_ARG, "unknown dt mode");
+    if (!(param > 0.f) || !std::isfinite(param)) return set_error(GD_ERR_INVALID_ARG, "dt parameter must be > 0");
+    gd::DeviceGuard g(ctx->c.device);
+    gd::Context &c = ctx->c;
+    cudaStream_t st = (cudaStream_t)stream;
+    // step buffers: nu, gain (FP32) and Q (FP64) unless the caller provides them
+    const size_t n = (size_t)c.d.n_pnt * ld;
+    float *nu_b = nu, *gain_b = gain;
+    double *q_b = q;
+    std::vector<void *> tmp;
+    auto alloc = [&](size_t bytes) -> void * {
+        void *p = nullptr;
+        if (cudaMallocAsync(&p, bytes, st) != cudaSuccess) return nullptr;
+        tmp.push_back(p);
+        return p;
+    };
+    if (!nu_b) nu_b = static_cast<float *>(alloc(n * sizeof(float)));
+    if (!gain_b) gain_b = static_cast<float *>(alloc(n * sizeof(float)));
+    if (!q_b) q_b = static_cast<double *>(alloc(n * sizeof(double)));
+    if (!nu_b || !gain_b || !q_b) {
+        for (void *p : tmp) cudaFreeAsync(p, st);
+        return set_error(GD_ERR_OUT_OF_MEMORY, "step buffers");
+    }
+    rc = gd::run_loss(c, f, ncells, ld, nu_b, st);
+    if (!rc) rc = gd::run_gain(c, f, ncells, ld, gain_b, st);
+    if (!rc) rc = gd::run_project(c, f, nu_b, gain_b, ncells, ld, nu_b, q_b, nullptr, 0, 0.f, nullptr, m5, st);
+    if (!rc) rc = gd::run_relax_q(c, f, nu_b, gain_b, q_b, ncells, ld, mode, param, time_dev, dt_dev, st);
+    for (void *p : tmp) cudaFreeAsync(p, st);
+    return rc;
+}
+
+int gd_moments(gd_ctx *ctx, const float *f, int ncells, int ld, double *m5, gd_stream stream)
+{
+    int rc = gd::check_batch(ctx, f, ncells, ld);
+    if (rc) return rc;
+    if (!m5) return set_error(GD_ERR_INVALID_ARG, "m5 is NULL");
+    gd::DeviceGuard g(ctx->c.device);
+    return gd::run_moments(ctx->c, f, ncells, ld, m5, (cudaStream_t)stream);
+}
+
+}  // extern "C"

@@ -1,0 +1,248 @@
+// gd_gain.cu -- gain term of the hard-sphere collision integral (sm_103a).
+//
+// The reference sums, for each output node i, over partners i1 and
+// post-collision offsets n (collision_integral.cu:75-188, host loop :637-648):
+//   I_i = sum_{i1} sum_n w(|i - i1|, n) P(i + i1, n),
+//   P(s, n) = f(lx,ly,lz) f(l1x,l1y,l1z) + f(lx,l1y,l1z) f(l1x,ly,lz)
+//           + f(lx,ly,l1z) f(l1x,l1y,lz) + f(lx,l1y,lz)  f(l1x,ly,l1z),
+//   l = (s + n)/2, l1 = (s - n)/2 per axis, n of the parity of s.
+// The pair product P depends only on the pair sum s = i + i1 and on n, so this
+// kernel walks s instead of i:
+//   1. P_s[n] for every n of the class box B(D(s)), D_a = min(s_a, 2 n_a - 2 - s_a)
+//      (exactly the n whose l, l1 stay in the box) -> shared memory,
+//   2. C_s[g] = sum_n w(g, n) P_s[n] for every g in B(D(s)) (the |2i - s| of the
+//      outputs that have a partner in the box),
+//   3. C_s[g] is added to the outputs i = (s +- g)/2 (one per sign pattern).
+// Each P is formed once per (s, n) and reused by every output on its collision
+// shell instead of being regathered per (i, i1, n).
+//
+// Parallel layout: lane = cell (CB cells per row, 32/CB rows per warp), one
+// CTA per (cell block, chunk of s).  A chunk owns its own partial output
+// buffer; within one s all targets (s +- g)/2 are distinct and successive s
+// are separated by barriers, so every partial sum is formed in a fixed
+// order.  A second kernel adds the chunk partials in chunk order.  No atomics:
+// results are bitwise reproducible.
+#include "gd_internal.h"
+
+#include <algorithm>
+#include <cstdio>
+
+namespace gd {
+namespace {
+
+constexpr int kThreads = 512;
+
+struct GainArgs {
+    Dims d;
+    const float *f;
+    int ld, ncells, cells_pad;
+    const int16_t *cmap;
+    const int *list_off;
+    const WEntry *list;
+    const int *s_bounds;
+    float *part;  // [chunk][n_pnt][cells_pad]
+};
+
+template <int CB>
+__global__ void __launch_bounds__(kThreads, 1) gain_pair_kernel(GainArgs a)
+{
+    constexpr int G = 32 / CB;  // item rows per warp
+    extern __shared__ __align__(16) unsigned char smem[];
+    const Dims &d = a.d;
+    int16_t *cmap = reinterpret_cast<int16_t *>(smem);
+    float *P = reinterpret_cast<float *>(smem + ((d.nxyz * 2 + 15) & ~15));
+
+    for (int t = threadIdx.x; t < d.nxyz; t += blockDim.x) cmap[t] = a.cmap[t];
+
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    const int cl = lane % CB, grp = lane / CB;
+    const int cell = blockIdx.x * CB + cl;
+    const bool live = cell < a.ncells;
+    const float *fcol = a.f + (live ? cell : 0);
+    const int chunk = blockIdx.y;
+    float *part = a.part + (size_t)chunk * d.n_pnt * a.cells_pad + blockIdx.x * CB + cl;
+    const int item0 = warp * G + grp, istep = nwarps * G;
+    __syncthreads();
+
+    const int s_begin = a.s_bounds[chunk], s_end = a.s_bounds[chunk + 1];
+    for (int sl = s_begin; sl < s_end; sl++) {
+        const int sz = sl % d.sz, sy = (sl / d.sz) % d.sy, sx = sl / (d.sz * d.sy);
+        const int Dx = min(sx, 2 * d.nx - 2 - sx), Dy = min(sy, 2 * d.ny - 2 - sy),
+                  Dz = min(sz, 2 * d.nz - 2 - sz);
+        const int ex = (Dx >> 1) + 1, ey = (Dy >> 1) + 1, ez = (Dz >> 1) + 1;
+        const int px = sx & 1, py = sy & 1, pz = sz & 1;
+        const int nB = ex * ey * ez;
+
+        // 1. pair products P_s[n] -------------------------------------------
+        for (int t = item0; t < nB; t += istep) {
+            const int c2 = t % ez, b2 = (t / ez) % ey, a2 = t / (ez * ey);
+            const int nxv = 2 * a2 + px, nyv = 2 * b2 + py, nzv = 2 * c2 + pz;
+            const int lx = (sx + nxv) >> 1, l1x = (sx - nxv) >> 1;
+            const int ly = (sy + nyv) >> 1, l1y = (sy - nyv) >> 1;
+            const int lz = (sz + nzv) >> 1, l1z = (sz - nzv) >> 1;
+            const int X0 = lx * d.nyz, X1 = l1x * d.nyz;
+            const int Y0 = ly * d.nz, Y1 = l1y * d.nz;
+            const int k0 = cmap[X0 + Y0 + lz], k1 = cmap[X1 + Y1 + l1z];
+            const int k2 = cmap[X0 + Y1 + l1z], k3 = cmap[X1 + Y0 + lz];
+            const int k4 = cmap[X0 + Y0 + l1z], k5 = cmap[X1 + Y1 + lz];
+            const int k6 = cmap[X0 + Y1 + lz], k7 = cmap[X1 + Y0 + l1z];
+            const int ld = a.ld;
+            const float f0 = (k0 >= 0 && live) ? __ldg(fcol + (size_t)k0 * ld) : 0.f;
+            const float f1 = (k1 >= 0 && live) ? __ldg(fcol + (size_t)k1 * ld) : 0.f;
+            const float f2 = (k2 >= 0 && live) ? __ldg(fcol + (size_t)k2 * ld) : 0.f;
+            const float f3 = (k3 >= 0 && live) ? __ldg(fcol + (size_t)k3 * ld) : 0.f;
+            const float f4 = (k4 >= 0 && live) ? __ldg(fcol + (size_t)k4 * ld) : 0.f;
+            const float f5 = (k5 >= 0 && live) ? __ldg(fcol + (size_t)k5 * ld) : 0.f;
+            const float f6 = (k6 >= 0 && live) ? __ldg(fcol + (size_t)k6 * ld) : 0.f;
+            const float f7 = (k7 >= 0 && live) ? __ldg(fcol + (size_t)k7 * ld) : 0.f;
+            const float t1 = __fmaf_rn(f0, f1, f2 * f3);
+            const float t2 = __fmaf_rn(f4, f5, f6 * f7);
+            const int nc = (a2 * d.hy + b2) * d.hz + c2;
+            P[nc * CB + cl] = t1 + t2;
+        }
+        __syncthreads();
+
+        // 2./3. contraction with the weight rows and scatter to outputs -------
+        for (int t = item0; t < nB; t += istep) {
+            const int c2 = t % ez, b2 = (t / ez) % ey, a2 = t / (ez * ey);
+            const int gx = 2 * a2 + px, gy = 2 * b2 + py, gz = 2 * c2 + pz;
+            // targets i = (s +- g)/2, distinct sign patterns only
+            int tgt[8];
+            float old[8];
+            int nt = 0;
+#pragma unroll
+            for (int sg = 0; sg < 8; sg++) {
+                const int sgx = (sg & 1) ? -1 : 1, sgy = (sg & 2) ? -1 : 1, sgz = (sg & 4) ? -1 : 1;
+                const bool dup = (gx == 0 && sgx < 0) || (gy == 0 && sgy < 0) || (gz == 0 && sgz < 0);
+                const int ix = (sx + sgx * gx) >> 1, iy = (sy + sgy * gy) >> 1, iz = (sz + sgz * gz) >> 1;
+                const int k = dup ? -1 : cmap[ix * d.nyz + iy * d.nz + iz];
+                tgt[sg] = k;
+                old[sg] = 0.f;
+                if (k >= 0) {
+                    nt++;
+                    old[sg] = part[(size_t)k * a.cells_pad];
+                }
+            }
+            if (nt == 0) continue;
+            const int gbox = (gx * d.ny + gy) * d.nz + gz;
+            const int e0 = __ldg(a.list_off + gbox), e1 = __ldg(a.list_off + gbox + 1);
+            const uint32_t hx2 = (uint32_t)(Dx >> 1), hy2 = (uint32_t)(Dy >> 1), hz2 = (uint32_t)(Dz >> 1);
+            float acc0 = 0.f, acc1 = 0.f;
+            int e = e0;
+            for (; e + 1 < e1; e += 2) {
+                const uint2 r0 = __ldg(reinterpret_cast<const uint2 *>(a.list + e));
+                const uint2 r1 = __ldg(reinterpret_cast<const uint2 *>(a.list + e + 1));
+                const uint32_t m0 = r0.x, m1 = r1.x;
+                const bool in0 = ((m0 >> 15) & 31) <= hx2 && ((m0 >> 20) & 31) <= hy2 && ((m0 >> 25) & 31) <= hz2;
+                const bool in1 = ((m1 >> 15) & 31) <= hx2 && ((m1 >> 20) & 31) <= hy2 && ((m1 >> 25) & 31) <= hz2;
+                if (in0) acc0 = __fmaf_rn(__uint_as_float(r0.y), P[(m0 & 0x7fff) * CB + cl], acc0);
+                if (in1) acc1 = __fmaf_rn(__uint_as_float(r1.y), P[(m1 & 0x7fff) * CB + cl], acc1);
+            }
+            if (e < e1) {
+                const uint2 r0 = __ldg(reinterpret_cast<const uint2 *>(a.list + e));
+                const uint32_t m0 = r0.x;
+                const bool in0 = ((m0 >> 15) & 31) <= hx2 && ((m0 >> 20) & 31) <= hy2 && ((m0 >> 25) & 31) <= hz2;
+                if (in0) acc0 = __fmaf_rn(__uint_as_float(r0.y), P[(m0 & 0x7fff) * CB + cl], acc0);
+            }
+            const float acc = acc0 + acc1;
+            if (live) {
+#pragma unroll
+                for (int sg = 0; sg < 8; sg++)
+                    if (tgt[sg] >= 0) part[(size_t)tgt[sg] * a.cells_pad] = old[sg] + acc;
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// gain[node][c] = sum over chunks of the partials, in chunk order.
+__global__ void gain_reduce_kernel(const float *__restrict__ part, int nchunks, int n_pnt,
+                                   int cells_pad, int ncells, int ld, float *__restrict__ gain)
+{
+    const int64_t total = (int64_t)n_pnt * ncells;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total;
+         t += (int64_t)gridDim.x * blockDim.x) {
+        const int node = (int)(t / ncells), c = (int)(t % ncells);
+        const float *p = part + (size_t)node * cells_pad + c;
+        float s = 0.f;
+        for (int k = 0; k < nchunks; k++) s += p[(size_t)k * n_pnt * cells_pad];
+        gain[(size_t)node * ld + c] = s;
+    }
+}
+
+size_t gain_smem_bytes(const Dims &d, int cb)
+{
+    return (size_t)((d.nxyz * 2 + 15) & ~15) + (size_t)d.nclass * cb * sizeof(float);
+}
+
+}  // namespace
+
+int run_gain(Context &c, const float *f, int ncells, int ld, float *gain, cudaStream_t st)
+{
+    const Dims &d = c.d;
+    int max_smem = 0;
+    GD_CUDA(cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, c.device));
+    int cb = 32;
+    while (cb > 4 && gain_smem_bytes(d, cb) > (size_t)max_smem) cb >>= 1;
+    if (gain_smem_bytes(d, cb) > (size_t)max_smem)
+        return set_error(GD_ERR_UNSUPPORTED, "velocity grid too large for the gain kernel's shared memory");
+    const size_t smem = gain_smem_bytes(d, cb);
+    const int nblk = (ncells + cb - 1) / cb;
+    const int cells_pad = nblk * cb;
+    // enough chunks of s for about four CTAs per SM, bounded by the partial buffer
+    int nchunks = std::max(1, (4 * c.sm_count + nblk - 1) / nblk);
+    nchunks = std::min<int64_t>(nchunks, std::min<int64_t>(d.ns, 512));
+    const size_t part_elems = (size_t)nchunks * d.n_pnt * cells_pad;
+    while (nchunks > 1 && part_elems * sizeof(float) > ((size_t)16 << 30)) nchunks--;
+    // work-balanced chunk boundaries over the linear s order
+    std::vector<int> bounds(nchunks + 1);
+    const int64_t total = c.s_work_prefix[d.ns];
+    bounds[0] = 0;
+    for (int k = 1; k < nchunks; k++) {
+        const int64_t target = total * k / nchunks;
+        bounds[k] = (int)(std::lower_bound(c.s_work_prefix.begin(), c.s_work_prefix.end(), target) -
+                          c.s_work_prefix.begin());
+        bounds[k] = std::max(bounds[k], bounds[k - 1]);
+    }
+    bounds[nchunks] = (int)d.ns;
+    if (c.s_bounds_cap < nchunks + 1) {
+        if (c.d_s_bounds) cudaFree(c.d_s_bounds);
+        c.d_s_bounds = nullptr;
+        GD_CUDA(cudaMalloc(&c.d_s_bounds, sizeof(int) * (nchunks + 1)));
+        c.s_bounds_cap = nchunks + 1;
+    }
+    GD_CUDA(cudaMemcpyAsync(c.d_s_bounds, bounds.data(), sizeof(int) * (nchunks + 1),
+                            cudaMemcpyHostToDevice, st));
+    const size_t part_bytes = (size_t)nchunks * d.n_pnt * cells_pad * sizeof(float);
+    int rc = ensure_scratch(c, part_bytes);
+    if (rc) return rc;
+    float *part = static_cast<float *>(c.scratch.ptr);
+    GD_CUDA(cudaMemsetAsync(part, 0, part_bytes, st));
+
+    GainArgs a{d, f, ld, ncells, cells_pad, c.d_cmap, c.d_list_off, c.d_list, c.d_s_bounds, part};
+    dim3 grid(nblk, nchunks);
+    switch (cb) {
+#define GD_GAIN_CASE(CBV)                                                                       \
+    case CBV:                                                                                   \
+        GD_CUDA(cudaFuncSetAttribute(gain_pair_kernel<CBV>,                                     \
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));  \
+        gain_pair_kernel<CBV><<<grid, kThreads, smem, st>>>(a);                                 \
+        break;
+        GD_GAIN_CASE(32)
+        GD_GAIN_CASE(16)
+        GD_GAIN_CASE(8)
+        GD_GAIN_CASE(4)
+#undef GD_GAIN_CASE
+    default:
+        return set_error(GD_ERR_UNSUPPORTED, "gain kernel cell block");
+    }
+    GD_CUDA(cudaGetLastError());
+    const int64_t outs = (int64_t)d.n_pnt * ncells;
+    int rblocks = (int)std::min<int64_t>((outs + 255) / 256, (int64_t)c.sm_count * 16);
+    gain_reduce_kernel<<<std::max(rblocks, 1), 256, 0, st>>>(part, nchunks, d.n_pnt, cells_pad,
+                                                              ncells, ld, gain);
+    GD_CUDA(cudaGetLastError());
+    return GD_OK;
+}
+
+}  // namespace gd

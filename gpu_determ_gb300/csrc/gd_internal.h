@@ -1,0 +1,112 @@
+// gd_internal.h -- shared declarations of the GB300 collision-integral library.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "gpu_determ.h"
+
+namespace gd {
+
+// Lattice sizes derived from a grid spec.  The "class box" of a parity
+// class is the set of offsets v with 0 <= v_a < n_a and v_a of one parity per
+// axis; it has hx*hy*hz members, indexed (x2*hy + y2)*hz + z2 with v_a = 2*v2_a +
+// parity_a.
+struct Dims {
+    int nx, ny, nz, nyz, nxyz;
+    int hx, hy, hz, nclass;  // half sizes and class-box size
+    int sx, sy, sz;          // extents of the pair sums s = i + i1: 2n - 1
+    int64_t ns;              // sx*sy*sz
+    int n_pnt;
+    float du, dv, dw, d3v;
+};
+
+// One nonzero post-collision weight of the row |g|: meta packs the class
+// index of n (bits 0..14) and its half components x2, y2, z2 (5 bits each at
+// 15, 20, 25); w is the FP32 weight.
+struct WEntry {
+    uint32_t meta;
+    float w;
+};
+static_assert(sizeof(WEntry) == 8, "WEntry must be 8 bytes");
+
+__host__ __device__ inline uint32_t wentry_meta(int nc, int x2, int y2, int z2)
+{
+    return (uint32_t)nc | ((uint32_t)x2 << 15) | ((uint32_t)y2 << 20) | ((uint32_t)z2 << 25);
+}
+
+struct Scratch {
+    void *ptr = nullptr;
+    size_t bytes = 0;
+};
+
+struct Context {
+    gd_grid_spec spec{};
+    Dims d{};
+    int device = 0;
+    // host copies of the grid
+    std::vector<float> u, v, w;
+    std::vector<int> ui, vi, wi;
+    std::vector<int> cmap;  // box index -> compact index or -1
+    // device tables
+    int16_t *d_cmap = nullptr;    // [nxyz] box -> compact, -1 outside the sphere
+    uint32_t *d_nodes = nullptr;  // [n_pnt] packed box coords x | y << 10 | z << 20
+    float *d_b = nullptr;         // [nxyz] loss kernel by |g|
+    double *d_phi = nullptr;      // [5][n_pnt] basis 1, xi_x, xi_y, xi_z, xi^2 (FP64)
+    int *d_list_off = nullptr;    // [nxyz + 1] weight-row offsets by |g| box index
+    WEntry *d_list = nullptr;     // nonzero weights, rows in box order of |g|
+    int64_t n_entries = 0;
+    // pair-sum schedule for the gain kernel: work-balanced chunk boundaries
+    std::vector<int64_t> s_work_prefix;  // [ns + 1] cumulative work in linear s order
+    // counts reported by gd_ctx_info
+    int64_t pair_products = 0, contraction_terms = 0, scatter_terms = 0;
+    bool contraction_exact = false;  // contraction_terms filtered by n in B(D(s))
+    // scratch owned by the context (grown on demand)
+    Scratch scratch;
+    int *d_s_bounds = nullptr;  // chunk boundaries for the current launch shape
+    int s_bounds_cap = 0;
+    float *d_reduce = nullptr;  // small device scalars (max nu, dt)
+    int sm_count = 0;
+};
+
+// error state -------------------------------------------------------------
+int set_error(int code, const std::string &msg);
+int cuda_error(cudaError_t e, const char *what);
+#define GD_CUDA(call)                                        \
+    do {                                                     \
+        cudaError_t e_ = (call);                             \
+        if (e_ != cudaSuccess) return gd::cuda_error(e_, #call); \
+    } while (0)
+
+// grid (host, gd_grid.cpp) -------------------------------------------------
+int grid_count(const gd_grid_spec &s);
+int grid_fill(const gd_grid_spec &s, float *u, float *v, float *w, int *ui, int *vi, int *wi,
+              float *steps);
+
+// device table builders (gd_weights.cu) ------------------------------------
+// Dense reference-layout tables: b[nxyz] and/or a[(nx/2)*nx*(ny/2)*(nz/2)*ny*nz].
+int launch_dense_tables(const Dims &d, float *b, float *a, cudaStream_t st);
+// Compact the dense table a into per-|g| rows (device), returns entries.
+int build_weight_rows(Context &c, const float *a_dense, cudaStream_t st);
+
+// kernels -------------------------------------------------------------------
+int run_loss(Context &c, const float *f, int ncells, int ld, float *nu, cudaStream_t st);
+int run_gain(Context &c, const float *f, int ncells, int ld, float *gain, cudaStream_t st);
+int run_project(Context &c, const float *f, const float *nu, const float *gain, int ncells,
+                int ld, float *nu_corr, double *q, double *x, int fixed_dt_mode, float dt,
+                float *f_out, double *m5, cudaStream_t st);
+int run_relax(Context &c, float *f, const float *nu_corr, const float *gain, int ncells, int ld,
+              int mode, float param, float *time_dev, float *dt_dev, cudaStream_t st);
+int run_relax_q(Context &c, float *f, const float *nu_corr, const float *gain, const double *q,
+                int ncells, int ld, int mode, float param, float *time_dev, float *dt_dev,
+                cudaStream_t st);
+int run_moments(Context &c, const float *f, int ncells, int ld, double *m5, cudaStream_t st);
+int run_basis(Context &c, float *basis, cudaStream_t st);
+
+// scratch -------------------------------------------------------------------
+int ensure_scratch(Context &c, size_t bytes);
+
+}  // namespace gd

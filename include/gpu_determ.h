@@ -1,0 +1,143 @@
+/*
+ * gpu_determ.h -- C ABI of the GB300 collision-integral library.
+ *
+ * Deterministic discrete-velocity evaluation of the hard-sphere Boltzmann
+ * collision integral Q(f) = I(f) - f nu(f) on a uniform 3-D velocity lattice
+ * truncated to a sphere, batched over spatial cells, on one GPU (sm_103a).
+ *
+ * Conventions
+ *  - Every function returns GD_OK (0) or a GD_ERR_* code; the message of the
+ *    last failure on the calling host thread is gd_last_error().
+ *  - Distribution arrays are device pointers laid out [node][cell]: node is the
+ *    compact index over the in-sphere lattice nodes (the order of the grid's
+ *    u/v/w index lists), cell is fastest, `ld` is the stride between nodes
+ *    (ld >= ncells).  With R large enough to keep every node this is exactly
+ *    the reference layout f[(i*ny + j)*nz + k][cell] with npx = ld.
+ *  - Streams are cudaStream_t passed as gd_stream (NULL = legacy stream).
+ *  - Results are bitwise reproducible run to run: no atomics, fixed-order
+ *    reductions.
+ *
+ * Reference interfaces (savthe/gpu_determ) each entry point replaces are cited
+ * as file:line.
+ */
+#ifndef GPU_DETERM_H
+#define GPU_DETERM_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct CUstream_st *gd_stream;
+typedef struct gd_ctx gd_ctx;
+
+enum {
+    GD_OK = 0,
+    GD_ERR_INVALID_ARG = 1,  /* bad size, pointer or option */
+    GD_ERR_CUDA = 2,         /* a CUDA runtime call or launch failed */
+    GD_ERR_OUT_OF_MEMORY = 3,
+    GD_ERR_UNSUPPORTED = 4,  /* grid or batch outside what the kernels support */
+    GD_ERR_SINGULAR = 5,     /* a 5x5 conservation system had no solution */
+    GD_ERR_IO = 6,           /* file could not be opened or parsed */
+};
+
+/* Velocity grid: nodes u_i = vmin + d (2i+1)/2 per axis, kept when
+ * u^2+v^2+w^2 < R^2 (R <= 0 keeps all).  nx, ny, nz even.
+ * Replaces VelocityGrid::init (velocity_grid.hpp:39-43, velocity_grid.cu:73-126)
+ * and check_if_point_is_in_domain (velocity_grid.cu:6-14). */
+typedef struct {
+    int nx, ny, nz;
+    float vmin[3], vmax[3];
+    float R;
+} gd_grid_spec;
+
+typedef struct {
+    int nx, ny, nz, n_pnt;
+    float du, dv, dw, d3v;
+    int64_t nonzero_weights;   /* nonzero entries of the weight table a */
+    int64_t table_a_elems;     /* (nx/2)*nx*(ny/2)*(nz/2)*ny*nz, reference layout */
+    int64_t pair_products;     /* (s, n) pair products formed per cell-eval */
+    int64_t contraction_terms; /* nonzero-weight x pair-product terms per cell-eval */
+    int64_t scatter_terms;     /* (s, g, sign) output updates per cell-eval */
+} gd_info;
+
+/* Library version (major*10000 + minor*100 + patch). */
+int gd_version(void);
+/* Message of the last failure on this host thread ("" when none). */
+const char *gd_last_error(void);
+
+/* ---- host-side grid (no GPU needed) ------------------------------------ */
+/* Number of in-sphere nodes.  Replaces the counting loop of
+ * VelocityGrid::init (velocity_grid.cu:80-84). */
+int gd_grid_count(const gd_grid_spec *spec, int *n_pnt);
+/* Node centres u[nx], v[ny], w[nz]; index lists ui/vi/wi[n_pnt];
+ * steps[4] = {du, dv, dw, d3v}.  Replaces VelocityGrid::init
+ * (velocity_grid.cu:73-126) and its VelocityGridBase fields
+ * (velocity_grid.hpp:6-31). */
+int gd_grid_fill(const gd_grid_spec *spec, float *u, float *v, float *w, int *ui, int *vi,
+                 int *wi, float *steps);
+
+/* ---- context ----------------------------------------------------------- */
+/* Binds to `device`, uploads the grid and builds the weight tables on the GPU
+ * (FP64 analytic builder, compacted to nonzero entries).  Replaces the
+ * device half of VelocityGrid (VelocityGrid::device, DeviceVelocityGrid,
+ * velocity_grid.cu:21-48) and init_matrices (compute_matrix.h:13,
+ * compute_matrix.cu:564-600). */
+int gd_ctx_create(const gd_grid_spec *spec, int device, gd_ctx **out);
+int gd_ctx_destroy(gd_ctx *ctx);
+int gd_ctx_info(const gd_ctx *ctx, gd_info *out);
+
+/* Dense tables in the reference layout: b[nx*ny*nz] (loss kernel
+ * 4 pi |g| d3v) and a[table_a_elems] (post-collision weights), device
+ * buffers owned by the caller; either may be NULL.  Replaces the table
+ * contents of init_matrices (compute_matrix.cu:505-562). */
+int gd_export_tables(gd_ctx *ctx, float *b, float *a, gd_stream stream);
+/* 14 moment-basis rows over the full box [14][nx*ny*nz] (xi_x, xi_y, xi_z,
+ * xi^2, xi_x^2, xi_x xi_y, xi_x xi_z, xi_x xi^2, xi_y^2, xi_y xi_z,
+ * xi_y xi^2, xi_z^2, xi_z xi^2, xi^2 xi^2).  Replaces init_correction_array
+ * (velocity.h:41, velocity.cu:17-65). */
+int gd_correction_basis(gd_ctx *ctx, float *basis, gd_stream stream);
+
+/* ---- collision operator ------------------------------------------------ */
+/* Loss frequency nu[i][c] = sum_j b(|i-j|) f[j][c] and gain I[i][c] over the
+ * in-sphere nodes, FP32 (either output may be NULL).  Replaces the loss and
+ * gain stages of evolve_colisions (collision_integral.h:11-17,
+ * collision_integral.cu:32-188, 587-648). */
+int gd_collision(gd_ctx *ctx, const float *f, int ncells, int ld, float *nu, float *gain,
+                 gd_stream stream);
+/* FP64 mass/momentum/energy projection per cell: solves A X = B with
+ * A_kl = sum f nu phi_k phi_l, B_k = sum (I - f nu) phi_k, phi = (1, xi, xi^2),
+ * then nu' = nu (1 + X.phi) and Q = I - f nu' (so sum Q phi_k = 0).
+ * nu_corr (FP32, may alias nu), q (FP64, may be NULL, leading dim ld) and
+ * x[5*ncells] (FP64, may be NULL).  Replaces before_correction,
+ * linear_solver and correct_frequency (collision_integral.cu:217-526,
+ * 669-744) with the intended per-cell solve. */
+int gd_project(gd_ctx *ctx, const float *f, const float *nu, const float *gain, int ncells,
+               int ld, float *nu_corr, double *q, double *x, gd_stream stream);
+/* Explicit relaxation f <- f + dt (I - f nu') with
+ * mode GD_DT_COURANT: dt = param / max(nu') over all nodes and cells
+ *                     (get_delta_t, collision_integral.cu:776-807);
+ * mode GD_DT_FIXED:   dt = param.
+ * time_dev (device float, may be NULL) is advanced by dt; dt_dev (device
+ * float, may be NULL) receives dt.  Replaces relax_f and evolve_f
+ * (collision_integral.h:19-24, collision_integral.cu:809-880). */
+enum { GD_DT_COURANT = 0, GD_DT_FIXED = 1 };
+int gd_relax(gd_ctx *ctx, float *f, const float *nu_corr, const float *gain, int ncells, int ld,
+             int mode, float param, float *time_dev, float *dt_dev, gd_stream stream);
+/* One full step: collision, projection and relaxation (FP64 Q), with the
+ * per-cell moments (n, n u_x, n u_y, n u_z, sum f xi^2 d3v) of f before the
+ * update in m5[5*ncells] (device FP64, may be NULL).  nu/gain/q receive the
+ * step's corrected frequency, gain and Q (each may be NULL). */
+int gd_step(gd_ctx *ctx, float *f, int ncells, int ld, int mode, float param, float *nu,
+            float *gain, double *q, double *m5, float *time_dev, float *dt_dev, gd_stream stream);
+/* Per-cell moments sum f phi_k d3v, phi = (1, xi_x, xi_y, xi_z, xi^2), FP64,
+ * m5[5*ncells] on the device.  Restates print_moments (determ.cu:123-144)
+ * per cell. */
+int gd_moments(gd_ctx *ctx, const float *f, int ncells, int ld, double *m5, gd_stream stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

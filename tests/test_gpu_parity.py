@@ -1,0 +1,233 @@
+"""Parity of the CUDA path with the oracle, through the C ABI, on the GPU.
+
+Tolerances (stated per result, against the FP64 oracle on the same inputs):
+  b table            bit-exact (same float expression, -fmad=false)
+  a table            identical nonzero pattern; |da| <= 4 ulp(float)
+  nu (loss)          max relative error <= 1e-5 (FP32 sum over the partners)
+  I  (gain)          relative L2 <= 1e-5; max |dI| <= 1e-4 * max|I| per cell
+  Q after projection relative L2 <= 1e-4 (Q = I - f nu' is a difference)
+  moments of Q       |sum Q phi_k| <= 1e-12 * sum |I phi_k|  (FP64 projection)
+  golden nodes       within 1e-4 relative of true_results.out (6 printed digits,
+                     FP32 reference accumulation ~5e-5 off the FP64 value)
+  determinism        two runs bitwise equal
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from gpu_determ_gb300 import inputs
+from oracle.pyoracle import Oracle
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def _dev(torch, a, ld=None):
+    a = np.asarray(a, np.float32)
+    ld = a.shape[1] if ld is None else ld
+    t = torch.zeros((a.shape[0], ld), dtype=torch.float32, device="cuda")
+    t[:, : a.shape[1]] = torch.from_numpy(a).cuda()
+    return t
+
+
+def run_collision(torch, ctx, f, ld=None):
+    n, nc = f.shape
+    ft = _dev(torch, f, ld)
+    ld = ft.shape[1]
+    nu = torch.full_like(ft, -1.0)
+    gain = torch.full_like(ft, -1.0)
+    ctx.collision(ft, nc, ld, nu, gain)
+    torch.cuda.synchronize()
+    return nu[:, :nc].cpu().numpy(), gain[:, :nc].cpu().numpy(), ft, nu, gain
+
+
+def check_gain(g_gpu, g_ref):
+    g_ref = np.asarray(g_ref, np.float64)
+    d = g_gpu.astype(np.float64) - g_ref
+    rel_l2 = np.linalg.norm(d) / np.linalg.norm(g_ref)
+    assert rel_l2 <= 1e-5, rel_l2
+    per_cell = np.abs(d).max(axis=0) / np.abs(g_ref).max(axis=0)
+    assert per_cell.max() <= 1e-4, per_cell.max()
+    return rel_l2
+
+
+CASES = [(8, 16.5, 5, None), (12, 4.8, 37, 40), (16, 4.8, 33, 33), (10, 3.9, 64, 64)]
+
+
+@pytest.mark.parametrize("n,R,ncells,ld", CASES)
+def test_collision_matches_oracle(cuda, gdlib, n, R, ncells, ld):
+    spec = gdlib.GridSpec(n, R=R)
+    ctx = gdlib.Context(spec)
+    grid = spec.fill()
+    f = inputs.mixtures(grid, ncells, seed=n)
+    nu, gain, *_ = run_collision(cuda, ctx, f, ld)
+    o = Oracle(n, R=R)
+    fb = o.to_box(f)
+    nu64 = o.loss_f64(fb)
+    g64 = o.gain_f64(fb)
+    assert np.max(np.abs(nu - nu64) / np.abs(nu64)) <= 1e-5
+    check_gain(gain, g64)
+
+
+def test_padding_columns_untouched(cuda, gdlib):
+    spec = gdlib.GridSpec(8, R=16.5)
+    ctx = gdlib.Context(spec)
+    f = inputs.mixtures(spec.fill(), 3, seed=3)
+    _, _, ft, nu, gain = run_collision(cuda, ctx, f, ld=8)
+    assert bool((nu[:, 3:] == -1.0).all()) and bool((gain[:, 3:] == -1.0).all())
+
+
+def test_tables_match_oracle(cuda, gdlib):
+    for n in (8, 12, 16):
+        spec = gdlib.GridSpec(n, R=16.5)
+        ctx = gdlib.Context(spec)
+        o = Oracle(n, R=16.5)
+        b = cuda.zeros(o.nxyz, dtype=cuda.float32, device="cuda")
+        a = cuda.zeros(o.a_size, dtype=cuda.float32, device="cuda")
+        ctx.export_tables(b, a)
+        cuda.cuda.synchronize()
+        assert np.array_equal(b.cpu().numpy(), o.table_b())
+        ag, ao = a.cpu().numpy(), o.table_a()
+        assert np.array_equal(ag != 0, ao != 0)
+        ulp = np.spacing(np.abs(ao).astype(np.float32))
+        assert np.all(np.abs(ag - ao) <= 4 * ulp)
+        assert ctx.info["nonzero_weights"] == int(np.count_nonzero(ao))
+
+
+def test_correction_basis_matches_reference_formula(cuda, gdlib):
+    spec = gdlib.GridSpec(8, ny=10, nz=6, R=16.5)
+    ctx = gdlib.Context(spec)
+    g = spec.fill()
+    nxyz = 8 * 10 * 6
+    out = cuda.zeros(14 * nxyz, dtype=cuda.float32, device="cuda")
+    ctx.correction_basis(out)
+    cuda.cuda.synchronize()
+    out = out.cpu().numpy().reshape(14, nxyz)
+    xx = np.repeat(g["u"], 60)
+    xy = np.tile(np.repeat(g["v"], 6), 8)
+    xz = np.tile(g["w"], 80)
+    x2 = (xx * xx + xy * xy) + xz * xz
+    ref = [xx, xy, xz, x2, xx * xx, xx * xy, xx * xz, xx * x2, xy * xy, xy * xz, xy * x2, xz * xz,
+           xz * x2, x2 * x2]
+    for r in range(14):
+        assert np.array_equal(out[r], np.asarray(ref[r], np.float32)), r
+
+
+def test_golden_reference_case(cuda, gdlib):
+    """determ.cu's configuration: 16^3, R=16.5, 256 identical cells."""
+    gold = json.load(open(os.path.join(GOLDEN, "true_results_nodes.json")))
+    spec = gdlib.GridSpec(16, R=16.5)
+    ctx = gdlib.Context(spec)
+    f = inputs.reference_initial_state(spec.fill(), 256)
+    nu, gain, *_ = run_collision(cuda, ctx, f)
+    # cells identical: every column bitwise equal
+    assert np.array_equal(gain, np.repeat(gain[:, :1], 256, axis=1))
+    for k in range(8):
+        lo = np.array(gold["nodes"][str(k)]["min"])
+        hi = np.array(gold["nodes"][str(k)]["max"])
+        mid = 0.5 * (lo + hi)
+        assert abs(f[k, 1] - mid[0]) <= 1e-5 * mid[0]
+        assert abs(nu[k, 1] - mid[1]) <= 2e-5 * mid[1], (k, nu[k, 1], mid[1])
+        assert abs(gain[k, 1] - mid[2]) <= 1e-4 * mid[2], (k, gain[k, 1], mid[2])
+        q = np.float32(-f[k, 1] * nu[k, 1]) + gain[k, 1]
+        assert abs(q - mid[3]) <= 2e-4 * abs(mid[3]), (k, q, mid[3])
+
+
+def test_deterministic_bitwise(cuda, gdlib):
+    spec = gdlib.GridSpec(12, R=4.8)
+    ctx = gdlib.Context(spec)
+    f = inputs.mixtures(spec.fill(), 70, seed=5)
+    r1 = run_collision(cuda, ctx, f)
+    r2 = run_collision(cuda, ctx, f)
+    assert np.array_equal(r1[0], r2[0]) and np.array_equal(r1[1], r2[1])
+
+
+def test_projection_conserves_and_matches_oracle(cuda, gdlib):
+    torch = cuda
+    n, R, nc = 12, 4.8, 48
+    spec = gdlib.GridSpec(n, R=R)
+    ctx = gdlib.Context(spec)
+    f = inputs.mixtures(spec.fill(), nc, seed=11)
+    nu, gain, ft, nut, gaint = run_collision(torch, ctx, f)
+    nuc = torch.zeros_like(ft)
+    q = torch.zeros(ft.shape, dtype=torch.float64, device="cuda")
+    x = torch.zeros((nc, 5), dtype=torch.float64, device="cuda")
+    ctx.project(ft, nut, gaint, nc, nc, nuc, q, x)
+    torch.cuda.synchronize()
+    q = q.cpu().numpy()
+    o = Oracle(n, R=R)
+    phi = o.phi()
+    mom = phi.T @ q
+    scale = np.abs(phi).T @ np.abs(gain.astype(np.float64))
+    assert np.all(np.abs(mom) <= 1e-12 * scale), np.max(np.abs(mom) / scale)
+    # same FP32 inputs through the oracle's FP64 projection
+    nu_c, q_o, x_o, sing = o.project(f, nu, gain)
+    assert sing == 0
+    assert np.linalg.norm(q - q_o) <= 1e-10 * np.linalg.norm(q_o)
+    assert np.allclose(x.cpu().numpy(), x_o, rtol=1e-8, atol=1e-14)
+    # end to end against the FP64 oracle operator
+    fb = o.to_box(f)
+    nu_c64, q64, _, _ = o.project(f, o.loss_f64(fb).astype(np.float32), o.gain_f64(fb).astype(np.float32))
+    assert np.linalg.norm(q - q64) <= 1e-4 * np.linalg.norm(q64)
+
+
+def test_relax_courant_and_fixed(cuda, gdlib):
+    torch = cuda
+    n, R, nc = 10, 16.5, 20
+    spec = gdlib.GridSpec(n, R=R)
+    ctx = gdlib.Context(spec)
+    f = inputs.mixtures(spec.fill(), nc, seed=2)
+    nu, gain, ft, nut, gaint = run_collision(torch, ctx, f)
+    for mode, param in ((gdlib.DT_COURANT, 0.5), (gdlib.DT_FIXED, 0.05)):
+        f2 = ft.clone()
+        t = torch.zeros(1, dtype=torch.float32, device="cuda")
+        dt = torch.zeros(1, dtype=torch.float32, device="cuda")
+        ctx.relax(f2, nut, gaint, nc, nc, mode, param, t, dt)
+        torch.cuda.synchronize()
+        dtv = np.float32(param) / nu.max() if mode == gdlib.DT_COURANT else np.float32(param)
+        assert dt.item() == dtv and t.item() == dtv
+        ref = (f.astype(np.float64) + float(dtv) * (gain.astype(np.float64) - f.astype(np.float64) * nu)).astype(np.float32)
+        assert np.array_equal(f2.cpu().numpy(), ref)
+
+
+def test_step_conserves_moments(cuda, gdlib):
+    torch = cuda
+    n, R, nc = 12, 4.8, 32
+    spec = gdlib.GridSpec(n, R=R)
+    ctx = gdlib.Context(spec)
+    f = inputs.mixtures(spec.fill(), nc, seed=7)
+    ft = _dev(torch, f)
+    q = torch.zeros(ft.shape, dtype=torch.float64, device="cuda")
+    gt = torch.zeros_like(ft)
+    m0 = torch.zeros((nc, 5), dtype=torch.float64, device="cuda")
+    m1 = torch.zeros((nc, 5), dtype=torch.float64, device="cuda")
+    ctx.step(ft, nc, nc, gdlib.DT_FIXED, 0.05, gain=gt, q=q, m5=m0)
+    ctx.moments(ft, nc, nc, m1)
+    torch.cuda.synchronize()
+    m0, m1 = m0.cpu().numpy(), m1.cpu().numpy()
+    # f is stored in FP32 after the update, so moments move by FP32 rounding only
+    assert np.all(np.abs(m1 - m0) <= 1e-6 * np.abs(m0).max(axis=0) + 1e-12)
+    o = Oracle(n, R=R)
+    mom = o.phi().T @ q.cpu().numpy()
+    scale = np.abs(o.phi()).T @ np.abs(gt.cpu().numpy().astype(np.float64))
+    assert np.all(np.abs(mom) <= 1e-12 * scale)
+
+
+def test_20cube_sampled_nodes(cuda, gdlib):
+    n, R, nc = 20, 4.8, 40
+    spec = gdlib.GridSpec(n, R=R)
+    ctx = gdlib.Context(spec)
+    f = inputs.mixtures(spec.fill(), nc, seed=20)
+    nu, gain, *_ = run_collision(cuda, ctx, f)
+    o = Oracle(n, R=R)
+    rng = np.random.default_rng(0)
+    pick = rng.choice(o.n_pnt, 48, replace=False)
+    fb = o.to_box(f)
+    g64 = o.gain_f64(fb, o.box_of_compact[pick])
+    nu64 = o.loss_f64(fb, o.box_of_compact[pick])
+    assert np.max(np.abs(nu[pick] - nu64) / nu64) <= 1e-5
+    d = gain[pick] - g64
+    assert np.linalg.norm(d) <= 1e-5 * np.linalg.norm(g64)
