@@ -74,9 +74,10 @@ def lib():
     L.gd_relax.argtypes = [vp, vp, vp, vp, i, i, i, f, vp, vp, vp]
     L.gd_step.argtypes = [vp, vp, i, i, i, f, vp, vp, vp, vp, vp, vp, vp]
     L.gd_moments.argtypes = [vp, vp, i, i, vp, vp]
+    L.gd_gain_noalloc.argtypes = [vp, vp, i, i, vp, vp]
     for name in ("gd_grid_count", "gd_grid_fill", "gd_ctx_create", "gd_ctx_destroy", "gd_ctx_info",
                  "gd_export_tables", "gd_correction_basis", "gd_collision", "gd_project",
-                 "gd_relax", "gd_step", "gd_moments"):
+                 "gd_relax", "gd_step", "gd_moments", "gd_gain_noalloc"):
         getattr(L, name).restype = i
     _lib = L
     return L

@@ -245,4 +245,75 @@ int run_gain(Context &c, const float *f, int ncells, int ld, float *gain, cudaSt
     return GD_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Launch pieces for callers that bring their own partial-sum buffer (the
+// allocation-free entry point in gd_noalloc.cu).  run_gain above does not
+// use them.
+
+int gain_launch_shape(Context &c, int ncells, int *cb_out, size_t *smem_out, int *nblk_out,
+                      int *chunks_out)
+{
+    const Dims &d = c.d;
+    int max_smem = 0;
+    GD_CUDA(cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, c.device));
+    int cb = 32;
+    while (cb > 4 && gain_smem_bytes(d, cb) > (size_t)max_smem) cb >>= 1;
+    if (gain_smem_bytes(d, cb) > (size_t)max_smem)
+        return set_error(GD_ERR_UNSUPPORTED, "velocity grid too large for the gain kernel's shared memory");
+    const int nblk = (ncells + cb - 1) / cb;
+    int nchunks = std::max(1, (4 * c.sm_count + nblk - 1) / nblk);
+    nchunks = (int)std::min<int64_t>(nchunks, std::min<int64_t>(d.ns, 512));
+    *cb_out = cb;
+    *smem_out = gain_smem_bytes(d, cb);
+    *nblk_out = nblk;
+    *chunks_out = nchunks;
+    return GD_OK;
+}
+
+void gain_chunk_bounds(const Context &c, int nchunks, int *bounds)
+{
+    const int64_t total = c.s_work_prefix[c.d.ns];
+    bounds[0] = 0;
+    for (int k = 1; k < nchunks; k++) {
+        const int64_t target = total * k / nchunks;
+        bounds[k] = (int)(std::lower_bound(c.s_work_prefix.begin(), c.s_work_prefix.end(), target) -
+                          c.s_work_prefix.begin());
+        bounds[k] = std::max(bounds[k], bounds[k - 1]);
+    }
+    bounds[nchunks] = (int)c.d.ns;
+}
+
+int launch_gain_pair(Context &c, const float *f, int ncells, int ld, float *gain, float *part,
+                     int nchunks, const int *d_bounds, int cb, size_t smem, cudaStream_t st)
+{
+    const Dims &d = c.d;
+    const int nblk = (ncells + cb - 1) / cb;
+    const int cells_pad = nblk * cb;
+    GD_CUDA(cudaMemsetAsync(part, 0, (size_t)nchunks * d.n_pnt * cells_pad * sizeof(float), st));
+    GainArgs a{d, f, ld, ncells, cells_pad, c.d_cmap, c.d_list_off, c.d_list, d_bounds, part};
+    dim3 grid(nblk, nchunks);
+    switch (cb) {
+#define GD_GAIN_CASE(CBV)                                                                       \
+    case CBV:                                                                                   \
+        GD_CUDA(cudaFuncSetAttribute(gain_pair_kernel<CBV>,                                     \
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));  \
+        gain_pair_kernel<CBV><<<grid, kThreads, smem, st>>>(a);                                 \
+        break;
+        GD_GAIN_CASE(32)
+        GD_GAIN_CASE(16)
+        GD_GAIN_CASE(8)
+        GD_GAIN_CASE(4)
+#undef GD_GAIN_CASE
+    default:
+        return set_error(GD_ERR_UNSUPPORTED, "gain kernel cell block");
+    }
+    GD_CUDA(cudaGetLastError());
+    const int64_t outs = (int64_t)d.n_pnt * ncells;
+    int rblocks = (int)std::min<int64_t>((outs + 255) / 256, (int64_t)c.sm_count * 16);
+    gain_reduce_kernel<<<std::max(rblocks, 1), 256, 0, st>>>(part, nchunks, d.n_pnt, cells_pad,
+                                                              ncells, ld, gain);
+    GD_CUDA(cudaGetLastError());
+    return GD_OK;
+}
+
 }  // namespace gd

@@ -106,6 +106,12 @@ int run_relax_q(Context &c, float *f, const float *nu_corr, const float *gain, c
 int run_moments(Context &c, const float *f, int ncells, int ld, double *m5, cudaStream_t st);
 int run_basis(Context &c, float *basis, cudaStream_t st);
 
+// gain launch pieces for a caller-provided partial buffer (gd_gain.cu)
+int gain_launch_shape(Context &c, int ncells, int *cb, size_t *smem, int *nblk, int *chunks);
+void gain_chunk_bounds(const Context &c, int nchunks, int *bounds);
+int launch_gain_pair(Context &c, const float *f, int ncells, int ld, float *gain, float *part,
+                     int nchunks, const int *d_bounds, int cb, size_t smem, cudaStream_t st);
+
 // scratch -------------------------------------------------------------------
 int ensure_scratch(Context &c, size_t bytes);
 

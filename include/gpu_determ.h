@@ -137,6 +137,19 @@ int gd_step(gd_ctx *ctx, float *f, int ncells, int ld, int mode, float param, fl
  * per cell. */
 int gd_moments(gd_ctx *ctx, const float *f, int ncells, int ld, double *m5, gd_stream stream);
 
+/* Gain I[i][c] exactly as gd_collision computes it, but with no device
+ * allocation of any kind during the call.  No counterpart in the reference:
+ * it exists for callers that cannot let a library call cudaMalloc (a custom
+ * allocator or memory pool owns the device, a latency-critical loop must not
+ * hit cudaMalloc's implicit synchronisation, or allocation is forbidden after
+ * start-up).  Its partial sums live in a fixed 64 MiB array inside the
+ * library image, held on every GPU that loads the library until exit; a batch
+ * needing more (about 4500 cells on a 20^3 grid cut to R=4.8) is rejected with
+ * GD_ERR_UNSUPPORTED.  The first call on a device looks the array's address
+ * up (make it before any stream capture).  All calls share the array: calls
+ * that overlap on the GPU race, so order them. */
+int gd_gain_noalloc(gd_ctx *ctx, const float *f, int ncells, int ld, float *gain, gd_stream stream);
+
 #ifdef __cplusplus
 }
 #endif
