@@ -43,7 +43,7 @@ int check_spec(const gd_grid_spec *s)
     const int n[3] = {s->nx, s->ny, s->nz};
     for (int a = 0; a < 3; a++) {
         if (n[a] < 2 || (n[a] & 1)) return set_error(GD_ERR_INVALID_ARG, "grid sizes must be even and >= 2");
-        if (n[a] > 64) return set_error(GD_ERR_UNSUPPORTED, "grid sizes above 64 per axis are not supported");
+        if (n[a] > 62) return set_error(GD_ERR_UNSUPPORTED, "grid sizes above 62 per axis are not supported");
         if (!(s->vmax[a] > s->vmin[a]) || !std::isfinite(s->vmin[a]) || !std::isfinite(s->vmax[a]))
             return set_error(GD_ERR_INVALID_ARG, "velocity bounds must be finite with vmin < vmax");
     }
@@ -124,15 +124,14 @@ int exact_contraction_terms(Context &c, int64_t *out)
         for (int Dy = 0; Dy < d.ny; Dy++)
             for (int Dz = 0; Dz < d.nz; Dz++) {
                 const int mult = (Dx == d.nx - 1 ? 1 : 2) * (Dy == d.ny - 1 ? 1 : 2) * (Dz == d.nz - 1 ? 1 : 2);
-                const uint32_t hx2 = Dx >> 1, hy2 = Dy >> 1, hz2 = Dz >> 1;
+                const uint32_t bound = wentry_bound(Dx >> 1, Dy >> 1, Dz >> 1);
                 int64_t t = 0;
                 for (int gx = Dx & 1; gx <= Dx; gx += 2)
                     for (int gy = Dy & 1; gy <= Dy; gy += 2)
                         for (int gz = Dz & 1; gz <= Dz; gz += 2) {
                             const int gbox = (gx * d.ny + gy) * d.nz + gz;
                             for (int e = off[gbox]; e < off[gbox + 1]; e++) {
-                                const uint32_t m = rows[e].meta;
-                                t += ((m >> 15) & 31) <= hx2 && ((m >> 20) & 31) <= hy2 && ((m >> 25) & 31) <= hz2;
+                                t += ((bound - rows[e].meta) & kWGuard) == kWGuard;
                             }
                         }
                 total += t * mult;
@@ -208,6 +207,8 @@ static int create_context(Context &c, const gd_grid_spec &spec, int device)
     const int np = grid_count(spec);
     if (np < 1) return set_error(GD_ERR_INVALID_ARG, "no lattice node lies inside the sphere");
     if (np > 32767) return set_error(GD_ERR_UNSUPPORTED, "more than 32767 in-sphere nodes");
+    if ((int64_t)d.hx * d.hy * d.hz > kMaxClass)
+        return set_error(GD_ERR_UNSUPPORTED, "parity class box larger than 16384 offsets");
     c.u.resize(d.nx);
     c.v.resize(d.ny);
     c.w.resize(d.nz);

@@ -30,7 +30,7 @@
 namespace gd {
 namespace {
 
-constexpr int kThreads = 512;
+constexpr int kThreads = 1024;
 
 struct GainArgs {
     Dims d;
@@ -48,6 +48,7 @@ __global__ void __launch_bounds__(kThreads, 1) gain_pair_kernel(GainArgs a)
 {
     constexpr int G = 32 / CB;  // item rows per warp
     extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ int row_next;
     const Dims &d = a.d;
     int16_t *cmap = reinterpret_cast<int16_t *>(smem);
     float *P = reinterpret_cast<float *>(smem + ((d.nxyz * 2 + 15) & ~15));
@@ -100,13 +101,26 @@ __global__ void __launch_bounds__(kThreads, 1) gain_pair_kernel(GainArgs a)
             const int nc = (a2 * d.hy + b2) * d.hz + c2;
             P[nc * CB + cl] = t1 + t2;
         }
+        if (threadIdx.x == 0) row_next = 0;
         __syncthreads();
 
         // 2./3. contraction with the weight rows and scatter to outputs -------
-        for (int t = item0; t < nB; t += istep) {
+        // Rows are handed out through a shared counter (a warp takes G rows at
+        // a time, one per lane group).  Each row's sum is formed by one lane
+        // group in entry order and written to targets no other row of this s
+        // touches, so the result does not depend on which warp takes it.
+        const uint32_t bound = wentry_bound(Dx >> 1, Dy >> 1, Dz >> 1);
+        for (;;) {
+            int t0 = 0;
+            if (lane == 0) t0 = atomicAdd(&row_next, G);
+            t0 = __shfl_sync(0xffffffffu, t0, 0);
+            if (t0 >= nB) break;
+            const int t = t0 + grp;
+            if (t >= nB) continue;
             const int c2 = t % ez, b2 = (t / ez) % ey, a2 = t / (ez * ey);
             const int gx = 2 * a2 + px, gy = 2 * b2 + py, gz = 2 * c2 + pz;
-            // targets i = (s +- g)/2, distinct sign patterns only
+            // targets i = (s +- g)/2, distinct sign patterns only; their
+            // partial sums are loaded before the row so the loads overlap it
             int tgt[8];
             float old[8];
             int nt = 0;
@@ -126,25 +140,28 @@ __global__ void __launch_bounds__(kThreads, 1) gain_pair_kernel(GainArgs a)
             if (nt == 0) continue;
             const int gbox = (gx * d.ny + gy) * d.nz + gz;
             const int e0 = __ldg(a.list_off + gbox), e1 = __ldg(a.list_off + gbox + 1);
-            const uint32_t hx2 = (uint32_t)(Dx >> 1), hy2 = (uint32_t)(Dy >> 1), hz2 = (uint32_t)(Dz >> 1);
-            float acc0 = 0.f, acc1 = 0.f;
+            const uint2 *rows = reinterpret_cast<const uint2 *>(a.list);
+            const float *Pc = P + cl;
+            float acc0 = 0.f, acc1 = 0.f, acc2 = 0.f, acc3 = 0.f;
             int e = e0;
-            for (; e + 1 < e1; e += 2) {
-                const uint2 r0 = __ldg(reinterpret_cast<const uint2 *>(a.list + e));
-                const uint2 r1 = __ldg(reinterpret_cast<const uint2 *>(a.list + e + 1));
-                const uint32_t m0 = r0.x, m1 = r1.x;
-                const bool in0 = ((m0 >> 15) & 31) <= hx2 && ((m0 >> 20) & 31) <= hy2 && ((m0 >> 25) & 31) <= hz2;
-                const bool in1 = ((m1 >> 15) & 31) <= hx2 && ((m1 >> 20) & 31) <= hy2 && ((m1 >> 25) & 31) <= hz2;
-                if (in0) acc0 = __fmaf_rn(__uint_as_float(r0.y), P[(m0 & 0x7fff) * CB + cl], acc0);
-                if (in1) acc1 = __fmaf_rn(__uint_as_float(r1.y), P[(m1 & 0x7fff) * CB + cl], acc1);
+            for (; e + 3 < e1; e += 4) {
+                const uint2 r0 = __ldg(rows + e), r1 = __ldg(rows + e + 1);
+                const uint2 r2 = __ldg(rows + e + 2), r3 = __ldg(rows + e + 3);
+                if (((bound - r0.x) & kWGuard) == kWGuard)
+                    acc0 = __fmaf_rn(__uint_as_float(r0.y), Pc[(r0.x >> kWClassShift) * CB], acc0);
+                if (((bound - r1.x) & kWGuard) == kWGuard)
+                    acc1 = __fmaf_rn(__uint_as_float(r1.y), Pc[(r1.x >> kWClassShift) * CB], acc1);
+                if (((bound - r2.x) & kWGuard) == kWGuard)
+                    acc2 = __fmaf_rn(__uint_as_float(r2.y), Pc[(r2.x >> kWClassShift) * CB], acc2);
+                if (((bound - r3.x) & kWGuard) == kWGuard)
+                    acc3 = __fmaf_rn(__uint_as_float(r3.y), Pc[(r3.x >> kWClassShift) * CB], acc3);
             }
-            if (e < e1) {
-                const uint2 r0 = __ldg(reinterpret_cast<const uint2 *>(a.list + e));
-                const uint32_t m0 = r0.x;
-                const bool in0 = ((m0 >> 15) & 31) <= hx2 && ((m0 >> 20) & 31) <= hy2 && ((m0 >> 25) & 31) <= hz2;
-                if (in0) acc0 = __fmaf_rn(__uint_as_float(r0.y), P[(m0 & 0x7fff) * CB + cl], acc0);
+            for (; e < e1; e++) {
+                const uint2 r0 = __ldg(rows + e);
+                if (((bound - r0.x) & kWGuard) == kWGuard)
+                    acc0 = __fmaf_rn(__uint_as_float(r0.y), Pc[(r0.x >> kWClassShift) * CB], acc0);
             }
-            const float acc = acc0 + acc1;
+            const float acc = (acc0 + acc1) + (acc2 + acc3);
             if (live) {
 #pragma unroll
                 for (int sg = 0; sg < 8; sg++)

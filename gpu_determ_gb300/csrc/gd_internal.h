@@ -24,18 +24,30 @@ struct Dims {
     float du, dv, dw, d3v;
 };
 
-// One nonzero post-collision weight of the row |g|: meta packs the class
-// index of n (bits 0..14) and its half components x2, y2, z2 (5 bits each at
-// 15, 20, 25); w is the FP32 weight.
+// One nonzero post-collision weight of the row |g|: meta packs the half
+// components x2, y2, z2 of n in 6-bit fields at bits 0, 6, 12 (bit 5 of each
+// field is a guard bit, so a field-wise "n2 <= D2" test is one subtraction)
+// and the class index of n in bits 18..31; w is the FP32 weight.
 struct WEntry {
     uint32_t meta;
     float w;
 };
 static_assert(sizeof(WEntry) == 8, "WEntry must be 8 bytes");
 
+constexpr uint32_t kWGuard = (1u << 5) | (1u << 11) | (1u << 17);
+constexpr int kWClassShift = 18;
+constexpr int kMaxClass = 1 << (32 - kWClassShift);  // class boxes up to 16384 members
+
 __host__ __device__ inline uint32_t wentry_meta(int nc, int x2, int y2, int z2)
 {
-    return (uint32_t)nc | ((uint32_t)x2 << 15) | ((uint32_t)y2 << 20) | ((uint32_t)z2 << 25);
+    return (uint32_t)x2 | ((uint32_t)y2 << 6) | ((uint32_t)z2 << 12) | ((uint32_t)nc << kWClassShift);
+}
+
+// Guarded bound for the field-wise test: an entry's n lies in B(D) exactly
+// when ((wentry_bound(D) - meta) & kWGuard) == kWGuard.
+__host__ __device__ inline uint32_t wentry_bound(int dx2, int dy2, int dz2)
+{
+    return (uint32_t)dx2 | ((uint32_t)dy2 << 6) | ((uint32_t)dz2 << 12) | kWGuard;
 }
 
 struct Scratch {
