@@ -124,14 +124,17 @@ int exact_contraction_terms(Context &c, int64_t *out)
         for (int Dy = 0; Dy < d.ny; Dy++)
             for (int Dz = 0; Dz < d.nz; Dz++) {
                 const int mult = (Dx == d.nx - 1 ? 1 : 2) * (Dy == d.ny - 1 ? 1 : 2) * (Dz == d.nz - 1 ? 1 : 2);
-                const uint32_t bound = wentry_bound(Dx >> 1, Dy >> 1, Dz >> 1);
+                const int dx2 = Dx >> 1, dy2 = Dy >> 1, dz2 = Dz >> 1;
+                const uint32_t unit = (uint32_t)c.gain_cb * 4u;
                 int64_t t = 0;
                 for (int gx = Dx & 1; gx <= Dx; gx += 2)
                     for (int gy = Dy & 1; gy <= Dy; gy += 2)
                         for (int gz = Dz & 1; gz <= Dz; gz += 2) {
                             const int gbox = (gx * d.ny + gy) * d.nz + gz;
                             for (int e = off[gbox]; e < off[gbox + 1]; e++) {
-                                t += ((bound - rows[e].meta) & kWGuard) == kWGuard;
+                                const int nc = (int)(rows[e].off / unit);
+                                const int z2 = nc % d.hz, y2 = (nc / d.hz) % d.hy, x2 = nc / (d.hz * d.hy);
+                                t += x2 <= dx2 && y2 <= dy2 && z2 <= dz2;
                             }
                         }
                 total += t * mult;
@@ -207,8 +210,7 @@ static int create_context(Context &c, const gd_grid_spec &spec, int device)
     const int np = grid_count(spec);
     if (np < 1) return set_error(GD_ERR_INVALID_ARG, "no lattice node lies inside the sphere");
     if (np > 32767) return set_error(GD_ERR_UNSUPPORTED, "more than 32767 in-sphere nodes");
-    if ((int64_t)d.hx * d.hy * d.hz > kMaxClass)
-        return set_error(GD_ERR_UNSUPPORTED, "parity class box larger than 16384 offsets");
+
     c.u.resize(d.nx);
     c.v.resize(d.ny);
     c.w.resize(d.nz);
@@ -246,6 +248,7 @@ static int create_context(Context &c, const gd_grid_spec &spec, int device)
     if (!guard.ok) return set_error(GD_ERR_CUDA, "cudaSetDevice failed");
     GD_CUDA(cudaDeviceGetAttribute(&c.sm_count, cudaDevAttrMultiProcessorCount, device));
     cudaStream_t st = nullptr;
+    int rc = GD_OK;
     GD_CUDA(cudaMalloc(&c.d_cmap, sizeof(int16_t) * d.nxyz));
     GD_CUDA(cudaMalloc(&c.d_nodes, sizeof(uint32_t) * d.n_pnt));
     GD_CUDA(cudaMalloc(&c.d_phi, sizeof(double) * 5 * d.n_pnt));
@@ -255,11 +258,12 @@ static int create_context(Context &c, const gd_grid_spec &spec, int device)
     GD_CUDA(cudaMemcpy(c.d_nodes, nodes.data(), sizeof(uint32_t) * d.n_pnt, cudaMemcpyHostToDevice));
     GD_CUDA(cudaMemcpy(c.d_phi, phi.data(), sizeof(double) * 5 * d.n_pnt, cudaMemcpyHostToDevice));
 
+    if ((rc = gain_plan_cells(c))) return rc;
     // analytic weights: dense FP64-built table (transient), compacted to rows
     const size_t na = (size_t)d.hx * d.nx * d.hy * d.hz * d.nyz;
     float *a_dense = nullptr;
     GD_CUDA(cudaMalloc(&a_dense, sizeof(float) * na));
-    int rc = launch_dense_tables(d, c.d_b, a_dense, st);
+    rc = launch_dense_tables(d, c.d_b, a_dense, st);
     if (!rc) rc = build_weight_rows(c, a_dense, st);
     cudaFree(a_dense);
     if (rc) return rc;

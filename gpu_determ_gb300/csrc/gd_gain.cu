@@ -50,10 +50,12 @@ __global__ void __launch_bounds__(kThreads, 1) gain_pair_kernel(GainArgs a)
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ int row_next;
     const Dims &d = a.d;
-    int16_t *cmap = reinterpret_cast<int16_t *>(smem);
-    float *P = reinterpret_cast<float *>(smem + ((d.nxyz * 2 + 15) & ~15));
+    // P_s[class index][CB] first, then the box -> compact map
+    float *P = reinterpret_cast<float *>(smem);
+    int16_t *cmap = reinterpret_cast<int16_t *>(smem + (size_t)d.nclass * CB * sizeof(float));
 
     for (int t = threadIdx.x; t < d.nxyz; t += blockDim.x) cmap[t] = a.cmap[t];
+    for (int t = threadIdx.x; t < d.nclass * CB; t += blockDim.x) P[t] = 0.f;
 
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
     const int cl = lane % CB, grp = lane / CB;
@@ -62,7 +64,11 @@ __global__ void __launch_bounds__(kThreads, 1) gain_pair_kernel(GainArgs a)
     const float *fcol = a.f + (live ? cell : 0);
     const int chunk = blockIdx.y;
     float *part = a.part + (size_t)chunk * d.n_pnt * a.cells_pad + blockIdx.x * CB + cl;
+    const unsigned char *Pc = smem + cl * sizeof(float);
+    const uint2 *rows = reinterpret_cast<const uint2 *>(a.list);
     const int item0 = warp * G + grp, istep = nwarps * G;
+    // extents of the previous s's class box: P is zero outside it
+    int pex = 0, pey = 0, pez = 0;
     __syncthreads();
 
     const int s_begin = a.s_bounds[chunk], s_end = a.s_bounds[chunk + 1];
@@ -74,9 +80,18 @@ __global__ void __launch_bounds__(kThreads, 1) gain_pair_kernel(GainArgs a)
         const int px = sx & 1, py = sy & 1, pz = sz & 1;
         const int nB = ex * ey * ez;
 
-        // 1. pair products P_s[n] -------------------------------------------
-        for (int t = item0; t < nB; t += istep) {
-            const int c2 = t % ez, b2 = (t / ez) % ey, a2 = t / (ez * ey);
+        // 1. pair products P_s[n] on B(D(s)); zeros where only the previous
+        //    s's box had values, so P_s is zero outside B(D(s)) and the rows
+        //    can be summed without testing n against the box.
+        const int ux = max(ex, pex), uy = max(ey, pey), uz = max(ez, pez);
+        const int nU = ux * uy * uz;
+        for (int t = item0; t < nU; t += istep) {
+            const int c2 = t % uz, b2 = (t / uz) % uy, a2 = t / (uz * uy);
+            const int nc = (a2 * d.hy + b2) * d.hz + c2;
+            if (a2 >= ex || b2 >= ey || c2 >= ez) {
+                P[nc * CB + cl] = 0.f;
+                continue;
+            }
             const int nxv = 2 * a2 + px, nyv = 2 * b2 + py, nzv = 2 * c2 + pz;
             const int lx = (sx + nxv) >> 1, l1x = (sx - nxv) >> 1;
             const int ly = (sy + nyv) >> 1, l1y = (sy - nyv) >> 1;
@@ -98,9 +113,11 @@ __global__ void __launch_bounds__(kThreads, 1) gain_pair_kernel(GainArgs a)
             const float f7 = (k7 >= 0 && live) ? __ldg(fcol + (size_t)k7 * ld) : 0.f;
             const float t1 = __fmaf_rn(f0, f1, f2 * f3);
             const float t2 = __fmaf_rn(f4, f5, f6 * f7);
-            const int nc = (a2 * d.hy + b2) * d.hz + c2;
             P[nc * CB + cl] = t1 + t2;
         }
+        pex = ex;
+        pey = ey;
+        pez = ez;
         if (threadIdx.x == 0) row_next = 0;
         __syncthreads();
 
@@ -109,7 +126,6 @@ __global__ void __launch_bounds__(kThreads, 1) gain_pair_kernel(GainArgs a)
         // a time, one per lane group).  Each row's sum is formed by one lane
         // group in entry order and written to targets no other row of this s
         // touches, so the result does not depend on which warp takes it.
-        const uint32_t bound = wentry_bound(Dx >> 1, Dy >> 1, Dz >> 1);
         for (;;) {
             int t0 = 0;
             if (lane == 0) t0 = atomicAdd(&row_next, G);
@@ -140,26 +156,24 @@ __global__ void __launch_bounds__(kThreads, 1) gain_pair_kernel(GainArgs a)
             if (nt == 0) continue;
             const int gbox = (gx * d.ny + gy) * d.nz + gz;
             const int e0 = __ldg(a.list_off + gbox), e1 = __ldg(a.list_off + gbox + 1);
-            const uint2 *rows = reinterpret_cast<const uint2 *>(a.list);
-            const float *Pc = P + cl;
             float acc0 = 0.f, acc1 = 0.f, acc2 = 0.f, acc3 = 0.f;
             int e = e0;
-            for (; e + 3 < e1; e += 4) {
-                const uint2 r0 = __ldg(rows + e), r1 = __ldg(rows + e + 1);
-                const uint2 r2 = __ldg(rows + e + 2), r3 = __ldg(rows + e + 3);
-                if (((bound - r0.x) & kWGuard) == kWGuard)
-                    acc0 = __fmaf_rn(__uint_as_float(r0.y), Pc[(r0.x >> kWClassShift) * CB], acc0);
-                if (((bound - r1.x) & kWGuard) == kWGuard)
-                    acc1 = __fmaf_rn(__uint_as_float(r1.y), Pc[(r1.x >> kWClassShift) * CB], acc1);
-                if (((bound - r2.x) & kWGuard) == kWGuard)
-                    acc2 = __fmaf_rn(__uint_as_float(r2.y), Pc[(r2.x >> kWClassShift) * CB], acc2);
-                if (((bound - r3.x) & kWGuard) == kWGuard)
-                    acc3 = __fmaf_rn(__uint_as_float(r3.y), Pc[(r3.x >> kWClassShift) * CB], acc3);
+            for (; e + 7 < e1; e += 8) {
+                uint2 r[8];
+#pragma unroll
+                for (int k = 0; k < 8; k++) r[k] = __ldg(rows + e + k);
+                acc0 = __fmaf_rn(__uint_as_float(r[0].y), *reinterpret_cast<const float *>(Pc + r[0].x), acc0);
+                acc1 = __fmaf_rn(__uint_as_float(r[1].y), *reinterpret_cast<const float *>(Pc + r[1].x), acc1);
+                acc2 = __fmaf_rn(__uint_as_float(r[2].y), *reinterpret_cast<const float *>(Pc + r[2].x), acc2);
+                acc3 = __fmaf_rn(__uint_as_float(r[3].y), *reinterpret_cast<const float *>(Pc + r[3].x), acc3);
+                acc0 = __fmaf_rn(__uint_as_float(r[4].y), *reinterpret_cast<const float *>(Pc + r[4].x), acc0);
+                acc1 = __fmaf_rn(__uint_as_float(r[5].y), *reinterpret_cast<const float *>(Pc + r[5].x), acc1);
+                acc2 = __fmaf_rn(__uint_as_float(r[6].y), *reinterpret_cast<const float *>(Pc + r[6].x), acc2);
+                acc3 = __fmaf_rn(__uint_as_float(r[7].y), *reinterpret_cast<const float *>(Pc + r[7].x), acc3);
             }
             for (; e < e1; e++) {
                 const uint2 r0 = __ldg(rows + e);
-                if (((bound - r0.x) & kWGuard) == kWGuard)
-                    acc0 = __fmaf_rn(__uint_as_float(r0.y), Pc[(r0.x >> kWClassShift) * CB], acc0);
+                acc0 = __fmaf_rn(__uint_as_float(r0.y), *reinterpret_cast<const float *>(Pc + r0.x), acc0);
             }
             const float acc = (acc0 + acc1) + (acc2 + acc3);
             if (live) {
@@ -189,28 +203,37 @@ __global__ void gain_reduce_kernel(const float *__restrict__ part, int nchunks, 
 
 size_t gain_smem_bytes(const Dims &d, int cb)
 {
-    return (size_t)((d.nxyz * 2 + 15) & ~15) + (size_t)d.nclass * cb * sizeof(float);
+    return (size_t)d.nclass * cb * sizeof(float) + (size_t)((d.nxyz * 2 + 15) & ~15);
 }
 
 }  // namespace
 
-int run_gain(Context &c, const float *f, int ncells, int ld, float *gain, cudaStream_t st)
+int gain_plan_cells(Context &c)
 {
-    const Dims &d = c.d;
     int max_smem = 0;
     GD_CUDA(cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, c.device));
     int cb = 32;
-    while (cb > 4 && gain_smem_bytes(d, cb) > (size_t)max_smem) cb >>= 1;
-    if (gain_smem_bytes(d, cb) > (size_t)max_smem)
+    while (cb > 4 && gain_smem_bytes(c.d, cb) > (size_t)max_smem) cb >>= 1;
+    if (gain_smem_bytes(c.d, cb) > (size_t)max_smem)
         return set_error(GD_ERR_UNSUPPORTED, "velocity grid too large for the gain kernel's shared memory");
+    if ((int64_t)c.d.nclass * cb * 4 >= ((int64_t)1 << 32))
+        return set_error(GD_ERR_UNSUPPORTED, "pair-product array too large");
+    c.gain_cb = cb;
+    c.gain_smem = gain_smem_bytes(c.d, cb);
+    return GD_OK;
+}
+
+int run_gain(Context &c, const float *f, int ncells, int ld, float *gain, cudaStream_t st)
+{
+    const Dims &d = c.d;
+    const int cb = c.gain_cb;
     const size_t smem = gain_smem_bytes(d, cb);
     const int nblk = (ncells + cb - 1) / cb;
     const int cells_pad = nblk * cb;
     // enough chunks of s for about four CTAs per SM, bounded by the partial buffer
     int nchunks = std::max(1, (4 * c.sm_count + nblk - 1) / nblk);
     nchunks = std::min<int64_t>(nchunks, std::min<int64_t>(d.ns, 512));
-    const size_t part_elems = (size_t)nchunks * d.n_pnt * cells_pad;
-    while (nchunks > 1 && part_elems * sizeof(float) > ((size_t)16 << 30)) nchunks--;
+    while (nchunks > 1 && (size_t)nchunks * d.n_pnt * cells_pad * sizeof(float) > ((size_t)16 << 30)) nchunks--;
     // work-balanced chunk boundaries over the linear s order
     std::vector<int> bounds(nchunks + 1);
     const int64_t total = c.s_work_prefix[d.ns];
@@ -271,17 +294,12 @@ int gain_launch_shape(Context &c, int ncells, int *cb_out, size_t *smem_out, int
                       int *chunks_out)
 {
     const Dims &d = c.d;
-    int max_smem = 0;
-    GD_CUDA(cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, c.device));
-    int cb = 32;
-    while (cb > 4 && gain_smem_bytes(d, cb) > (size_t)max_smem) cb >>= 1;
-    if (gain_smem_bytes(d, cb) > (size_t)max_smem)
-        return set_error(GD_ERR_UNSUPPORTED, "velocity grid too large for the gain kernel's shared memory");
+    const int cb = c.gain_cb;
     const int nblk = (ncells + cb - 1) / cb;
     int nchunks = std::max(1, (4 * c.sm_count + nblk - 1) / nblk);
     nchunks = (int)std::min<int64_t>(nchunks, std::min<int64_t>(d.ns, 512));
     *cb_out = cb;
-    *smem_out = gain_smem_bytes(d, cb);
+    *smem_out = c.gain_smem;
     *nblk_out = nblk;
     *chunks_out = nchunks;
     return GD_OK;

@@ -24,31 +24,14 @@ struct Dims {
     float du, dv, dw, d3v;
 };
 
-// One nonzero post-collision weight of the row |g|: meta packs the half
-// components x2, y2, z2 of n in 6-bit fields at bits 0, 6, 12 (bit 5 of each
-// field is a guard bit, so a field-wise "n2 <= D2" test is one subtraction)
-// and the class index of n in bits 18..31; w is the FP32 weight.
+// One nonzero post-collision weight of the row |g|: off is the byte offset
+// of n's pair product in the gain kernel's shared P_s array (class index of
+// n times the kernel's cell block times 4), w the FP32 weight.
 struct WEntry {
-    uint32_t meta;
+    uint32_t off;
     float w;
 };
 static_assert(sizeof(WEntry) == 8, "WEntry must be 8 bytes");
-
-constexpr uint32_t kWGuard = (1u << 5) | (1u << 11) | (1u << 17);
-constexpr int kWClassShift = 18;
-constexpr int kMaxClass = 1 << (32 - kWClassShift);  // class boxes up to 16384 members
-
-__host__ __device__ inline uint32_t wentry_meta(int nc, int x2, int y2, int z2)
-{
-    return (uint32_t)x2 | ((uint32_t)y2 << 6) | ((uint32_t)z2 << 12) | ((uint32_t)nc << kWClassShift);
-}
-
-// Guarded bound for the field-wise test: an entry's n lies in B(D) exactly
-// when ((wentry_bound(D) - meta) & kWGuard) == kWGuard.
-__host__ __device__ inline uint32_t wentry_bound(int dx2, int dy2, int dz2)
-{
-    return (uint32_t)dx2 | ((uint32_t)dy2 << 6) | ((uint32_t)dz2 << 12) | kWGuard;
-}
 
 struct Scratch {
     void *ptr = nullptr;
@@ -76,6 +59,8 @@ struct Context {
     // counts reported by gd_ctx_info
     int64_t pair_products = 0, contraction_terms = 0, scatter_terms = 0;
     bool contraction_exact = false;  // contraction_terms filtered by n in B(D(s))
+    int gain_cb = 32;                // cells per lane row of the gain kernel (fixed per grid)
+    size_t gain_smem = 0;            // its dynamic shared memory
     // scratch owned by the context (grown on demand)
     Scratch scratch;
     int *d_s_bounds = nullptr;  // chunk boundaries for the current launch shape
@@ -118,6 +103,8 @@ int run_relax_q(Context &c, float *f, const float *nu_corr, const float *gain, c
 int run_moments(Context &c, const float *f, int ncells, int ld, double *m5, cudaStream_t st);
 int run_basis(Context &c, float *basis, cudaStream_t st);
 
+// gain kernel shape for this grid: cells per lane row and shared memory (gd_gain.cu)
+int gain_plan_cells(Context &c);
 // gain launch pieces for a caller-provided partial buffer (gd_gain.cu)
 int gain_launch_shape(Context &c, int ncells, int *cb, size_t *smem, int *nblk, int *chunks);
 void gain_chunk_bounds(const Context &c, int nchunks, int *bounds);

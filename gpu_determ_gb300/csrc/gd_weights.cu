@@ -149,8 +149,10 @@ __global__ void dense_b_kernel(Dims d, float *__restrict__ b)
 }
 
 // Row |g| of the compact table: the nonzero a entries over (in1, jn1, kn1),
-// in that lexicographic order.  Pass 1 counts, pass 2 fills.
-__global__ void weight_rows_kernel(Dims d, const float *__restrict__ a, const int *__restrict__ off,
+// in that lexicographic order, each stored with the byte offset of n's pair
+// product in the gain kernel's P_s array (cb cells per class row).  Pass 1
+// counts, pass 2 fills.
+__global__ void weight_rows_kernel(Dims d, int cb, const float *__restrict__ a, const int *__restrict__ off,
                                    int *__restrict__ counts, WEntry *__restrict__ out)
 {
     const int gbox = blockIdx.x * blockDim.x + threadIdx.x;
@@ -168,7 +170,7 @@ __global__ void weight_rows_kernel(Dims d, const float *__restrict__ a, const in
                 if (wv == 0.0f) continue;
                 if (out) {
                     const int nc = (in1 * d.hy + jn1) * d.hz + kn1;
-                    out[pos].meta = wentry_meta(nc, in1, jn1, kn1);
+                    out[pos].off = (uint32_t)nc * (uint32_t)cb * 4u;
                     out[pos].w = wv;
                     pos++;
                 }
@@ -200,7 +202,7 @@ int build_weight_rows(Context &c, const float *a_dense, cudaStream_t st)
     const Dims &d = c.d;
     int *d_counts = nullptr;
     GD_CUDA(cudaMalloc(&d_counts, sizeof(int) * d.nxyz));
-    weight_rows_kernel<<<(d.nxyz + 127) / 128, 128, 0, st>>>(d, a_dense, nullptr, d_counts, nullptr);
+    weight_rows_kernel<<<(d.nxyz + 127) / 128, 128, 0, st>>>(d, c.gain_cb, a_dense, nullptr, d_counts, nullptr);
     cudaError_t e = cudaGetLastError();
     std::vector<int> counts(d.nxyz);
     if (e == cudaSuccess) e = cudaMemcpyAsync(counts.data(), d_counts, sizeof(int) * d.nxyz,
@@ -228,7 +230,7 @@ int build_weight_rows(Context &c, const float *a_dense, cudaStream_t st)
         e = cudaMemcpyAsync(c.d_list_off, off.data(), sizeof(int) * (d.nxyz + 1),
                             cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) {
-        weight_rows_kernel<<<(d.nxyz + 127) / 128, 128, 0, st>>>(d, a_dense, c.d_list_off, nullptr,
+        weight_rows_kernel<<<(d.nxyz + 127) / 128, 128, 0, st>>>(d, c.gain_cb, a_dense, c.d_list_off, nullptr,
                                                                  c.d_list);
         e = cudaGetLastError();
     }
