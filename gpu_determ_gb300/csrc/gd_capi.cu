@@ -7,6 +7,7 @@
 #include <cstring>
 #include <new>
 #include <string>
+#include <unordered_map>
 #include <vector>
 
 #include "gd_internal.h"
@@ -62,88 +63,136 @@ int check_batch(const gd_ctx *ctx, const void *f, int ncells, int ld)
     return GD_OK;
 }
 
-// Cumulative per-s work estimate (pair products, weight-row visits, scatter)
-// in linear s order; used to cut s into chunks of equal work.
-void build_s_schedule(Context &c, const std::vector<int> &row_off)
+// Per-s work in linear s order (pair products, grouped weight-row visits,
+// scatter) and the exact operation counts reported by gd_ctx_info.  Work
+// depends on s only through D(s); each D stands for
+// prod_a (D_a == n_a - 1 ? 1 : 2) pair sums s.
+void build_s_schedule(Context &c, const std::vector<int> &gid_of_gbox)
 {
     const Dims &d = c.d;
-    // per parity class: inclusive 3-D prefix sums of row lengths over the class box
-    std::vector<int64_t> pref((size_t)8 * d.nclass, 0);
-    for (int p = 0; p < 8; p++) {
-        const int px = p & 1, py = (p >> 1) & 1, pz = (p >> 2) & 1;
-        int64_t *P = pref.data() + (size_t)p * d.nclass;
-        for (int a2 = 0; a2 < d.hx; a2++)
-            for (int b2 = 0; b2 < d.hy; b2++)
-                for (int c2 = 0; c2 < d.hz; c2++) {
-                    const int gx = 2 * a2 + px, gy = 2 * b2 + py, gz = 2 * c2 + pz;
-                    const int gbox = (gx * d.ny + gy) * d.nz + gz;
-                    int64_t v = row_off[gbox + 1] - row_off[gbox];
-                    auto at = [&](int x, int y, int z) -> int64_t {
-                        return (x < 0 || y < 0 || z < 0) ? 0 : P[(x * d.hy + y) * d.hz + z];
-                    };
-                    v += at(a2 - 1, b2, c2) + at(a2, b2 - 1, c2) + at(a2, b2, c2 - 1) -
-                         at(a2 - 1, b2 - 1, c2) - at(a2 - 1, b2, c2 - 1) - at(a2, b2 - 1, c2 - 1) +
-                         at(a2 - 1, b2 - 1, c2 - 1);
-                    P[(a2 * d.hy + b2) * d.hz + c2] = v;
-                }
-    }
+    std::vector<int64_t> work_by_D(d.nxyz, 0);
+    std::vector<int> stamp(c.n_groups, -1);
+    const uint32_t unit = (uint32_t)c.gain_cb * 4u;
+    int64_t pairs = 0, terms = 0;
+    for (int Dx = 0; Dx < d.nx; Dx++)
+        for (int Dy = 0; Dy < d.ny; Dy++)
+            for (int Dz = 0; Dz < d.nz; Dz++) {
+                const int Did = (Dx * d.ny + Dy) * d.nz + Dz;
+                const int mult = (Dx == d.nx - 1 ? 1 : 2) * (Dy == d.ny - 1 ? 1 : 2) * (Dz == d.nz - 1 ? 1 : 2);
+                const int dx2 = Dx >> 1, dy2 = Dy >> 1, dz2 = Dz >> 1;
+                int64_t nB = 0, visits = 0, used = 0;
+                for (int gx = Dx & 1; gx <= Dx; gx += 2)
+                    for (int gy = Dy & 1; gy <= Dy; gy += 2)
+                        for (int gz = Dz & 1; gz <= Dz; gz += 2) {
+                            nB++;
+                            const int k = gid_of_gbox[(gx * d.ny + gy) * d.nz + gz];
+                            if (stamp[k] == Did) continue;
+                            stamp[k] = Did;
+                            visits += c.h_grp_row_off[k + 1] - c.h_grp_row_off[k];
+                            for (int e = c.h_grp_row_off[k]; e < c.h_grp_row_off[k + 1]; e++) {
+                                const int nc = (int)(c.h_grp_rows[e].off / unit);
+                                const int z2 = nc % d.hz, y2 = (nc / d.hz) % d.hy, x2 = nc / (d.hz * d.hy);
+                                used += x2 <= dx2 && y2 <= dy2 && z2 <= dz2;
+                            }
+                        }
+                work_by_D[Did] = 12 * nB + visits;
+                pairs += nB * mult;
+                terms += used * mult;
+            }
     c.s_work_prefix.assign(d.ns + 1, 0);
-    int64_t acc = 0, pairs = 0, visits = 0;
+    int64_t acc = 0;
     for (int sx = 0; sx < d.sx; sx++)
         for (int sy = 0; sy < d.sy; sy++)
             for (int sz = 0; sz < d.sz; sz++) {
                 const int64_t sl = ((int64_t)sx * d.sy + sy) * d.sz + sz;
                 const int Dx = std::min(sx, 2 * d.nx - 2 - sx), Dy = std::min(sy, 2 * d.ny - 2 - sy),
                           Dz = std::min(sz, 2 * d.nz - 2 - sz);
-                const int64_t nB = (int64_t)((Dx >> 1) + 1) * ((Dy >> 1) + 1) * ((Dz >> 1) + 1);
-                const int p = (sx & 1) | ((sy & 1) << 1) | ((sz & 1) << 2);
-                const int64_t rows =
-                    pref[(size_t)p * d.nclass + ((Dx >> 1) * d.hy + (Dy >> 1)) * d.hz + (Dz >> 1)];
                 c.s_work_prefix[sl] = acc;
-                acc += 12 * nB + rows;
-                pairs += nB;
-                visits += rows;
+                acc += work_by_D[(Dx * d.ny + Dy) * d.nz + Dz];
             }
     c.s_work_prefix[d.ns] = acc;
     c.pair_products = pairs;
-    c.contraction_terms = visits;
+    c.contraction_terms = terms;
 }
 
-// Exact number of (weight, pair product) terms per cell-eval: for every s the
-// entries of the rows g in B(D(s)) whose n also lies in B(D(s)).  Depends on s
-// only through D(s); each D stands for prod_a (D_a == n_a - 1 ? 1 : 2) sums s.
-int exact_contraction_terms(Context &c, int64_t *out)
+}  // namespace
+
+// Group the per-|g| weight rows: rows with the same parity class and
+// byte-identical (offset, weight) entries are one group.  Groups are ordered
+// by parity class, then by first appearance in box order of g.
+int build_row_groups(Context &c)
 {
     const Dims &d = c.d;
     std::vector<int> off(d.nxyz + 1);
     std::vector<WEntry> rows(c.n_entries + 1);
     GD_CUDA(cudaMemcpy(off.data(), c.d_list_off, sizeof(int) * (d.nxyz + 1), cudaMemcpyDeviceToHost));
     GD_CUDA(cudaMemcpy(rows.data(), c.d_list, sizeof(WEntry) * c.n_entries, cudaMemcpyDeviceToHost));
-    int64_t total = 0;
-    for (int Dx = 0; Dx < d.nx; Dx++)
-        for (int Dy = 0; Dy < d.ny; Dy++)
-            for (int Dz = 0; Dz < d.nz; Dz++) {
-                const int mult = (Dx == d.nx - 1 ? 1 : 2) * (Dy == d.ny - 1 ? 1 : 2) * (Dz == d.nz - 1 ? 1 : 2);
-                const int dx2 = Dx >> 1, dy2 = Dy >> 1, dz2 = Dz >> 1;
-                const uint32_t unit = (uint32_t)c.gain_cb * 4u;
-                int64_t t = 0;
-                for (int gx = Dx & 1; gx <= Dx; gx += 2)
-                    for (int gy = Dy & 1; gy <= Dy; gy += 2)
-                        for (int gz = Dz & 1; gz <= Dz; gz += 2) {
-                            const int gbox = (gx * d.ny + gy) * d.nz + gz;
-                            for (int e = off[gbox]; e < off[gbox + 1]; e++) {
-                                const int nc = (int)(rows[e].off / unit);
-                                const int z2 = nc % d.hz, y2 = (nc / d.hz) % d.hy, x2 = nc / (d.hz * d.hy);
-                                t += x2 <= dx2 && y2 <= dy2 && z2 <= dz2;
-                            }
-                        }
-                total += t * mult;
+    struct Group {
+        int gbox0;  // first member (box index of g), row source
+        std::vector<uint32_t> members;
+    };
+    std::vector<std::vector<Group>> by_class(8);
+    std::vector<std::pair<int, int>> gref(d.nxyz);  // (class, index within class)
+    std::vector<std::unordered_map<uint64_t, std::vector<int>>> index(8);
+    auto same_row = [&](int a, int b) {
+        const int la = off[a + 1] - off[a], lb = off[b + 1] - off[b];
+        return la == lb && std::memcmp(&rows[off[a]], &rows[off[b]], sizeof(WEntry) * la) == 0;
+    };
+    for (int gx = 0; gx < d.nx; gx++)
+        for (int gy = 0; gy < d.ny; gy++)
+            for (int gz = 0; gz < d.nz; gz++) {
+                const int gbox = (gx * d.ny + gy) * d.nz + gz;
+                const int p = (gx & 1) | ((gy & 1) << 1) | ((gz & 1) << 2);
+                uint64_t h = 1469598103934665603ull;  // FNV-1a over the row bytes
+                const unsigned char *bytes = reinterpret_cast<const unsigned char *>(&rows[off[gbox]]);
+                for (size_t t = 0; t < sizeof(WEntry) * (size_t)(off[gbox + 1] - off[gbox]); t++)
+                    h = (h ^ bytes[t]) * 1099511628211ull;
+                int found = -1;
+                for (int k : index[p][h])
+                    if (same_row(by_class[p][k].gbox0, gbox)) {
+                        found = k;
+                        break;
+                    }
+                if (found < 0) {
+                    found = (int)by_class[p].size();
+                    by_class[p].push_back(Group{gbox, {}});
+                    index[p][h].push_back(found);
+                }
+                by_class[p][found].members.push_back(half_pack(gx >> 1, gy >> 1, gz >> 1));
+                gref[gbox] = {p, found};
             }
-    *out = total;
+    c.h_grp_row_off.assign(1, 0);
+    c.h_grp_mem_off.assign(1, 0);
+    c.h_grp_rows.clear();
+    c.h_grp_members.clear();
+    std::vector<int> base(9, 0);
+    for (int p = 0; p < 8; p++) {
+        base[p] = (int)c.h_grp_row_off.size() - 1;
+        c.class_grp_off[p] = base[p];
+        for (const Group &g : by_class[p]) {
+            c.h_grp_rows.insert(c.h_grp_rows.end(), rows.begin() + off[g.gbox0], rows.begin() + off[g.gbox0 + 1]);
+            c.h_grp_row_off.push_back((int)c.h_grp_rows.size());
+            c.h_grp_members.insert(c.h_grp_members.end(), g.members.begin(), g.members.end());
+            c.h_grp_mem_off.push_back((int)c.h_grp_members.size());
+        }
+    }
+    c.n_groups = (int)c.h_grp_row_off.size() - 1;
+    c.class_grp_off[8] = c.n_groups;
+    c.n_grp_entries = (int64_t)c.h_grp_rows.size();
+    std::vector<int> gid(d.nxyz);
+    for (int gbox = 0; gbox < d.nxyz; gbox++) gid[gbox] = base[gref[gbox].first] + gref[gbox].second;
+    GD_CUDA(cudaMalloc(&c.d_grp_row_off, sizeof(int) * (c.n_groups + 1)));
+    GD_CUDA(cudaMalloc(&c.d_grp_rows, sizeof(WEntry) * (c.n_grp_entries + 1)));
+    GD_CUDA(cudaMalloc(&c.d_grp_mem_off, sizeof(int) * (c.n_groups + 1)));
+    GD_CUDA(cudaMalloc(&c.d_grp_members, sizeof(uint32_t) * c.h_grp_members.size()));
+    GD_CUDA(cudaMemcpy(c.d_grp_row_off, c.h_grp_row_off.data(), sizeof(int) * (c.n_groups + 1), cudaMemcpyHostToDevice));
+    GD_CUDA(cudaMemcpy(c.d_grp_rows, c.h_grp_rows.data(), sizeof(WEntry) * c.n_grp_entries, cudaMemcpyHostToDevice));
+    GD_CUDA(cudaMemcpy(c.d_grp_mem_off, c.h_grp_mem_off.data(), sizeof(int) * (c.n_groups + 1), cudaMemcpyHostToDevice));
+    GD_CUDA(cudaMemcpy(c.d_grp_members, c.h_grp_members.data(), sizeof(uint32_t) * c.h_grp_members.size(),
+                       cudaMemcpyHostToDevice));
+    build_s_schedule(c, gid);
     return GD_OK;
 }
-
-}  // namespace
 
 int set_error(int code, const std::string &msg)
 {
@@ -184,6 +233,10 @@ static void destroy_context(Context &c)
     cudaFree(c.d_phi);
     cudaFree(c.d_list_off);
     cudaFree(c.d_list);
+    cudaFree(c.d_grp_row_off);
+    cudaFree(c.d_grp_rows);
+    cudaFree(c.d_grp_mem_off);
+    cudaFree(c.d_grp_members);
     cudaFree(c.d_s_bounds);
     cudaFree(c.d_reduce);
     cudaFree(c.scratch.ptr);
@@ -267,9 +320,7 @@ static int create_context(Context &c, const gd_grid_spec &spec, int device)
     if (!rc) rc = build_weight_rows(c, a_dense, st);
     cudaFree(a_dense);
     if (rc) return rc;
-    std::vector<int> row_off(d.nxyz + 1);
-    GD_CUDA(cudaMemcpy(row_off.data(), c.d_list_off, sizeof(int) * (d.nxyz + 1), cudaMemcpyDeviceToHost));
-    build_s_schedule(c, row_off);
+    if ((rc = build_row_groups(c))) return rc;
     // scatter updates: distinct sign patterns of g whose target lies in the sphere
     int64_t sc = 0;
     for (int sx = 0; sx < d.sx; sx++)
@@ -354,13 +405,6 @@ int gd_ctx_destroy(gd_ctx *ctx)
 int gd_ctx_info(const gd_ctx *ctx, gd_info *out)
 {
     if (!ctx || !out) return set_error(GD_ERR_INVALID_ARG, "NULL argument");
-    if (!ctx->c.contraction_exact) {
-        gd::DeviceGuard g(ctx->c.device);
-        gd::Context &mc = const_cast<gd_ctx *>(ctx)->c;
-        int rc = gd::exact_contraction_terms(mc, &mc.contraction_terms);
-        if (rc) return rc;
-        mc.contraction_exact = true;
-    }
     const gd::Dims &d = ctx->c.d;
     out->nx = d.nx;
     out->ny = d.ny;

@@ -16,12 +16,15 @@
 // Each P is formed once per (s, n) and reused by every output on its collision
 // shell instead of being regathered per (i, i1, n).
 //
+// Rows of the weight table that are bitwise identical (same parity class and
+// same |g|) give identical C_s[g], so each such group is contracted once.
+//
 // Parallel layout: lane = cell (CB cells per row, 32/CB rows per warp), one
 // CTA per (cell block, chunk of s).  A chunk owns its own partial output
 // buffer; within one s all targets (s +- g)/2 are distinct and successive s
-// are separated by barriers, so every partial sum is formed in a fixed
-// order.  A second kernel adds the chunk partials in chunk order.  No atomics:
-// results are bitwise reproducible.
+// are separated by barriers, so every partial sum receives its updates in s
+// order.  A second kernel adds the chunk partials in chunk order.  Results are
+// bitwise reproducible run to run.
 #include "gd_internal.h"
 
 #include <algorithm>
@@ -37,8 +40,11 @@ struct GainArgs {
     const float *f;
     int ld, ncells, cells_pad;
     const int16_t *cmap;
-    const int *list_off;
-    const WEntry *list;
+    const int *grp_row_off;
+    const WEntry *grp_rows;
+    const int *grp_mem_off;
+    const uint32_t *grp_members;
+    int class_grp_off[9];
     const int *s_bounds;
     float *part;  // [chunk][n_pnt][cells_pad]
 };
@@ -65,7 +71,7 @@ __global__ void __launch_bounds__(kThreads, 1) gain_pair_kernel(GainArgs a)
     const int chunk = blockIdx.y;
     float *part = a.part + (size_t)chunk * d.n_pnt * a.cells_pad + blockIdx.x * CB + cl;
     const unsigned char *Pc = smem + cl * sizeof(float);
-    const uint2 *rows = reinterpret_cast<const uint2 *>(a.list);
+    const uint2 *rows = reinterpret_cast<const uint2 *>(a.grp_rows);
     const int item0 = warp * G + grp, istep = nwarps * G;
     // extents of the previous s's class box: P is zero outside it
     int pex = 0, pey = 0, pez = 0;
@@ -121,47 +127,38 @@ __global__ void __launch_bounds__(kThreads, 1) gain_pair_kernel(GainArgs a)
         if (threadIdx.x == 0) row_next = 0;
         __syncthreads();
 
-        // 2./3. contraction with the weight rows and scatter to outputs -------
-        // Rows are handed out through a shared counter (a warp takes G rows at
-        // a time, one per lane group).  Each row's sum is formed by one lane
-        // group in entry order and written to targets no other row of this s
-        // touches, so the result does not depend on which warp takes it.
+        // 2./3. contraction and scatter --------------------------------------
+        // g's whose weight rows are identical form a group: the group's row is
+        // contracted with P_s once and the sum goes to the targets (s +- g)/2 of
+        // every member g in B(D(s)).  Groups are handed out through a shared
+        // counter (a warp takes G at a time, one per lane group).  Each sum is
+        // formed by one lane group in entry order; within one s every target
+        // receives exactly one update and successive s are separated by a
+        // barrier, so every partial sum is updated in s order whichever warp
+        // does the work.
+        const int cls = px | (py << 1) | (pz << 2);
+        const int G0 = a.class_grp_off[cls], nG = a.class_grp_off[cls + 1] - G0;
+        const uint32_t bound = half_bound(Dx >> 1, Dy >> 1, Dz >> 1);
         for (;;) {
             int t0 = 0;
             if (lane == 0) t0 = atomicAdd(&row_next, G);
             t0 = __shfl_sync(0xffffffffu, t0, 0);
-            if (t0 >= nB) break;
+            if (t0 >= nG) break;
             const int t = t0 + grp;
-            if (t >= nB) continue;
-            const int c2 = t % ez, b2 = (t / ez) % ey, a2 = t / (ez * ey);
-            const int gx = 2 * a2 + px, gy = 2 * b2 + py, gz = 2 * c2 + pz;
-            // targets i = (s +- g)/2, distinct sign patterns only; their
-            // partial sums are loaded before the row so the loads overlap it
-            int tgt[8];
-            float old[8];
-            int nt = 0;
-#pragma unroll
-            for (int sg = 0; sg < 8; sg++) {
-                const int sgx = (sg & 1) ? -1 : 1, sgy = (sg & 2) ? -1 : 1, sgz = (sg & 4) ? -1 : 1;
-                const bool dup = (gx == 0 && sgx < 0) || (gy == 0 && sgy < 0) || (gz == 0 && sgz < 0);
-                const int ix = (sx + sgx * gx) >> 1, iy = (sy + sgy * gy) >> 1, iz = (sz + sgz * gz) >> 1;
-                const int k = dup ? -1 : cmap[ix * d.nyz + iy * d.nz + iz];
-                tgt[sg] = k;
-                old[sg] = 0.f;
-                if (k >= 0) {
-                    nt++;
-                    old[sg] = part[(size_t)k * a.cells_pad];
-                }
-            }
-            if (nt == 0) continue;
-            const int gbox = (gx * d.ny + gy) * d.nz + gz;
-            const int e0 = __ldg(a.list_off + gbox), e1 = __ldg(a.list_off + gbox + 1);
+            if (t >= nG) continue;
+            const int k = G0 + t;
+            const int m0 = __ldg(a.grp_mem_off + k), m1 = __ldg(a.grp_mem_off + k + 1);
+            bool any = false;
+            for (int m = m0; m < m1 && !any; m++)
+                any = ((bound - __ldg(a.grp_members + m)) & kHalfGuard) == kHalfGuard;
+            if (!any) continue;
+            const int e0 = __ldg(a.grp_row_off + k), e1 = __ldg(a.grp_row_off + k + 1);
             float acc0 = 0.f, acc1 = 0.f, acc2 = 0.f, acc3 = 0.f;
             int e = e0;
             for (; e + 7 < e1; e += 8) {
                 uint2 r[8];
 #pragma unroll
-                for (int k = 0; k < 8; k++) r[k] = __ldg(rows + e + k);
+                for (int q = 0; q < 8; q++) r[q] = __ldg(rows + e + q);
                 acc0 = __fmaf_rn(__uint_as_float(r[0].y), *reinterpret_cast<const float *>(Pc + r[0].x), acc0);
                 acc1 = __fmaf_rn(__uint_as_float(r[1].y), *reinterpret_cast<const float *>(Pc + r[1].x), acc1);
                 acc2 = __fmaf_rn(__uint_as_float(r[2].y), *reinterpret_cast<const float *>(Pc + r[2].x), acc2);
@@ -176,7 +173,24 @@ __global__ void __launch_bounds__(kThreads, 1) gain_pair_kernel(GainArgs a)
                 acc0 = __fmaf_rn(__uint_as_float(r0.y), *reinterpret_cast<const float *>(Pc + r0.x), acc0);
             }
             const float acc = (acc0 + acc1) + (acc2 + acc3);
-            if (live) {
+            if (!live) continue;
+            // explicit load/add/store: global float reductions flush subnormal
+            // values to zero, and corner-node contributions are subnormal
+            for (int m = m0; m < m1; m++) {
+                const uint32_t mm = __ldg(a.grp_members + m);
+                if (((bound - mm) & kHalfGuard) != kHalfGuard) continue;
+                const int gx = 2 * (int)(mm & 31) + px, gy = 2 * (int)((mm >> 6) & 31) + py,
+                          gz = 2 * (int)((mm >> 12) & 31) + pz;
+                int tgt[8];
+                float old[8];
+#pragma unroll
+                for (int sg = 0; sg < 8; sg++) {
+                    const int sgx = (sg & 1) ? -1 : 1, sgy = (sg & 2) ? -1 : 1, sgz = (sg & 4) ? -1 : 1;
+                    const bool dup = (gx == 0 && sgx < 0) || (gy == 0 && sgy < 0) || (gz == 0 && sgz < 0);
+                    const int ix = (sx + sgx * gx) >> 1, iy = (sy + sgy * gy) >> 1, iz = (sz + sgz * gz) >> 1;
+                    tgt[sg] = dup ? -1 : cmap[ix * d.nyz + iy * d.nz + iz];
+                    old[sg] = tgt[sg] >= 0 ? part[(size_t)tgt[sg] * a.cells_pad] : 0.f;
+                }
 #pragma unroll
                 for (int sg = 0; sg < 8; sg++)
                     if (tgt[sg] >= 0) part[(size_t)tgt[sg] * a.cells_pad] = old[sg] + acc;
@@ -259,7 +273,9 @@ int run_gain(Context &c, const float *f, int ncells, int ld, float *gain, cudaSt
     float *part = static_cast<float *>(c.scratch.ptr);
     GD_CUDA(cudaMemsetAsync(part, 0, part_bytes, st));
 
-    GainArgs a{d, f, ld, ncells, cells_pad, c.d_cmap, c.d_list_off, c.d_list, c.d_s_bounds, part};
+    GainArgs a{d, f, ld, ncells, cells_pad, c.d_cmap, c.d_grp_row_off, c.d_grp_rows, c.d_grp_mem_off,
+               c.d_grp_members, {}, c.d_s_bounds, part};
+    for (int k = 0; k < 9; k++) a.class_grp_off[k] = c.class_grp_off[k];
     dim3 grid(nblk, nchunks);
     switch (cb) {
 #define GD_GAIN_CASE(CBV)                                                                       \
@@ -325,7 +341,9 @@ int launch_gain_pair(Context &c, const float *f, int ncells, int ld, float *gain
     const int nblk = (ncells + cb - 1) / cb;
     const int cells_pad = nblk * cb;
     GD_CUDA(cudaMemsetAsync(part, 0, (size_t)nchunks * d.n_pnt * cells_pad * sizeof(float), st));
-    GainArgs a{d, f, ld, ncells, cells_pad, c.d_cmap, c.d_list_off, c.d_list, d_bounds, part};
+    GainArgs a{d, f, ld, ncells, cells_pad, c.d_cmap, c.d_grp_row_off, c.d_grp_rows, c.d_grp_mem_off,
+               c.d_grp_members, {}, d_bounds, part};
+    for (int k = 0; k < 9; k++) a.class_grp_off[k] = c.class_grp_off[k];
     dim3 grid(nblk, nchunks);
     switch (cb) {
 #define GD_GAIN_CASE(CBV)                                                                       \

@@ -33,6 +33,19 @@ struct WEntry {
 };
 static_assert(sizeof(WEntry) == 8, "WEntry must be 8 bytes");
 
+// Half components (x2, y2, z2) in 6-bit fields whose bit 5 is a guard bit:
+// "x2 <= Dx2 and y2 <= Dy2 and z2 <= Dz2" is
+// ((half_bound(Dx2, Dy2, Dz2) - half_pack(x2, y2, z2)) & kHalfGuard) == kHalfGuard.
+constexpr uint32_t kHalfGuard = (1u << 5) | (1u << 11) | (1u << 17);
+__host__ __device__ inline uint32_t half_pack(int x2, int y2, int z2)
+{
+    return (uint32_t)x2 | ((uint32_t)y2 << 6) | ((uint32_t)z2 << 12);
+}
+__host__ __device__ inline uint32_t half_bound(int dx2, int dy2, int dz2)
+{
+    return half_pack(dx2, dy2, dz2) | kHalfGuard;
+}
+
 struct Scratch {
     void *ptr = nullptr;
     size_t bytes = 0;
@@ -54,11 +67,23 @@ struct Context {
     int *d_list_off = nullptr;    // [nxyz + 1] weight-row offsets by |g| box index
     WEntry *d_list = nullptr;     // nonzero weights, rows in box order of |g|
     int64_t n_entries = 0;
+    // Rows that are bitwise identical (same parity class, same |g|) form one
+    // group; the gain kernel contracts a group once and scatters the result to
+    // every member g.  Groups are ordered by parity class.
+    int n_groups = 0;
+    int class_grp_off[9] = {};      // group range of each parity class
+    int *d_grp_row_off = nullptr;   // [n_groups + 1] into d_grp_rows
+    WEntry *d_grp_rows = nullptr;   // one row per group
+    int *d_grp_mem_off = nullptr;   // [n_groups + 1] into d_grp_members
+    uint32_t *d_grp_members = nullptr;  // member g as guarded half components x2 | y2 << 6 | z2 << 12
+    int64_t n_grp_entries = 0;
+    std::vector<int> h_grp_row_off, h_grp_mem_off;
+    std::vector<uint32_t> h_grp_members;
+    std::vector<WEntry> h_grp_rows;
     // pair-sum schedule for the gain kernel: work-balanced chunk boundaries
     std::vector<int64_t> s_work_prefix;  // [ns + 1] cumulative work in linear s order
     // counts reported by gd_ctx_info
     int64_t pair_products = 0, contraction_terms = 0, scatter_terms = 0;
-    bool contraction_exact = false;  // contraction_terms filtered by n in B(D(s))
     int gain_cb = 32;                // cells per lane row of the gain kernel (fixed per grid)
     size_t gain_smem = 0;            // its dynamic shared memory
     // scratch owned by the context (grown on demand)
@@ -102,6 +127,9 @@ int run_relax_q(Context &c, float *f, const float *nu_corr, const float *gain, c
                 cudaStream_t st);
 int run_moments(Context &c, const float *f, int ncells, int ld, double *m5, cudaStream_t st);
 int run_basis(Context &c, float *basis, cudaStream_t st);
+
+// group identical weight rows (gd_capi.cu)
+int build_row_groups(Context &c);
 
 // gain kernel shape for this grid: cells per lane row and shared memory (gd_gain.cu)
 int gain_plan_cells(Context &c);
