@@ -13,7 +13,7 @@ from __future__ import annotations
 import ctypes as C
 import os
 
-__all__ = ["GDError", "GridSpec", "Context", "lib", "library_path", "DT_COURANT", "DT_FIXED"]
+__all__ = ["GDError", "GridSpec", "Context", "lib", "library_path", "load_options", "DT_COURANT", "DT_FIXED"]
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 _LIB_PATH = os.path.join(_HERE, "libgpu_determ.so")
@@ -35,6 +35,11 @@ class GDError(RuntimeError):
 class _Spec(C.Structure):
     _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int),
                 ("vmin", C.c_float * 3), ("vmax", C.c_float * 3), ("R", C.c_float)]
+
+
+class _Options(C.Structure):
+    _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int), ("nyz", C.c_int), ("nxyz", C.c_int),
+                ("npx", C.c_int)]
 
 
 class _Info(C.Structure):
@@ -75,9 +80,13 @@ def lib():
     L.gd_step.argtypes = [vp, vp, i, i, i, f, vp, vp, vp, vp, vp, vp, vp]
     L.gd_moments.argtypes = [vp, vp, i, i, vp, vp]
     L.gd_gain_noalloc.argtypes = [vp, vp, i, i, vp, vp]
+    L.gd_load_options.argtypes = [C.c_char_p, P(_Options)]
+    L.gd_box_to_compact.argtypes = [vp, vp, i, i, vp, i, vp]
+    L.gd_compact_to_box.argtypes = [vp, vp, i, i, vp, i, vp]
     for name in ("gd_grid_count", "gd_grid_fill", "gd_ctx_create", "gd_ctx_destroy", "gd_ctx_info",
                  "gd_export_tables", "gd_correction_basis", "gd_collision", "gd_project",
-                 "gd_relax", "gd_step", "gd_moments", "gd_gain_noalloc"):
+                 "gd_relax", "gd_step", "gd_moments", "gd_gain_noalloc",
+                 "gd_box_to_compact", "gd_compact_to_box", "gd_load_options"):
         getattr(L, name).restype = i
     _lib = L
     return L
@@ -103,6 +112,13 @@ def _stream(s):
     if isinstance(s, int):
         return s
     return s.cuda_stream
+
+
+def load_options(path: str) -> dict:
+    """Parse a reference options file (gpu.conf): nx, ny, nz, npx, nyz, nxyz."""
+    o = _Options()
+    _check(lib().gd_load_options(str(path).encode(), C.byref(o)))
+    return {k: getattr(o, k) for k, _ in _Options._fields_}
 
 
 class GridSpec:
@@ -188,6 +204,14 @@ class Context:
         _check(lib().gd_step(self._h, _ptr(f), int(ncells), int(ld), int(mode), float(param),
                              _ptr(nu), _ptr(gain), _ptr(q), _ptr(m5), _ptr(time), _ptr(dt),
                              _stream(stream)))
+
+    def box_to_compact(self, box, ncells, ld_box, compact, ld, stream=None):
+        _check(lib().gd_box_to_compact(self._h, _ptr(box), int(ncells), int(ld_box), _ptr(compact), int(ld),
+                                       _stream(stream)))
+
+    def compact_to_box(self, compact, ncells, ld, box, ld_box, stream=None):
+        _check(lib().gd_compact_to_box(self._h, _ptr(compact), int(ncells), int(ld), _ptr(box), int(ld_box),
+                                       _stream(stream)))
 
     def moments(self, f, ncells, ld, m5, stream=None):
         _check(lib().gd_moments(self._h, _ptr(f), int(ncells), int(ld), _ptr(m5), _stream(stream)))

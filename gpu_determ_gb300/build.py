@@ -19,6 +19,8 @@ ROOT = os.path.dirname(PKG)
 CSRC = os.path.join(PKG, "csrc")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libgpu_determ.so")
+APP_SRC = os.path.join(CSRC, "app", "determ_main.cpp")
+APP = os.path.join(PKG, "gd_determ")
 INCLUDE = os.path.join(ROOT, "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -85,6 +87,17 @@ def build(force: bool = False, verbose: bool = False) -> str:
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
         os.replace(LIB + ".tmp", LIB)
+    hdrs = [os.path.join(INCLUDE, "gpu_determ_api.hpp"), os.path.join(INCLUDE, "gpu_determ.h")]
+    if force or not os.path.exists(APP) or os.path.getmtime(APP) < _newest([LIB, APP_SRC] + hdrs):
+        cmd = [nvcc(), "-x", "c++", APP_SRC, "-o", APP + ".tmp", "-std=c++17", "-O2", "-I" + INCLUDE,
+               "-Xcompiler", "-ffp-contract=off", "-L" + PKG, "-lgpu_determ", "-lcudart",
+               "-Xlinker", "-rpath", "-Xlinker", "$ORIGIN"]
+        if verbose:
+            print(" ".join(cmd), flush=True)
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"driver build failed:\n{r.stdout}\n{r.stderr}")
+        os.replace(APP + ".tmp", APP)
     return LIB
 
 

@@ -348,6 +348,9 @@ static int create_context(Context &c, const gd_grid_spec &spec, int device)
 
 using gd::set_error;
 
+// error message setter for the C++ host layer (gd_api.cpp)
+int gd_set_error_message(int code, const std::string &msg) { return gd::set_error(code, msg); }
+
 extern "C" {
 
 int gd_version(void) { return 100; }

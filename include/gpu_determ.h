@@ -79,6 +79,16 @@ int gd_grid_count(const gd_grid_spec *spec, int *n_pnt);
 int gd_grid_fill(const gd_grid_spec *spec, float *u, float *v, float *w, int *ui, int *vi,
                  int *wi, float *steps);
 
+/* ---- options file ------------------------------------------------------ */
+/* "key = value" lines with '#' comments; keys nx, ny, nz, npx (others are
+ * ignored); nyz and nxyz derived.  GD_ERR_IO when the file cannot be opened
+ * ("Can't open <path>"), GD_ERR_INVALID_ARG when a value is not an integer.
+ * Replaces load_options (options.hpp:16, options.cu:34-53). */
+typedef struct {
+    int nx, ny, nz, nyz, nxyz, npx;
+} gd_options;
+int gd_load_options(const char *path, gd_options *out);
+
 /* ---- context ----------------------------------------------------------- */
 /* Binds to `device`, uploads the grid and builds the weight tables on the GPU
  * (FP64 analytic builder, compacted to nonzero entries).  Replaces the
@@ -136,6 +146,14 @@ int gd_step(gd_ctx *ctx, float *f, int ncells, int ld, int mode, float param, fl
  * m5[5*ncells] on the device.  Restates print_moments (determ.cu:123-144)
  * per cell. */
 int gd_moments(gd_ctx *ctx, const float *f, int ncells, int ld, double *m5, gd_stream stream);
+
+/* Layout conversion between the full box [nx*ny*nz][ld_box] of the reference
+ * (determ.cu:107-120) and the compact in-sphere layout [n_pnt][ld]; nodes
+ * outside the sphere come out as 0.  Needed only when R cuts the box. */
+int gd_box_to_compact(gd_ctx *ctx, const float *box, int ncells, int ld_box, float *compact, int ld,
+                      gd_stream stream);
+int gd_compact_to_box(gd_ctx *ctx, const float *compact, int ncells, int ld, float *box, int ld_box,
+                      gd_stream stream);
 
 /* Gain I[i][c] exactly as gd_collision computes it, but with no device
  * allocation of any kind during the call.  No counterpart in the reference:
