@@ -129,9 +129,10 @@ def cpu_baseline(args, seconds):
         o.project(f, nu, gain)
         return time.perf_counter() - t0
 
-    t1 = run(1)
-    nc = max(1, min(64, int(seconds / max(t1, 1e-3))))
-    t = run(nc) if nc > 1 else t1
+    run(1)  # thread pool and page warm-up
+    per_cell = run(2) / 2
+    nc = max(1, min(512, int(seconds / max(per_cell, 1e-4))))
+    t = run(nc)
     return {"value": nc / t, "unit": UNIT, "cores": threads, "kind": "port",
             "sample": f"{nc} cell(s) x 1 step, all {o.n_pnt} nodes, {t:.1f} s"}
 

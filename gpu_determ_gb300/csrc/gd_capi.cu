@@ -67,11 +67,16 @@ int check_batch(const gd_ctx *ctx, const void *f, int ncells, int ld)
 // scatter) and the exact operation counts reported by gd_ctx_info.  Work
 // depends on s only through D(s); each D stands for
 // prod_a (D_a == n_a - 1 ? 1 : 2) pair sums s.
-void build_s_schedule(Context &c, const std::vector<int> &gid_of_gbox)
+int build_s_schedule(Context &c, const std::vector<int> &gid_of_gbox)
 {
     const Dims &d = c.d;
     std::vector<int64_t> work_by_D(d.nxyz, 0);
     std::vector<int> stamp(c.n_groups, -1);
+    std::vector<int> item_off(d.nxyz + 1, 0);
+    std::vector<int4> items;
+    std::vector<uint32_t> members;
+    std::vector<std::vector<uint32_t>> bucket(c.n_groups);
+    std::vector<int> present;
     const uint32_t unit = (uint32_t)c.gain_cb * 4u;
     int64_t pairs = 0, terms = 0;
     for (int Dx = 0; Dx < d.nx; Dx++)
@@ -81,13 +86,17 @@ void build_s_schedule(Context &c, const std::vector<int> &gid_of_gbox)
                 const int mult = (Dx == d.nx - 1 ? 1 : 2) * (Dy == d.ny - 1 ? 1 : 2) * (Dz == d.nz - 1 ? 1 : 2);
                 const int dx2 = Dx >> 1, dy2 = Dy >> 1, dz2 = Dz >> 1;
                 int64_t nB = 0, visits = 0, used = 0;
+                item_off[Did] = (int)items.size();
+                present.clear();
                 for (int gx = Dx & 1; gx <= Dx; gx += 2)
                     for (int gy = Dy & 1; gy <= Dy; gy += 2)
                         for (int gz = Dz & 1; gz <= Dz; gz += 2) {
                             nB++;
                             const int k = gid_of_gbox[(gx * d.ny + gy) * d.nz + gz];
+                            bucket[k].push_back(half_pack(gx >> 1, gy >> 1, gz >> 1));
                             if (stamp[k] == Did) continue;
                             stamp[k] = Did;
+                            present.push_back(k);
                             visits += c.h_grp_row_off[k + 1] - c.h_grp_row_off[k];
                             for (int e = c.h_grp_row_off[k]; e < c.h_grp_row_off[k + 1]; e++) {
                                 const int nc = (int)(c.h_grp_rows[e].off / unit);
@@ -95,6 +104,12 @@ void build_s_schedule(Context &c, const std::vector<int> &gid_of_gbox)
                                 used += x2 <= dx2 && y2 <= dy2 && z2 <= dz2;
                             }
                         }
+                for (int k : present) {
+                    const int mb = (int)members.size();
+                    members.insert(members.end(), bucket[k].begin(), bucket[k].end());
+                    items.push_back(make_int4(k, mb, (int)members.size(), 0));
+                    bucket[k].clear();
+                }
                 work_by_D[Did] = 12 * nB + visits;
                 pairs += nB * mult;
                 terms += used * mult;
@@ -113,6 +128,14 @@ void build_s_schedule(Context &c, const std::vector<int> &gid_of_gbox)
     c.s_work_prefix[d.ns] = acc;
     c.pair_products = pairs;
     c.contraction_terms = terms;
+    item_off[d.nxyz] = (int)items.size();
+    GD_CUDA(cudaMalloc(&c.d_D_item_off, sizeof(int) * (d.nxyz + 1)));
+    GD_CUDA(cudaMalloc(&c.d_D_items, sizeof(int4) * (items.size() + 1)));
+    GD_CUDA(cudaMalloc(&c.d_D_members, sizeof(uint32_t) * (members.size() + 1)));
+    GD_CUDA(cudaMemcpy(c.d_D_item_off, item_off.data(), sizeof(int) * (d.nxyz + 1), cudaMemcpyHostToDevice));
+    GD_CUDA(cudaMemcpy(c.d_D_items, items.data(), sizeof(int4) * items.size(), cudaMemcpyHostToDevice));
+    GD_CUDA(cudaMemcpy(c.d_D_members, members.data(), sizeof(uint32_t) * members.size(), cudaMemcpyHostToDevice));
+    return GD_OK;
 }
 
 }  // namespace
@@ -190,8 +213,7 @@ int build_row_groups(Context &c)
     GD_CUDA(cudaMemcpy(c.d_grp_mem_off, c.h_grp_mem_off.data(), sizeof(int) * (c.n_groups + 1), cudaMemcpyHostToDevice));
     GD_CUDA(cudaMemcpy(c.d_grp_members, c.h_grp_members.data(), sizeof(uint32_t) * c.h_grp_members.size(),
                        cudaMemcpyHostToDevice));
-    build_s_schedule(c, gid);
-    return GD_OK;
+    return build_s_schedule(c, gid);
 }
 
 int set_error(int code, const std::string &msg)
@@ -237,6 +259,9 @@ static void destroy_context(Context &c)
     cudaFree(c.d_grp_rows);
     cudaFree(c.d_grp_mem_off);
     cudaFree(c.d_grp_members);
+    cudaFree(c.d_D_item_off);
+    cudaFree(c.d_D_items);
+    cudaFree(c.d_D_members);
     cudaFree(c.d_s_bounds);
     cudaFree(c.d_reduce);
     cudaFree(c.scratch.ptr);

@@ -42,9 +42,9 @@ struct GainArgs {
     const int16_t *cmap;
     const int *grp_row_off;
     const WEntry *grp_rows;
-    const int *grp_mem_off;
-    const uint32_t *grp_members;
-    int class_grp_off[9];
+    const int *D_item_off;
+    const int4 *D_items;
+    const uint32_t *D_members;
     const int *s_bounds;
     float *part;  // [chunk][n_pnt][cells_pad]
 };
@@ -88,38 +88,45 @@ __global__ void __launch_bounds__(kThreads, 1) gain_pair_kernel(GainArgs a)
 
         // 1. pair products P_s[n] on B(D(s)); zeros where only the previous
         //    s's box had values, so P_s is zero outside B(D(s)) and the rows
-        //    can be summed without testing n against the box.
+        //    can be summed without testing n against the box.  Work is split
+        //    into z-runs (fixed n_x, n_y) so each run decodes its indices once.
         const int ux = max(ex, pex), uy = max(ey, pey), uz = max(ez, pez);
-        const int nU = ux * uy * uz;
-        for (int t = item0; t < nU; t += istep) {
-            const int c2 = t % uz, b2 = (t / uz) % uy, a2 = t / (uz * uy);
-            const int nc = (a2 * d.hy + b2) * d.hz + c2;
-            if (a2 >= ex || b2 >= ey || c2 >= ez) {
-                P[nc * CB + cl] = 0.f;
+        const int nRuns = ux * uy;
+        for (int r = item0; r < nRuns; r += istep) {
+            const int a2 = r / uy, b2 = r - a2 * uy;
+            float *Prun = P + (size_t)((a2 * d.hy + b2) * d.hz) * CB + cl;
+            if (a2 >= ex || b2 >= ey) {
+                for (int c2 = 0; c2 < uz; c2++) Prun[c2 * CB] = 0.f;
                 continue;
             }
-            const int nxv = 2 * a2 + px, nyv = 2 * b2 + py, nzv = 2 * c2 + pz;
-            const int lx = (sx + nxv) >> 1, l1x = (sx - nxv) >> 1;
-            const int ly = (sy + nyv) >> 1, l1y = (sy - nyv) >> 1;
-            const int lz = (sz + nzv) >> 1, l1z = (sz - nzv) >> 1;
-            const int X0 = lx * d.nyz, X1 = l1x * d.nyz;
-            const int Y0 = ly * d.nz, Y1 = l1y * d.nz;
-            const int k0 = cmap[X0 + Y0 + lz], k1 = cmap[X1 + Y1 + l1z];
-            const int k2 = cmap[X0 + Y1 + l1z], k3 = cmap[X1 + Y0 + lz];
-            const int k4 = cmap[X0 + Y0 + l1z], k5 = cmap[X1 + Y1 + lz];
-            const int k6 = cmap[X0 + Y1 + lz], k7 = cmap[X1 + Y0 + l1z];
+            const int nxv = 2 * a2 + px, nyv = 2 * b2 + py;
+            const int X0 = ((sx + nxv) >> 1) * d.nyz, X1 = ((sx - nxv) >> 1) * d.nyz;
+            const int Y0 = ((sy + nyv) >> 1) * d.nz, Y1 = ((sy - nyv) >> 1) * d.nz;
+            const int A = X0 + Y0, B = X1 + Y1, Cc = X0 + Y1, Dd = X1 + Y0;
             const int ld = a.ld;
-            const float f0 = (k0 >= 0 && live) ? __ldg(fcol + (size_t)k0 * ld) : 0.f;
-            const float f1 = (k1 >= 0 && live) ? __ldg(fcol + (size_t)k1 * ld) : 0.f;
-            const float f2 = (k2 >= 0 && live) ? __ldg(fcol + (size_t)k2 * ld) : 0.f;
-            const float f3 = (k3 >= 0 && live) ? __ldg(fcol + (size_t)k3 * ld) : 0.f;
-            const float f4 = (k4 >= 0 && live) ? __ldg(fcol + (size_t)k4 * ld) : 0.f;
-            const float f5 = (k5 >= 0 && live) ? __ldg(fcol + (size_t)k5 * ld) : 0.f;
-            const float f6 = (k6 >= 0 && live) ? __ldg(fcol + (size_t)k6 * ld) : 0.f;
-            const float f7 = (k7 >= 0 && live) ? __ldg(fcol + (size_t)k7 * ld) : 0.f;
-            const float t1 = __fmaf_rn(f0, f1, f2 * f3);
-            const float t2 = __fmaf_rn(f4, f5, f6 * f7);
-            P[nc * CB + cl] = t1 + t2;
+            for (int c2 = 0; c2 < uz; c2++) {
+                if (c2 >= ez) {
+                    Prun[c2 * CB] = 0.f;
+                    continue;
+                }
+                const int nzv = 2 * c2 + pz;
+                const int lz = (sz + nzv) >> 1, l1z = (sz - nzv) >> 1;
+                const int k0 = cmap[A + lz], k1 = cmap[B + l1z];
+                const int k2 = cmap[Cc + l1z], k3 = cmap[Dd + lz];
+                const int k4 = cmap[A + l1z], k5 = cmap[B + lz];
+                const int k6 = cmap[Cc + lz], k7 = cmap[Dd + l1z];
+                const float f0 = (k0 >= 0 && live) ? __ldg(fcol + (size_t)k0 * ld) : 0.f;
+                const float f1 = (k1 >= 0 && live) ? __ldg(fcol + (size_t)k1 * ld) : 0.f;
+                const float f2 = (k2 >= 0 && live) ? __ldg(fcol + (size_t)k2 * ld) : 0.f;
+                const float f3 = (k3 >= 0 && live) ? __ldg(fcol + (size_t)k3 * ld) : 0.f;
+                const float f4 = (k4 >= 0 && live) ? __ldg(fcol + (size_t)k4 * ld) : 0.f;
+                const float f5 = (k5 >= 0 && live) ? __ldg(fcol + (size_t)k5 * ld) : 0.f;
+                const float f6 = (k6 >= 0 && live) ? __ldg(fcol + (size_t)k6 * ld) : 0.f;
+                const float f7 = (k7 >= 0 && live) ? __ldg(fcol + (size_t)k7 * ld) : 0.f;
+                const float t1 = __fmaf_rn(f0, f1, f2 * f3);
+                const float t2 = __fmaf_rn(f4, f5, f6 * f7);
+                Prun[c2 * CB] = t1 + t2;
+            }
         }
         pex = ex;
         pey = ey;
@@ -128,31 +135,26 @@ __global__ void __launch_bounds__(kThreads, 1) gain_pair_kernel(GainArgs a)
         __syncthreads();
 
         // 2./3. contraction and scatter --------------------------------------
-        // g's whose weight rows are identical form a group: the group's row is
-        // contracted with P_s once and the sum goes to the targets (s +- g)/2 of
-        // every member g in B(D(s)).  Groups are handed out through a shared
-        // counter (a warp takes G at a time, one per lane group).  Each sum is
-        // formed by one lane group in entry order; within one s every target
-        // receives exactly one update and successive s are separated by a
-        // barrier, so every partial sum is updated in s order whichever warp
-        // does the work.
-        const int cls = px | (py << 1) | (pz << 2);
-        const int G0 = a.class_grp_off[cls], nG = a.class_grp_off[cls + 1] - G0;
-        const uint32_t bound = half_bound(Dx >> 1, Dy >> 1, Dz >> 1);
+        // The work items of D(s) are the row groups with a member in B(D(s))
+        // (rows of g's with equal |g| and parity are bitwise identical), each
+        // with its members in B(D(s)).  A group's row is contracted with P_s
+        // once; the sum goes to the targets (s +- g)/2 of every member g.
+        // Items are handed out through a shared counter (a warp takes G at a
+        // time, one per lane group).  Each sum is formed by one lane group in
+        // entry order; within one s every target receives exactly one update
+        // and successive s are separated by a barrier, so every partial sum is
+        // updated in s order whichever warp does the work.
+        const int Did = (Dx * d.ny + Dy) * d.nz + Dz;
+        const int it0 = __ldg(a.D_item_off + Did), nIt = __ldg(a.D_item_off + Did + 1) - it0;
         for (;;) {
             int t0 = 0;
             if (lane == 0) t0 = atomicAdd(&row_next, G);
             t0 = __shfl_sync(0xffffffffu, t0, 0);
-            if (t0 >= nG) break;
+            if (t0 >= nIt) break;
             const int t = t0 + grp;
-            if (t >= nG) continue;
-            const int k = G0 + t;
-            const int m0 = __ldg(a.grp_mem_off + k), m1 = __ldg(a.grp_mem_off + k + 1);
-            bool any = false;
-            for (int m = m0; m < m1 && !any; m++)
-                any = ((bound - __ldg(a.grp_members + m)) & kHalfGuard) == kHalfGuard;
-            if (!any) continue;
-            const int e0 = __ldg(a.grp_row_off + k), e1 = __ldg(a.grp_row_off + k + 1);
+            if (t >= nIt) continue;
+            const int4 item = __ldg(a.D_items + it0 + t);
+            const int e0 = __ldg(a.grp_row_off + item.x), e1 = __ldg(a.grp_row_off + item.x + 1);
             float acc0 = 0.f, acc1 = 0.f, acc2 = 0.f, acc3 = 0.f;
             int e = e0;
             for (; e + 7 < e1; e += 8) {
@@ -176,19 +178,21 @@ __global__ void __launch_bounds__(kThreads, 1) gain_pair_kernel(GainArgs a)
             if (!live) continue;
             // explicit load/add/store: global float reductions flush subnormal
             // values to zero, and corner-node contributions are subnormal
-            for (int m = m0; m < m1; m++) {
-                const uint32_t mm = __ldg(a.grp_members + m);
-                if (((bound - mm) & kHalfGuard) != kHalfGuard) continue;
+            for (int m = item.y; m < item.z; m++) {
+                const uint32_t mm = __ldg(a.D_members + m);
                 const int gx = 2 * (int)(mm & 31) + px, gy = 2 * (int)((mm >> 6) & 31) + py,
                           gz = 2 * (int)((mm >> 12) & 31) + pz;
+                // per axis the two target coordinates (s - g)/2 and (s + g)/2
+                const int X0 = ((sx - gx) >> 1) * d.nyz, X1 = X0 + gx * d.nyz;
+                const int Y0 = ((sy - gy) >> 1) * d.nz, Y1 = Y0 + gy * d.nz;
+                const int Z0 = (sz - gz) >> 1, Z1 = Z0 + gz;
                 int tgt[8];
                 float old[8];
 #pragma unroll
                 for (int sg = 0; sg < 8; sg++) {
-                    const int sgx = (sg & 1) ? -1 : 1, sgy = (sg & 2) ? -1 : 1, sgz = (sg & 4) ? -1 : 1;
-                    const bool dup = (gx == 0 && sgx < 0) || (gy == 0 && sgy < 0) || (gz == 0 && sgz < 0);
-                    const int ix = (sx + sgx * gx) >> 1, iy = (sy + sgy * gy) >> 1, iz = (sz + sgz * gz) >> 1;
-                    tgt[sg] = dup ? -1 : cmap[ix * d.nyz + iy * d.nz + iz];
+                    const bool hx = sg & 1, hy = (sg >> 1) & 1, hz = (sg >> 2) & 1;
+                    const bool dup = (hx && gx == 0) || (hy && gy == 0) || (hz && gz == 0);
+                    tgt[sg] = dup ? -1 : cmap[(hx ? X1 : X0) + (hy ? Y1 : Y0) + (hz ? Z1 : Z0)];
                     old[sg] = tgt[sg] >= 0 ? part[(size_t)tgt[sg] * a.cells_pad] : 0.f;
                 }
 #pragma unroll
@@ -273,9 +277,8 @@ int run_gain(Context &c, const float *f, int ncells, int ld, float *gain, cudaSt
     float *part = static_cast<float *>(c.scratch.ptr);
     GD_CUDA(cudaMemsetAsync(part, 0, part_bytes, st));
 
-    GainArgs a{d, f, ld, ncells, cells_pad, c.d_cmap, c.d_grp_row_off, c.d_grp_rows, c.d_grp_mem_off,
-               c.d_grp_members, {}, c.d_s_bounds, part};
-    for (int k = 0; k < 9; k++) a.class_grp_off[k] = c.class_grp_off[k];
+    GainArgs a{d, f, ld, ncells, cells_pad, c.d_cmap, c.d_grp_row_off, c.d_grp_rows, c.d_D_item_off,
+               c.d_D_items, c.d_D_members, c.d_s_bounds, part};
     dim3 grid(nblk, nchunks);
     switch (cb) {
 #define GD_GAIN_CASE(CBV)                                                                       \
@@ -341,9 +344,8 @@ int launch_gain_pair(Context &c, const float *f, int ncells, int ld, float *gain
     const int nblk = (ncells + cb - 1) / cb;
     const int cells_pad = nblk * cb;
     GD_CUDA(cudaMemsetAsync(part, 0, (size_t)nchunks * d.n_pnt * cells_pad * sizeof(float), st));
-    GainArgs a{d, f, ld, ncells, cells_pad, c.d_cmap, c.d_grp_row_off, c.d_grp_rows, c.d_grp_mem_off,
-               c.d_grp_members, {}, d_bounds, part};
-    for (int k = 0; k < 9; k++) a.class_grp_off[k] = c.class_grp_off[k];
+    GainArgs a{d, f, ld, ncells, cells_pad, c.d_cmap, c.d_grp_row_off, c.d_grp_rows, c.d_D_item_off,
+               c.d_D_items, c.d_D_members, d_bounds, part};
     dim3 grid(nblk, nchunks);
     switch (cb) {
 #define GD_GAIN_CASE(CBV)                                                                       \

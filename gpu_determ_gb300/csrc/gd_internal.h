@@ -77,6 +77,11 @@ struct Context {
     int *d_grp_mem_off = nullptr;   // [n_groups + 1] into d_grp_members
     uint32_t *d_grp_members = nullptr;  // member g as guarded half components x2 | y2 << 6 | z2 << 12
     int64_t n_grp_entries = 0;
+    // Work items per D = (Dx, Dy, Dz) (box-indexed like g): the row groups with
+    // a member in B(D), each with the list of its members that lie in B(D).
+    int *d_D_item_off = nullptr;   // [nxyz + 1] into d_D_items
+    int4 *d_D_items = nullptr;     // {group, member begin, member end, 0}
+    uint32_t *d_D_members = nullptr;  // member g as half_pack(x2, y2, z2)
     std::vector<int> h_grp_row_off, h_grp_mem_off;
     std::vector<uint32_t> h_grp_members;
     std::vector<WEntry> h_grp_rows;
