@@ -99,6 +99,7 @@ int build_s_schedule(Context &c, const std::vector<int> &gid_of_gbox)
                             present.push_back(k);
                             visits += c.h_grp_row_off[k + 1] - c.h_grp_row_off[k];
                             for (int e = c.h_grp_row_off[k]; e < c.h_grp_row_off[k + 1]; e++) {
+                                if (c.h_grp_rows[e].w == 0.0f) continue;  // row padding
                                 const int nc = (int)(c.h_grp_rows[e].off / unit);
                                 const int z2 = nc % d.hz, y2 = (nc / d.hz) % d.hy, x2 = nc / (d.hz * d.hy);
                                 used += x2 <= dx2 && y2 <= dy2 && z2 <= dz2;
@@ -193,7 +194,10 @@ int build_row_groups(Context &c)
         base[p] = (int)c.h_grp_row_off.size() - 1;
         c.class_grp_off[p] = base[p];
         for (const Group &g : by_class[p]) {
+            // rows are padded with zero-weight entries (offset 0) to a multiple
+            // of 8, so the kernel reads them in aligned 16-byte pairs with no tail
             c.h_grp_rows.insert(c.h_grp_rows.end(), rows.begin() + off[g.gbox0], rows.begin() + off[g.gbox0 + 1]);
+            while (c.h_grp_rows.size() % 8) c.h_grp_rows.push_back(WEntry{0u, 0.0f});
             c.h_grp_row_off.push_back((int)c.h_grp_rows.size());
             c.h_grp_members.insert(c.h_grp_members.end(), g.members.begin(), g.members.end());
             c.h_grp_mem_off.push_back((int)c.h_grp_members.size());

@@ -104,28 +104,25 @@ __global__ void __launch_bounds__(kThreads, 1) gain_pair_kernel(GainArgs a)
             const int Y0 = ((sy + nyv) >> 1) * d.nz, Y1 = ((sy - nyv) >> 1) * d.nz;
             const int A = X0 + Y0, B = X1 + Y1, Cc = X0 + Y1, Dd = X1 + Y0;
             const int ld = a.ld;
-            for (int c2 = 0; c2 < uz; c2++) {
-                if (c2 >= ez) {
-                    Prun[c2 * CB] = 0.f;
-                    continue;
-                }
-                const int nzv = 2 * c2 + pz;
-                const int lz = (sz + nzv) >> 1, l1z = (sz - nzv) >> 1;
-                const int k0 = cmap[A + lz], k1 = cmap[B + l1z];
-                const int k2 = cmap[Cc + l1z], k3 = cmap[Dd + lz];
-                const int k4 = cmap[A + l1z], k5 = cmap[B + lz];
-                const int k6 = cmap[Cc + lz], k7 = cmap[Dd + l1z];
-                const float f0 = (k0 >= 0 && live) ? __ldg(fcol + (size_t)k0 * ld) : 0.f;
-                const float f1 = (k1 >= 0 && live) ? __ldg(fcol + (size_t)k1 * ld) : 0.f;
-                const float f2 = (k2 >= 0 && live) ? __ldg(fcol + (size_t)k2 * ld) : 0.f;
-                const float f3 = (k3 >= 0 && live) ? __ldg(fcol + (size_t)k3 * ld) : 0.f;
-                const float f4 = (k4 >= 0 && live) ? __ldg(fcol + (size_t)k4 * ld) : 0.f;
-                const float f5 = (k5 >= 0 && live) ? __ldg(fcol + (size_t)k5 * ld) : 0.f;
-                const float f6 = (k6 >= 0 && live) ? __ldg(fcol + (size_t)k6 * ld) : 0.f;
-                const float f7 = (k7 >= 0 && live) ? __ldg(fcol + (size_t)k7 * ld) : 0.f;
-                const float t1 = __fmaf_rn(f0, f1, f2 * f3);
-                const float t2 = __fmaf_rn(f4, f5, f6 * f7);
-                Prun[c2 * CB] = t1 + t2;
+            for (int c2 = ez; c2 < uz; c2++) Prun[c2 * CB] = 0.f;
+            // two pair products per iteration: 16 independent loads in flight
+            for (int c2 = 0; c2 < ez; c2 += 2) {
+                const bool two = c2 + 1 < ez;
+                const int nz0 = 2 * c2 + pz, nz1 = nz0 + 2;
+                const int lz0 = (sz + nz0) >> 1, l1z0 = (sz - nz0) >> 1;
+                const int lz1 = two ? lz0 + 1 : lz0, l1z1 = two ? l1z0 - 1 : l1z0;
+                const int k0 = cmap[A + lz0], k1 = cmap[B + l1z0], k2 = cmap[Cc + l1z0], k3 = cmap[Dd + lz0];
+                const int k4 = cmap[A + l1z0], k5 = cmap[B + lz0], k6 = cmap[Cc + lz0], k7 = cmap[Dd + l1z0];
+                const int j0 = cmap[A + lz1], j1 = cmap[B + l1z1], j2 = cmap[Cc + l1z1], j3 = cmap[Dd + lz1];
+                const int j4 = cmap[A + l1z1], j5 = cmap[B + lz1], j6 = cmap[Cc + lz1], j7 = cmap[Dd + l1z1];
+#define GD_F(k) (((k) >= 0 && live) ? __ldg(fcol + (size_t)(k) * ld) : 0.f)
+                const float f0 = GD_F(k0), f1 = GD_F(k1), f2 = GD_F(k2), f3 = GD_F(k3);
+                const float f4 = GD_F(k4), f5 = GD_F(k5), f6 = GD_F(k6), f7 = GD_F(k7);
+                const float h0 = GD_F(j0), h1 = GD_F(j1), h2 = GD_F(j2), h3 = GD_F(j3);
+                const float h4 = GD_F(j4), h5 = GD_F(j5), h6 = GD_F(j6), h7 = GD_F(j7);
+#undef GD_F
+                Prun[c2 * CB] = __fmaf_rn(f0, f1, f2 * f3) + __fmaf_rn(f4, f5, f6 * f7);
+                if (two) Prun[(c2 + 1) * CB] = __fmaf_rn(h0, h1, h2 * h3) + __fmaf_rn(h4, h5, h6 * h7);
             }
         }
         pex = ex;
@@ -155,25 +152,36 @@ __global__ void __launch_bounds__(kThreads, 1) gain_pair_kernel(GainArgs a)
             if (t >= nIt) continue;
             const int4 item = __ldg(a.D_items + it0 + t);
             const int e0 = __ldg(a.grp_row_off + item.x), e1 = __ldg(a.grp_row_off + item.x + 1);
+            // rows are 8-entry padded and 16-byte aligned: two entries per
+            // load, 16 entries per batch
             float acc0 = 0.f, acc1 = 0.f, acc2 = 0.f, acc3 = 0.f;
-            int e = e0;
-            for (; e + 7 < e1; e += 8) {
-                uint2 r[8];
+            const uint4 *rp = reinterpret_cast<const uint4 *>(rows + e0);
+            const uint4 *rend = reinterpret_cast<const uint4 *>(rows + e1);
+#define GD_MAC(acc, wv, ov) acc = __fmaf_rn(__uint_as_float(wv), *reinterpret_cast<const float *>(Pc + (ov)), acc)
+            for (; rp + 8 <= rend; rp += 8) {
+                uint4 r[8];
 #pragma unroll
-                for (int q = 0; q < 8; q++) r[q] = __ldg(rows + e + q);
-                acc0 = __fmaf_rn(__uint_as_float(r[0].y), *reinterpret_cast<const float *>(Pc + r[0].x), acc0);
-                acc1 = __fmaf_rn(__uint_as_float(r[1].y), *reinterpret_cast<const float *>(Pc + r[1].x), acc1);
-                acc2 = __fmaf_rn(__uint_as_float(r[2].y), *reinterpret_cast<const float *>(Pc + r[2].x), acc2);
-                acc3 = __fmaf_rn(__uint_as_float(r[3].y), *reinterpret_cast<const float *>(Pc + r[3].x), acc3);
-                acc0 = __fmaf_rn(__uint_as_float(r[4].y), *reinterpret_cast<const float *>(Pc + r[4].x), acc0);
-                acc1 = __fmaf_rn(__uint_as_float(r[5].y), *reinterpret_cast<const float *>(Pc + r[5].x), acc1);
-                acc2 = __fmaf_rn(__uint_as_float(r[6].y), *reinterpret_cast<const float *>(Pc + r[6].x), acc2);
-                acc3 = __fmaf_rn(__uint_as_float(r[7].y), *reinterpret_cast<const float *>(Pc + r[7].x), acc3);
+                for (int q = 0; q < 8; q++) r[q] = __ldg(rp + q);
+#pragma unroll
+                for (int q = 0; q < 8; q += 2) {
+                    GD_MAC(acc0, r[q].y, r[q].x);
+                    GD_MAC(acc1, r[q].w, r[q].z);
+                    GD_MAC(acc2, r[q + 1].y, r[q + 1].x);
+                    GD_MAC(acc3, r[q + 1].w, r[q + 1].z);
+                }
             }
-            for (; e < e1; e++) {
-                const uint2 r0 = __ldg(rows + e);
-                acc0 = __fmaf_rn(__uint_as_float(r0.y), *reinterpret_cast<const float *>(Pc + r0.x), acc0);
+            if (rp < rend) {
+                const uint4 r01 = __ldg(rp), r23 = __ldg(rp + 1), r45 = __ldg(rp + 2), r67 = __ldg(rp + 3);
+                GD_MAC(acc0, r01.y, r01.x);
+                GD_MAC(acc1, r01.w, r01.z);
+                GD_MAC(acc2, r23.y, r23.x);
+                GD_MAC(acc3, r23.w, r23.z);
+                GD_MAC(acc0, r45.y, r45.x);
+                GD_MAC(acc1, r45.w, r45.z);
+                GD_MAC(acc2, r67.y, r67.x);
+                GD_MAC(acc3, r67.w, r67.z);
             }
+#undef GD_MAC
             const float acc = (acc0 + acc1) + (acc2 + acc3);
             if (!live) continue;
             // explicit load/add/store: global float reductions flush subnormal
