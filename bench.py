@@ -130,9 +130,10 @@ def cpu_baseline(args, seconds):
         return time.perf_counter() - t0
 
     run(1)  # thread pool and page warm-up
-    per_cell = run(2) / 2
-    nc = max(1, min(512, int(seconds / max(per_cell, 1e-4))))
-    t = run(nc)
+    nc, t = 2, run(2)
+    while t < 0.6 * seconds and nc < 2048:  # grow the sample to the target length
+        nc = min(2048, max(nc * 2, int(nc * seconds / max(t, 1e-3))))
+        t = run(nc)
     return {"value": nc / t, "unit": UNIT, "cores": threads, "kind": "port",
             "sample": f"{nc} cell(s) x 1 step, all {o.n_pnt} nodes, {t:.1f} s"}
 

@@ -232,6 +232,28 @@ size_t gain_smem_bytes(const Dims &d, int cb)
     return (size_t)d.nclass * cb * sizeof(float) + (size_t)((d.nxyz * 2 + 15) & ~15);
 }
 
+// Number of s-chunks for nblk cell blocks: at least 2 CTAs per SM, then the
+// count (up to 64 chunks, or 512 when a few blocks must fill the GPU) whose
+// CTA total fills the last wave best; ties go to fewer chunks.
+int gain_chunk_count(const Context &c, int nblk)
+{
+    const int sms = std::max(1, c.sm_count);
+    const int lo = std::max(1, (2 * sms + nblk - 1) / nblk);
+    const int hi = std::max(lo, std::min(lo + 64, 512));
+    int best = lo;
+    double best_fill = -1.0;
+    for (int k = lo; k <= hi; k++) {
+        const int64_t ctas = (int64_t)nblk * k;
+        const double fill = (double)ctas / (double)(((ctas + sms - 1) / sms) * sms);
+        if (fill > best_fill + 1e-9) {
+            best_fill = fill;
+            best = k;
+        }
+        if (fill > 0.999) break;
+    }
+    return (int)std::min<int64_t>(best, c.d.ns);
+}
+
 }  // namespace
 
 int gain_plan_cells(Context &c)
@@ -256,9 +278,9 @@ int run_gain(Context &c, const float *f, int ncells, int ld, float *gain, cudaSt
     const size_t smem = gain_smem_bytes(d, cb);
     const int nblk = (ncells + cb - 1) / cb;
     const int cells_pad = nblk * cb;
-    // enough chunks of s for about four CTAs per SM, bounded by the partial buffer
-    int nchunks = std::max(1, (4 * c.sm_count + nblk - 1) / nblk);
-    nchunks = std::min<int64_t>(nchunks, std::min<int64_t>(d.ns, 512));
+    // chunks of s: at least two CTAs per SM, whole waves preferred (one CTA
+    // per SM fits), bounded by the partial buffer
+    int nchunks = gain_chunk_count(c, nblk);
     while (nchunks > 1 && (size_t)nchunks * d.n_pnt * cells_pad * sizeof(float) > ((size_t)16 << 30)) nchunks--;
     // work-balanced chunk boundaries over the linear s order
     std::vector<int> bounds(nchunks + 1);
@@ -323,8 +345,7 @@ int gain_launch_shape(Context &c, int ncells, int *cb_out, size_t *smem_out, int
     const Dims &d = c.d;
     const int cb = c.gain_cb;
     const int nblk = (ncells + cb - 1) / cb;
-    int nchunks = std::max(1, (4 * c.sm_count + nblk - 1) / nblk);
-    nchunks = (int)std::min<int64_t>(nchunks, std::min<int64_t>(d.ns, 512));
+    const int nchunks = gain_chunk_count(c, nblk);
     *cb_out = cb;
     *smem_out = c.gain_smem;
     *nblk_out = nblk;
