@@ -2,7 +2,7 @@
 
 Workload: 20^3 velocity lattice on [-5,5]^3 cut to the sphere R=4.8 (3648
 nodes), a batch of spatial cells of seeded Maxwellian mixtures; one step =
-loss nu + gain I + FP64 conservation projection + relaxation (fixed dt).
+loss nu + gain I + FP64 conservation projection + relaxation (Courant dt).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
@@ -45,7 +45,7 @@ def parse():
     p.add_argument("--grid", type=int, default=20)
     p.add_argument("--radius", type=float, default=4.8)
     p.add_argument("--cells", type=int, default=4096)
-    p.add_argument("--dt", type=float, default=0.05)
+    p.add_argument("--courant", type=float, default=0.5)
     p.add_argument("--seed", type=int, default=0)
     p.add_argument("--cpu-seconds", type=float, default=15.0,
                    help="target length of the bounded CPU-baseline sample")
@@ -55,7 +55,7 @@ def parse():
 
 def workload(args, ncells):
     return {"workload": f"plain collision step, {args.grid}^3 lattice [-5,5]^3 cut to R={args.radius}",
-            "cells": ncells, "dt": args.dt, "dt_mode": "fixed",
+            "cells": ncells, "dt_mode": f"courant {args.courant} (dt = courant / max nu, as relax_f)",
             "inputs": "seeded Maxwellian mixtures: 1-3 components, n~LogN(0,0.3), u~N(0,0.7^2), T~U[0.6,1.8]",
             "l2": "256 MiB buffer written between timed steps (inside the timed region)"}
 
@@ -185,7 +185,7 @@ def run_ours(args):
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
 
     def step():
-        ctx.step(f, nc, nc, gd.DT_FIXED, args.dt, stream=stream)
+        ctx.step(f, nc, nc, gd.DT_COURANT, args.courant, stream=stream)
 
     for _ in range(args.warmup):
         step()
@@ -226,7 +226,7 @@ def run_ours(args):
     for _ in range(args.steps):
         flush.fill_(1)
         fdev.copy_(pinned_in, non_blocking=True)
-        ctx.step(fdev, nc, nc, gd.DT_FIXED, args.dt, stream=stream)
+        ctx.step(fdev, nc, nc, gd.DT_COURANT, args.courant, stream=stream)
         pinned_out.copy_(fdev, non_blocking=True)
     e1.record(stream)
     barrier()
@@ -271,7 +271,7 @@ def run_ours(args):
             "data": "synthetic", "config": workload(args, nc),
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
                     "ms_per_step": ms_e2e / args.steps},
-            "gpu_launches": 6 * args.steps,
+            "gpu_launches": 7 * args.steps,
             "clocks": clk.summary(), "roofline": roof}
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(args, args.cpu_seconds)
