@@ -13,7 +13,8 @@ from __future__ import annotations
 import ctypes as C
 import os
 
-__all__ = ["GDError", "GridSpec", "Context", "lib", "library_path", "load_options", "DT_COURANT", "DT_FIXED"]
+__all__ = ["GDError", "GridSpec", "Context", "CollisionMatrix", "lib", "library_path", "load_options",
+           "DT_COURANT", "DT_FIXED", "CMATRIX_BF16", "CMATRIX_BF16X3"]
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 _LIB_PATH = os.path.join(_HERE, "libgpu_determ.so")
@@ -21,6 +22,8 @@ _lib = None
 
 DT_COURANT = 0
 DT_FIXED = 1
+CMATRIX_BF16 = 0
+CMATRIX_BF16X3 = 1
 
 _ERRORS = {1: "invalid argument", 2: "CUDA error", 3: "out of memory", 4: "unsupported",
            5: "singular system", 6: "I/O error"}
@@ -81,12 +84,16 @@ def lib():
     L.gd_moments.argtypes = [vp, vp, i, i, vp, vp]
     L.gd_gain_noalloc.argtypes = [vp, vp, i, i, vp, vp]
     L.gd_load_options.argtypes = [C.c_char_p, P(_Options)]
+    L.gd_cmatrix_create.argtypes = [vp, i, P(vp)]
+    L.gd_cmatrix_gain.argtypes = [vp, vp, i, i, vp, vp]
+    L.gd_cmatrix_destroy.argtypes = [vp]
     L.gd_box_to_compact.argtypes = [vp, vp, i, i, vp, i, vp]
     L.gd_compact_to_box.argtypes = [vp, vp, i, i, vp, i, vp]
     for name in ("gd_grid_count", "gd_grid_fill", "gd_ctx_create", "gd_ctx_destroy", "gd_ctx_info",
                  "gd_export_tables", "gd_correction_basis", "gd_collision", "gd_project",
                  "gd_relax", "gd_step", "gd_moments", "gd_gain_noalloc",
-                 "gd_box_to_compact", "gd_compact_to_box", "gd_load_options"):
+                 "gd_box_to_compact", "gd_compact_to_box", "gd_load_options", "gd_cmatrix_create",
+                 "gd_cmatrix_gain", "gd_cmatrix_destroy"):
         getattr(L, name).restype = i
     _lib = L
     return L
@@ -215,3 +222,28 @@ class Context:
 
     def moments(self, f, ncells, ld, m5, stream=None):
         _check(lib().gd_moments(self._h, _ptr(f), int(ncells), int(ld), _ptr(m5), _stream(stream)))
+
+
+class CollisionMatrix:
+    """Dense collision matrices G_i of a context on the device and the
+    tensor-core gain I_i = f^T G_i f (modes CMATRIX_BF16, CMATRIX_BF16X3)."""
+
+    def __init__(self, ctx: Context, mode: int = CMATRIX_BF16X3):
+        self.ctx = ctx
+        self.mode = mode
+        self._h = C.c_void_p()
+        _check(lib().gd_cmatrix_create(ctx._h, int(mode), C.byref(self._h)))
+
+    def gain(self, f, ncells, ld, gain, stream=None):
+        _check(lib().gd_cmatrix_gain(self._h, _ptr(f), int(ncells), int(ld), _ptr(gain), _stream(stream)))
+
+    def close(self):
+        if self._h:
+            lib().gd_cmatrix_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

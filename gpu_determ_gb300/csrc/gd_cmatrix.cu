@@ -1,0 +1,560 @@
+// gd_cmatrix.cu -- collision-matrix form of the gain on the tensor cores (sm_103a).
+//
+// The gain is a bilinear form in f: I_i = sum_{a,b} G_i[a][b] f_a f_b.  With
+// s = a + b, d = a - b (lattice offsets) the reference's enumeration
+// (collision_integral.cu:75-188: partner i1 = s - i, post-collision offset
+// n = |d|, four sign patterns) gives the symmetric matrix
+//   G_i[a][b] = m(d) * w(|2i - s|, |d|) * [s - i in the box],
+//   m(d) = (d_x == 0 ? 1 : 1/2) * (d_y == 0 ? 2 : 1) * (d_z == 0 ? 2 : 1),
+// with w the analytic weight table (compute_matrix.cu:505-562).  G is stored
+// dense in BF16 (optionally as hi + lo parts), G[i][b][a] with a contiguous.
+//
+// Contraction: for output node i and 128 cells c,
+//   D[c][b] = sum_a F[c][a] G_i[a][b]   (tcgen05.mma, BF16 x BF16 -> FP32 in TMEM)
+//   I[i][c] = sum_b D[c][b] f[b][c]      (epilogue, FP32)
+// One CTA per (128-cell tile, i).  Warp 0 issues TMA loads of F (cells x 64 a)
+// and G_i (256 b x 64 a) into a ring of shared-memory stages (128-byte
+// swizzle); warp 1 issues the MMAs (M = 128, N = 256, K = 16) into one of two
+// TMEM accumulators; warps 2..5 read the finished accumulator with tcgen05.ld
+// and fold it into the per-cell sums while the next one is being filled.
+// Every mbarrier wait is bounded: on time-out the CTA records an error and
+// stops issuing work instead of waiting forever.
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <string>
+#include <vector>
+
+#include "gd_internal.h"
+
+struct gd_ctx {
+    gd::Context c;
+};
+
+namespace gd {
+namespace {
+
+constexpr int BM = 128;  // cells per tile (MMA M, TMEM lanes)
+constexpr int BN = 256;  // b per accumulator tile (MMA N, TMEM columns)
+constexpr int BK = 64;   // a per stage (128 bytes of BF16: one swizzle row)
+constexpr int kThreads = 192;
+constexpr uint32_t kTileA = BM * BK * 2;  // 16 KB
+constexpr uint32_t kTileB = BN * BK * 2;  // 32 KB
+constexpr uint32_t kWaitLimit = 1u << 20;  // bounded mbarrier polls per wait
+
+struct CmParams {
+    int ns;       // in-sphere nodes
+    int ns_k;     // padded node count (multiple of BK)
+    int ncells, ld;
+    const float *f;  // [ns][ld] FP32 distribution (epilogue)
+    float *gain;     // [ns][ld]
+    int *err;        // set to 1 when a wait times out
+};
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p)
+{
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint32_t bar)
+{
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity)
+{
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// Bounded wait for the phase with the given parity; false (and *err = 1)
+// when it did not complete.  Also gives up as soon as another CTA has
+// recorded a time-out, so a failing launch ends quickly.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int *err)
+{
+    for (uint32_t it = 0; it < kWaitLimit; it++) {
+        if (mbar_try_wait(bar, parity)) return true;
+        if ((it & 255u) == 255u && *(volatile int *)err) return false;
+    }
+    atomicExch(err, 1);
+    return false;
+}
+
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap *map, int c0, int c1, uint32_t bar)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];"
+        ::"r"(dst), "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(bar)
+        : "memory");
+}
+
+__device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap *map, int c0, int c1, int c2,
+                                            uint32_t bar)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];"
+        ::"r"(dst), "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(bar)
+        : "memory");
+}
+
+// Shared-memory matrix descriptor: K-major operand in the 128-byte swizzle
+// layout TMA writes (rows of 128 bytes, 8-row groups 1024 bytes apart).
+__device__ __forceinline__ uint64_t umma_desc(uint32_t addr)
+{
+    uint64_t d = (uint64_t)((addr & 0x3FFFFu) >> 4);  // start address
+    d |= (uint64_t)1 << 16;                           // leading byte offset (unused for this layout)
+    d |= (uint64_t)(1024u >> 4) << 32;                // stride byte offset: 8 rows x 128 B
+    d |= (uint64_t)1 << 46;                           // descriptor version
+    d |= (uint64_t)2 << 61;                           // 128-byte swizzle
+    return d;
+}
+
+// Instruction descriptor, kind::f16: A, B BF16 (K-major), D FP32, M = BM, N = BN.
+constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) |
+                            ((uint32_t)(BM >> 4) << 24);
+
+__device__ __forceinline__ void umma_bf16(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t accum)
+{
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}"
+        ::"r"(d_tmem), "l"(adesc), "l"(bdesc), "r"(kIdesc), "r"(accum)
+        : "memory");
+}
+
+__device__ __forceinline__ void umma_commit(uint32_t bar)
+{
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
+                 : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float *v)
+{
+    uint32_t r[32];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+        "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, "
+        "%16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+          "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+          "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int j = 0; j < 32; j++) v[j] = __uint_as_float(r[j]);
+}
+
+// NPASS = 1: D = F_hi G_hi.  NPASS = 3: D = F_hi G_hi + F_hi G_lo + F_lo G_hi.
+template <int NPASS>
+__global__ void __launch_bounds__(kThreads, 1)
+    cmatrix_gain_kernel(const __grid_constant__ CUtensorMap tmFh, const __grid_constant__ CUtensorMap tmFl,
+                        const __grid_constant__ CUtensorMap tmGh, const __grid_constant__ CUtensorMap tmGl,
+                        CmParams p)
+{
+    constexpr int NPARTS = NPASS == 1 ? 1 : 2;
+    constexpr int S = NPASS == 1 ? 4 : 2;  // pipeline stages
+    constexpr uint32_t kStage = NPARTS * (kTileA + kTileB);
+    extern __shared__ __align__(1024) unsigned char dsmem[];
+    // 1024-byte aligned tile area
+    unsigned char *base = reinterpret_cast<unsigned char *>(
+        (reinterpret_cast<uintptr_t>(dsmem) + 1023) & ~static_cast<uintptr_t>(1023));
+    __shared__ __align__(8) uint64_t full_bar[S], empty_bar[S], accf_bar[2], acce_bar[2];
+    __shared__ uint32_t tmem_base_holder;
+    __shared__ int abort_flag;
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int m_tile = blockIdx.x, node = blockIdx.y;
+    const int num_k = p.ns_k / BK;
+    const int num_n = (p.ns + BN - 1) / BN;
+
+    if (threadIdx.x == 0) abort_flag = *(volatile int *)p.err;
+    __syncthreads();
+    if (abort_flag) return;  // an earlier CTA timed out: do no work
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < S; s++) {
+            mbar_init(smem_u32(&full_bar[s]), 1);
+            mbar_init(smem_u32(&empty_bar[s]), 1);
+        }
+        for (int b = 0; b < 2; b++) {
+            mbar_init(smem_u32(&accf_bar[b]), 1);
+            mbar_init(smem_u32(&acce_bar[b]), 4);  // one arrival per epilogue warp
+        }
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 1) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                         smem_u32(&tmem_base_holder)),
+                     "r"(2 * BN)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    }
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = tmem_base_holder;
+
+    if (warp == 0) {
+        // ---- TMA producer ----------------------------------------------------
+        if (lane == 0) {
+            const int total = num_n * num_k;
+            for (int it = 0; it < total; it++) {
+                const int s = it % S;
+                const uint32_t ph = (uint32_t)(it / S) & 1u;
+                if (!mbar_wait(smem_u32(&empty_bar[s]), ph ^ 1u, p.err)) {
+                    abort_flag = 1;
+                    break;
+                }
+                if (*(volatile int *)&abort_flag) break;
+                const int n = it / num_k, k = it % num_k;
+                unsigned char *st = base + (size_t)s * kStage;
+                const uint32_t fb = smem_u32(&full_bar[s]);
+                mbar_expect_tx(fb, kStage);
+                tma_load_2d(smem_u32(st), &tmFh, k * BK, m_tile * BM, fb);
+                tma_load_3d(smem_u32(st + kTileA), &tmGh, k * BK, n * BN, node, fb);
+                if (NPARTS == 2) {
+                    tma_load_2d(smem_u32(st + kTileA + kTileB), &tmFl, k * BK, m_tile * BM, fb);
+                    tma_load_3d(smem_u32(st + 2 * kTileA + kTileB), &tmGl, k * BK, n * BN, node, fb);
+                }
+            }
+        }
+    } else if (warp == 1) {
+        // ---- MMA issuer --------------------------------------------------------
+        if (lane == 0) {
+            bool ok = true;
+            for (int n = 0; n < num_n && ok; n++) {
+                const int buf = n & 1;
+                const uint32_t use = (uint32_t)(n >> 1);
+                if (!mbar_wait(smem_u32(&acce_bar[buf]), (use & 1u) ^ 1u, p.err)) {
+                    ok = false;
+                    break;
+                }
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                const uint32_t d_tmem = tmem + (uint32_t)(buf * BN);
+                for (int k = 0; k < num_k; k++) {
+                    const int it = n * num_k + k;
+                    const int s = it % S;
+                    const uint32_t ph = (uint32_t)(it / S) & 1u;
+                    if (!mbar_wait(smem_u32(&full_bar[s]), ph, p.err)) {
+                        ok = false;
+                        break;
+                    }
+                    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                    const uint32_t st = smem_u32(base + (size_t)s * kStage);
+                    const uint32_t aH = st, bH = st + kTileA;
+                    const uint32_t aL = st + kTileA + kTileB, bL = st + 2 * kTileA + kTileB;
+#pragma unroll
+                    for (int kk = 0; kk < BK / 16; kk++) {
+                        const uint32_t off = (uint32_t)kk * 32u;  // 16 BF16 along K
+                        const uint32_t acc = (k > 0 || kk > 0) ? 1u : 0u;
+                        umma_bf16(d_tmem, umma_desc(aH + off), umma_desc(bH + off), acc);
+                        if (NPASS == 3) {
+                            umma_bf16(d_tmem, umma_desc(aH + off), umma_desc(bL + off), 1u);
+                            umma_bf16(d_tmem, umma_desc(aL + off), umma_desc(bH + off), 1u);
+                        }
+                    }
+                    umma_commit(smem_u32(&empty_bar[s]));
+                }
+                if (!ok) break;
+                umma_commit(smem_u32(&accf_bar[buf]));
+            }
+            if (!ok) abort_flag = 1;
+        }
+    } else {
+        // ---- epilogue: warps 2..5 own TMEM lane quadrants (warp % 4) -------------
+        const int quad = warp & 3;
+        const int row = quad * 32 + lane;
+        const int cell = m_tile * BM + row;
+        const bool live = cell < p.ncells;
+        float sum = 0.f;
+        for (int n = 0; n < num_n; n++) {
+            const int buf = n & 1;
+            const uint32_t use = (uint32_t)(n >> 1);
+            bool ok = true;
+            if (lane == 0) ok = mbar_wait(smem_u32(&accf_bar[buf]), use & 1u, p.err);
+            ok = __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
+            if (!ok) break;
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const uint32_t taddr = tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(buf * BN);
+            for (int c0 = 0; c0 < BN; c0 += 32) {
+                float v[32];
+                tmem_ld32(taddr + (uint32_t)c0, v);
+                const int b0 = n * BN + c0;
+                if (live) {
+#pragma unroll
+                    for (int j = 0; j < 32; j++) {
+                        const int b = b0 + j;
+                        if (b < p.ns) sum = __fmaf_rn(v[j], __ldg(p.f + (size_t)b * p.ld + cell), sum);
+                    }
+                }
+            }
+            asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+            __syncwarp();
+            if (lane == 0) mbar_arrive(smem_u32(&acce_bar[buf]));
+        }
+        if (live) p.gain[(size_t)node * p.ld + cell] = sum;
+    }
+    __syncthreads();
+    if (warp == 1) {
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * BN) : "memory");
+    }
+}
+
+// G[i][b][a] for i < ns, b, a < ns_k (zero for padding): hi = bf16(v),
+// lo = bf16(v - hi) with v = m(d) w(|2i - s|, |d|) [s - i in box].
+__global__ void assemble_g_kernel(Dims d, int ns_k, const uint32_t *__restrict__ nodes,
+                                  const float *__restrict__ w_dense, __nv_bfloat16 *__restrict__ gh,
+                                  __nv_bfloat16 *__restrict__ gl)
+{
+    const int64_t rows = (int64_t)d.n_pnt * ns_k;  // (i, b) rows of ns_k entries
+    const int vec = ns_k / 8;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < rows * vec;
+         t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t r = t / vec;
+        const int a0 = (int)(t % vec) * 8;
+        const int i = (int)(r / ns_k), b = (int)(r % ns_k);
+        __align__(16) __nv_bfloat16 hv[8], lv[8];
+        const uint32_t qi = nodes[i];
+        const int ix = qi & 1023, iy = (qi >> 10) & 1023, iz = qi >> 20;
+        const bool bin = b < d.n_pnt;
+        const uint32_t qb = bin ? nodes[b] : 0u;
+        const int bx = qb & 1023, by = (qb >> 10) & 1023, bz = qb >> 20;
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+            const int a = a0 + j;
+            float v = 0.f;
+            if (bin && a < d.n_pnt) {
+                const uint32_t qa = nodes[a];
+                const int ax = qa & 1023, ay = (qa >> 10) & 1023, az = qa >> 20;
+                const int sx = ax + bx, sy = ay + by, sz = az + bz;
+                const int jx = sx - ix, jy = sy - iy, jz = sz - iz;  // partner i1
+                if (jx >= 0 && jx < d.nx && jy >= 0 && jy < d.ny && jz >= 0 && jz < d.nz) {
+                    const int dx = abs(ax - bx), dy = abs(ay - by), dz = abs(az - bz);
+                    const int gx = abs(2 * ix - sx), gy = abs(2 * iy - sy), gz = abs(2 * iz - sz);
+                    const int64_t widx =
+                        ((int64_t)((dx >> 1) * d.nx + gx) * (d.hy * d.hz) + (dy >> 1) * d.hz + (dz >> 1)) * d.nyz +
+                        gy * d.nz + gz;
+                    const float m = (dx == 0 ? 1.f : 0.5f) * (dy == 0 ? 2.f : 1.f) * (dz == 0 ? 2.f : 1.f);
+                    v = m * w_dense[widx];
+                }
+            }
+            hv[j] = __float2bfloat16_rn(v);
+            lv[j] = __float2bfloat16_rn(v - __bfloat162float(hv[j]));
+        }
+        const size_t o = (size_t)r * ns_k + a0;
+        *reinterpret_cast<uint4 *>(gh + o) = *reinterpret_cast<const uint4 *>(hv);
+        if (gl) *reinterpret_cast<uint4 *>(gl + o) = *reinterpret_cast<const uint4 *>(lv);
+    }
+}
+
+// F[c][a] (BF16 hi/lo, a contiguous, padded to ns_k) from f[a][c] (FP32).
+__global__ void convert_f_kernel(const float *__restrict__ f, int ns, int ns_k, int ncells, int ld,
+                                 __nv_bfloat16 *__restrict__ fh, __nv_bfloat16 *__restrict__ fl)
+{
+    __shared__ float tile[32][33];
+    const int a0 = blockIdx.x * 32, c0 = blockIdx.y * 32;
+    for (int r = threadIdx.y; r < 32; r += blockDim.y) {
+        const int a = a0 + r, c = c0 + threadIdx.x;
+        tile[r][threadIdx.x] = (a < ns && c < ncells) ? f[(size_t)a * ld + c] : 0.f;
+    }
+    __syncthreads();
+    for (int r = threadIdx.y; r < 32; r += blockDim.y) {
+        const int c = c0 + r, a = a0 + threadIdx.x;
+        if (c < ncells && a < ns_k) {
+            const float v = tile[threadIdx.x][r];
+            const __nv_bfloat16 h = __float2bfloat16_rn(v);
+            fh[(size_t)c * ns_k + a] = h;
+            if (fl) fl[(size_t)c * ns_k + a] = __float2bfloat16_rn(v - __bfloat162float(h));
+        }
+    }
+}
+
+using EncodeTiled = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                 const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                 CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+int get_encoder(EncodeTiled *out)
+{
+    static EncodeTiled fn = nullptr;
+    if (!fn) {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        cudaError_t e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q);
+        if (e != cudaSuccess || q != cudaDriverEntryPointSuccess || !p)
+            return set_error(GD_ERR_CUDA, "cuTensorMapEncodeTiled is not available");
+        fn = reinterpret_cast<EncodeTiled>(p);
+    }
+    *out = fn;
+    return GD_OK;
+}
+
+int encode(EncodeTiled fn, CUtensorMap *m, void *ptr, int rank, const cuuint64_t *dims, const cuuint64_t *strides,
+           const cuuint32_t *box)
+{
+    const cuuint32_t es[3] = {1, 1, 1};
+    CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, (cuuint32_t)rank, ptr, dims, strides, box, es,
+                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return set_error(GD_ERR_CUDA, "cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
+    return GD_OK;
+}
+
+}  // namespace
+}  // namespace gd
+
+struct gd_cmatrix {
+    gd_ctx *ctx = nullptr;
+    int mode = 0;  // GD_CMATRIX_BF16 or GD_CMATRIX_BF16X3
+    int ns = 0, ns_k = 0;
+    __nv_bfloat16 *gh = nullptr, *gl = nullptr;
+    __nv_bfloat16 *fh = nullptr, *fl = nullptr;
+    int f_cells = 0;
+    int *err = nullptr;
+};
+
+extern "C" int gd_cmatrix_create(gd_ctx *ctx, int mode, gd_cmatrix **out)
+{
+    using namespace gd;
+    if (!ctx || !out) return set_error(GD_ERR_INVALID_ARG, "NULL argument");
+    if (mode != GD_CMATRIX_BF16 && mode != GD_CMATRIX_BF16X3) return set_error(GD_ERR_INVALID_ARG, "unknown mode");
+    *out = nullptr;
+    Context &c = ctx->c;
+    const Dims &d = c.d;
+    int major = 0;
+    GD_CUDA(cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, c.device));
+    if (major < 10) return set_error(GD_ERR_UNSUPPORTED, "the collision-matrix path needs tcgen05 (sm_100 family)");
+    gd_cmatrix *h = new gd_cmatrix();
+    h->ctx = ctx;
+    h->mode = mode;
+    h->ns = d.n_pnt;
+    h->ns_k = (d.n_pnt + BK - 1) / BK * BK;
+    const size_t elems = (size_t)h->ns * h->ns_k * h->ns_k;
+    size_t free_b = 0, total_b = 0;
+    GD_CUDA(cudaMemGetInfo(&free_b, &total_b));
+    const size_t need = elems * 2 * (mode == GD_CMATRIX_BF16X3 ? 2 : 1);
+    if (need + ((size_t)1 << 30) > free_b) {
+        delete h;
+        return set_error(GD_ERR_OUT_OF_MEMORY, "collision matrices need " + std::to_string(need >> 20) +
+                                                   " MiB; free device memory is " + std::to_string(free_b >> 20) + " MiB");
+    }
+    float *w = nullptr;
+    const size_t na = (size_t)d.hx * d.nx * d.hy * d.hz * d.nyz;
+    cudaError_t e = cudaMalloc(&h->gh, elems * 2);
+    if (e == cudaSuccess && mode == GD_CMATRIX_BF16X3) e = cudaMalloc(&h->gl, elems * 2);
+    if (e == cudaSuccess) e = cudaMalloc(&h->err, sizeof(int));
+    if (e == cudaSuccess) e = cudaMalloc(&w, na * sizeof(float));
+    int rc = GD_OK;
+    if (e != cudaSuccess) rc = cuda_error(e, "collision-matrix allocation");
+    if (!rc) rc = launch_dense_tables(d, nullptr, w, nullptr);
+    if (!rc) {
+        const int64_t work = (int64_t)h->ns * h->ns_k * (h->ns_k / 8);
+        const int blocks = (int)std::min<int64_t>((work + 255) / 256, (int64_t)c.sm_count * 64);
+        assemble_g_kernel<<<blocks, 256>>>(d, h->ns_k, c.d_nodes, w, h->gh, h->gl);
+        e = cudaGetLastError();
+        if (e == cudaSuccess) e = cudaMemset(h->err, 0, sizeof(int));
+        if (e == cudaSuccess) e = cudaDeviceSynchronize();
+        if (e != cudaSuccess) rc = cuda_error(e, "collision-matrix assembly");
+    }
+    cudaFree(w);
+    if (rc) {
+        cudaFree(h->gh);
+        cudaFree(h->gl);
+        cudaFree(h->err);
+        delete h;
+        return rc;
+    }
+    *out = h;
+    return GD_OK;
+}
+
+extern "C" int gd_cmatrix_destroy(gd_cmatrix *h)
+{
+    if (!h) return GD_OK;
+    cudaFree(h->gh);
+    cudaFree(h->gl);
+    cudaFree(h->fh);
+    cudaFree(h->fl);
+    cudaFree(h->err);
+    delete h;
+    return GD_OK;
+}
+
+extern "C" int gd_cmatrix_gain(gd_cmatrix *h, const float *f, int ncells, int ld, float *gain, gd_stream stream)
+{
+    using namespace gd;
+    if (!h || !f || !gain) return set_error(GD_ERR_INVALID_ARG, "NULL argument");
+    if (ncells < 1 || ld < ncells) return set_error(GD_ERR_INVALID_ARG, "need 1 <= ncells <= ld");
+    cudaStream_t st = (cudaStream_t)stream;
+    const bool split = h->mode == GD_CMATRIX_BF16X3;
+    if (h->f_cells < ncells) {
+        cudaFree(h->fh);
+        cudaFree(h->fl);
+        h->fh = h->fl = nullptr;
+        h->f_cells = 0;
+        GD_CUDA(cudaMalloc(&h->fh, (size_t)ncells * h->ns_k * 2));
+        if (split) GD_CUDA(cudaMalloc(&h->fl, (size_t)ncells * h->ns_k * 2));
+        h->f_cells = ncells;
+    }
+    dim3 cb(32, 8), cg((h->ns_k + 31) / 32, (ncells + 31) / 32);
+    convert_f_kernel<<<cg, cb, 0, st>>>(f, h->ns, h->ns_k, ncells, ld, h->fh, split ? h->fl : nullptr);
+    GD_CUDA(cudaGetLastError());
+
+    EncodeTiled enc;
+    int rc = get_encoder(&enc);
+    if (rc) return rc;
+    CUtensorMap tFh, tFl, tGh, tGl;
+    const cuuint64_t fdims[2] = {(cuuint64_t)h->ns_k, (cuuint64_t)ncells};
+    const cuuint64_t fstr[1] = {(cuuint64_t)h->ns_k * 2};
+    const cuuint32_t fbox[2] = {BK, BM};
+    const cuuint64_t gdims[3] = {(cuuint64_t)h->ns_k, (cuuint64_t)h->ns_k, (cuuint64_t)h->ns};
+    const cuuint64_t gstr[2] = {(cuuint64_t)h->ns_k * 2, (cuuint64_t)h->ns_k * h->ns_k * 2};
+    const cuuint32_t gbox[3] = {BK, BN, 1};
+    if ((rc = encode(enc, &tFh, h->fh, 2, fdims, fstr, fbox))) return rc;
+    if ((rc = encode(enc, &tGh, h->gh, 3, gdims, gstr, gbox))) return rc;
+    if (split) {
+        if ((rc = encode(enc, &tFl, h->fl, 2, fdims, fstr, fbox))) return rc;
+        if ((rc = encode(enc, &tGl, h->gl, 3, gdims, gstr, gbox))) return rc;
+    } else {
+        tFl = tFh;
+        tGl = tGh;
+    }
+    CmParams prm{h->ns, h->ns_k, ncells, ld, f, gain, h->err};
+    dim3 grid((ncells + BM - 1) / BM, h->ns);
+    const size_t smem = (split ? 2 * 2 * (kTileA + kTileB) : 4 * (kTileA + kTileB)) + 1024;
+    if (split) {
+        GD_CUDA(cudaFuncSetAttribute(cmatrix_gain_kernel<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        cmatrix_gain_kernel<3><<<grid, kThreads, smem, st>>>(tFh, tFl, tGh, tGl, prm);
+    } else {
+        GD_CUDA(cudaFuncSetAttribute(cmatrix_gain_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        cmatrix_gain_kernel<1><<<grid, kThreads, smem, st>>>(tFh, tFl, tGh, tGl, prm);
+    }
+    GD_CUDA(cudaGetLastError());
+    // the kernel records a time-out instead of hanging; report it
+    int flag = 0;
+    GD_CUDA(cudaMemcpyAsync(&flag, h->err, sizeof(int), cudaMemcpyDeviceToHost, st));
+    GD_CUDA(cudaStreamSynchronize(st));
+    if (flag) return set_error(GD_ERR_CUDA, "collision-matrix kernel: a pipeline wait timed out");
+    return GD_OK;
+}

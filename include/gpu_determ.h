@@ -147,6 +147,22 @@ int gd_step(gd_ctx *ctx, float *f, int ncells, int ld, int mode, float param, fl
  * per cell. */
 int gd_moments(gd_ctx *ctx, const float *f, int ncells, int ld, double *m5, gd_stream stream);
 
+/* ---- collision-matrix path (tensor cores) ------------------------------ */
+/* The gain as the bilinear form I_i = sum_ab G_i[a][b] f_a f_b with the dense
+ * collision matrices G_i assembled on the GPU from the analytic weights
+ * (n_pnt^3 BF16 entries, twice that for GD_CMATRIX_BF16X3) and contracted on
+ * the tcgen05 tensor cores with FP32 accumulation.  GD_CMATRIX_BF16 rounds
+ * f and G to BF16 (relative error ~1e-3 on I); GD_CMATRIX_BF16X3 splits both
+ * into BF16 hi + lo parts and sums hi*hi + hi*lo + lo*hi (~1e-5).  The loss
+ * and the FP64 projection are unchanged (gd_collision with gain = NULL, then
+ * gd_project).  No reference counterpart: the reference forms these matrices
+ * only implicitly in its gain loop (collision_integral.cu:75-188). */
+typedef struct gd_cmatrix gd_cmatrix;
+enum { GD_CMATRIX_BF16 = 0, GD_CMATRIX_BF16X3 = 1 };
+int gd_cmatrix_create(gd_ctx *ctx, int mode, gd_cmatrix **out);
+int gd_cmatrix_gain(gd_cmatrix *cm, const float *f, int ncells, int ld, float *gain, gd_stream stream);
+int gd_cmatrix_destroy(gd_cmatrix *cm);
+
 /* Layout conversion between the full box [nx*ny*nz][ld_box] of the reference
  * (determ.cu:107-120) and the compact in-sphere layout [n_pnt][ld]; nodes
  * outside the sphere come out as 0.  Needed only when R cuts the box. */
