@@ -50,11 +50,19 @@ def parse():
     p.add_argument("--cpu-seconds", type=float, default=15.0,
                    help="target length of the bounded CPU-baseline sample")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--gain", choices=["pair", "bf16", "bf16x3"], default="pair",
+                   help="gain algorithm of the timed step (FP32 pair-product kernel or tensor-core collision matrices)")
+    p.add_argument("--alternatives", default="bf16",
+                   help="comma list of other gain paths to time after the main run ('' for none)")
     return p.parse_args()
+
+
+GAIN_PATHS = {"pair": 0, "bf16": 1, "bf16x3": 2}
 
 
 def workload(args, ncells):
     return {"workload": f"plain collision step, {args.grid}^3 lattice [-5,5]^3 cut to R={args.radius}",
+            "gain": args.gain,
             "cells": ncells, "dt_mode": f"courant {args.courant} (dt = courant / max nu, as relax_f)",
             "inputs": "seeded Maxwellian mixtures: 1-3 components, n~LogN(0,0.3), u~N(0,0.7^2), T~U[0.6,1.8]",
             "l2": "256 MiB buffer written between timed steps (inside the timed region)"}
@@ -175,6 +183,7 @@ def run_ours(args):
 
     spec = gd.GridSpec(args.grid, R=args.radius)
     ctx = gd.Context(spec, device=local)
+    ctx.set_gain_path(GAIN_PATHS[args.gain])
     n = ctx.n_pnt
     nc = args.cells
     grid = spec.fill()
@@ -273,6 +282,11 @@ def run_ours(args):
                     "ms_per_step": ms_e2e / args.steps},
             "gpu_launches": 7 * args.steps,
             "clocks": clk.summary(), "roofline": roof}
+    alts = {}
+    if rank == 0 and world == 1:
+        alts = alternatives(args, ctx, f0, nc, stream, flush, peak, peak_kind)
+        if alts:
+            line["alternatives"] = alts
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(args, args.cpu_seconds)
     if rank == 0:
@@ -280,6 +294,71 @@ def run_ours(args):
     ctx.close()
     if dist is not None:
         dist.destroy_process_group()
+
+
+def one_step_q(gd, ctx, f0, nc):
+    import torch
+    f = f0.clone()
+    q = torch.zeros(f.shape, dtype=torch.float64, device=f.device)
+    ctx.step(f, nc, nc, gd.DT_COURANT, 0.5, q=q)
+    torch.cuda.synchronize()
+    return q
+
+
+def alternatives(args, ctx, f0, nc, stream, flush, peak, peak_kind):
+    """Step throughput of the other gain paths on the same workload, with the
+    relative L2 difference of their Q from the main path's Q on the input."""
+    import torch
+    import gpu_determ_gb300 as gd
+    names = [a for a in args.alternatives.split(",") if a and a != args.gain]
+    if not names:
+        return {}
+    out = {}
+    q_main = one_step_q(gd, ctx, f0, nc)
+    for name in names:
+        try:
+            ctx.set_gain_path(GAIN_PATHS[name])
+        except gd.GDError as e:
+            out[name] = {"unavailable": str(e)}
+            continue
+        f = f0.clone()
+        for _ in range(args.warmup):
+            ctx.step(f, nc, nc, gd.DT_COURANT, args.courant, stream=stream)
+        f.copy_(f0)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            flush.fill_(1)
+            ctx.step(f, nc, nc, gd.DT_COURANT, args.courant, stream=stream)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        q = one_step_q(gd, ctx, f0, nc)
+        rel = float(torch.linalg.norm(q - q_main) / torch.linalg.norm(q_main))
+        gain = torch.empty_like(f0)
+        g_ms = []
+        for _ in range(max(2, args.steps)):
+            a0 = torch.cuda.Event(enable_timing=True)
+            a1 = torch.cuda.Event(enable_timing=True)
+            a0.record(stream)
+            ctx.collision(f0, nc, nc, None, gain, stream=stream)
+            a1.record(stream)
+            a1.synchronize()
+            g_ms.append(a0.elapsed_time(a1))
+        g_avg = statistics.mean(g_ms[1:]) / 1000.0
+        ns, ns_k = ctx.n_pnt, (ctx.n_pnt + 63) // 64 * 64
+        dense = 2.0 * ns * ((nc + 127) // 128 * 128) * ((ns + 255) // 256 * 256) * ns_k * (3 if name == "bf16x3" else 1)
+        ach = dense / g_avg / 1e12
+        out[name] = {"value": nc * args.steps / (ms / 1000.0), "unit": UNIT, "ms_per_step": ms / args.steps,
+                     "q_rel_l2_vs_main": rel,
+                     "roofline": {"bound": "tensor", "kernel": "cmatrix_gain_kernel (tcgen05)", "achieved": ach,
+                                  "peak": peak, "unit": "TFLOP/s", "frac": ach / peak,
+                                  "peak_source": f"{peak_kind} bf16 dense (MEASURED_PEAKS.json)",
+                                  "work": "dense tile MACs x 2 (x3 passes for bf16x3)", "launch_ms": g_avg * 1e3}}
+    ctx.set_gain_path(GAIN_PATHS[args.gain])
+    return out
 
 
 def main():

@@ -24,6 +24,9 @@ DT_COURANT = 0
 DT_FIXED = 1
 CMATRIX_BF16 = 0
 CMATRIX_BF16X3 = 1
+GAIN_PAIR = 0
+GAIN_CMATRIX_BF16 = 1
+GAIN_CMATRIX_BF16X3 = 2
 
 _ERRORS = {1: "invalid argument", 2: "CUDA error", 3: "out of memory", 4: "unsupported",
            5: "singular system", 6: "I/O error"}
@@ -87,13 +90,14 @@ def lib():
     L.gd_cmatrix_create.argtypes = [vp, i, P(vp)]
     L.gd_cmatrix_gain.argtypes = [vp, vp, i, i, vp, vp]
     L.gd_cmatrix_destroy.argtypes = [vp]
+    L.gd_ctx_set_gain_path.argtypes = [vp, i]
     L.gd_box_to_compact.argtypes = [vp, vp, i, i, vp, i, vp]
     L.gd_compact_to_box.argtypes = [vp, vp, i, i, vp, i, vp]
     for name in ("gd_grid_count", "gd_grid_fill", "gd_ctx_create", "gd_ctx_destroy", "gd_ctx_info",
                  "gd_export_tables", "gd_correction_basis", "gd_collision", "gd_project",
                  "gd_relax", "gd_step", "gd_moments", "gd_gain_noalloc",
                  "gd_box_to_compact", "gd_compact_to_box", "gd_load_options", "gd_cmatrix_create",
-                 "gd_cmatrix_gain", "gd_cmatrix_destroy"):
+                 "gd_cmatrix_gain", "gd_cmatrix_destroy", "gd_ctx_set_gain_path"):
         getattr(L, name).restype = i
     _lib = L
     return L
@@ -185,6 +189,10 @@ class Context:
             self.close()
         except Exception:
             pass
+
+    def set_gain_path(self, path: int):
+        """GAIN_PAIR (FP32 pair-product kernel), GAIN_CMATRIX_BF16 or GAIN_CMATRIX_BF16X3."""
+        _check(lib().gd_ctx_set_gain_path(self._h, int(path)))
 
     # tables -----------------------------------------------------------------
     def export_tables(self, b=None, a=None, stream=None):

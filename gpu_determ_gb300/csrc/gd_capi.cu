@@ -253,6 +253,8 @@ int ensure_scratch(Context &c, size_t bytes)
 
 static void destroy_context(Context &c)
 {
+    gd_cmatrix_destroy(c.cmatrix);
+    c.cmatrix = nullptr;
     cudaFree(c.d_cmap);
     cudaFree(c.d_nodes);
     cudaFree(c.d_b);
@@ -434,6 +436,26 @@ int gd_ctx_destroy(gd_ctx *ctx)
     return GD_OK;
 }
 
+int gd_ctx_set_gain_path(gd_ctx *ctx, int path)
+{
+    if (!ctx) return set_error(GD_ERR_INVALID_ARG, "context is NULL");
+    if (path != GD_GAIN_PAIR && path != GD_GAIN_CMATRIX_BF16 && path != GD_GAIN_CMATRIX_BF16X3)
+        return set_error(GD_ERR_INVALID_ARG, "unknown gain path");
+    gd::Context &c = ctx->c;
+    if (path == c.gain_path) return GD_OK;
+    gd::DeviceGuard g(c.device);
+    gd_cmatrix_destroy(c.cmatrix);
+    c.cmatrix = nullptr;
+    c.gain_path = GD_GAIN_PAIR;
+    if (path != GD_GAIN_PAIR) {
+        const int mode = path == GD_GAIN_CMATRIX_BF16 ? GD_CMATRIX_BF16 : GD_CMATRIX_BF16X3;
+        int rc = gd_cmatrix_create(ctx, mode, &c.cmatrix);
+        if (rc) return rc;
+    }
+    c.gain_path = path;
+    return GD_OK;
+}
+
 int gd_ctx_info(const gd_ctx *ctx, gd_info *out)
 {
     if (!ctx || !out) return set_error(GD_ERR_INVALID_ARG, "NULL argument");
@@ -475,7 +497,7 @@ int gd_collision(gd_ctx *ctx, const float *f, int ncells, int ld, float *nu, flo
     gd::DeviceGuard g(ctx->c.device);
     cudaStream_t st = (cudaStream_t)stream;
     if (nu && (rc = gd::run_loss(ctx->c, f, ncells, ld, nu, st))) return rc;
-    if (gain && (rc = gd::run_gain(ctx->c, f, ncells, ld, gain, st))) return rc;
+    if (gain && (rc = gd::run_gain_path(ctx->c, f, ncells, ld, gain, st))) return rc;
     return GD_OK;
 }
 
@@ -532,7 +554,7 @@ int gd_step(gd_ctx *ctx, float *f, int ncells, int ld, int mode, float param, fl
         return set_error(GD_ERR_OUT_OF_MEMORY, "step buffers");
     }
     rc = gd::run_loss(c, f, ncells, ld, nu_b, st);
-    if (!rc) rc = gd::run_gain(c, f, ncells, ld, gain_b, st);
+    if (!rc) rc = gd::run_gain_path(c, f, ncells, ld, gain_b, st);
     if (!rc) rc = gd::run_project(c, f, nu_b, gain_b, ncells, ld, nu_b, q_b, nullptr, 0, 0.f, nullptr, m5, st);
     if (!rc) rc = gd::run_relax_q(c, f, nu_b, gain_b, q_b, ncells, ld, mode, param, time_dev, dt_dev, st);
     for (void *p : tmp) cudaFreeAsync(p, st);

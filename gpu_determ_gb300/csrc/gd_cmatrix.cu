@@ -558,3 +558,11 @@ extern "C" int gd_cmatrix_gain(gd_cmatrix *h, const float *f, int ncells, int ld
     if (flag) return set_error(GD_ERR_CUDA, "collision-matrix kernel: a pipeline wait timed out");
     return GD_OK;
 }
+
+namespace gd {
+int run_gain_path(Context &c, const float *f, int ncells, int ld, float *gain, cudaStream_t st)
+{
+    if (c.gain_path == GD_GAIN_PAIR || !c.cmatrix) return run_gain(c, f, ncells, ld, gain, st);
+    return gd_cmatrix_gain(c.cmatrix, f, ncells, ld, gain, st);
+}
+}  // namespace gd

@@ -89,6 +89,8 @@ struct Context {
     std::vector<int64_t> s_work_prefix;  // [ns + 1] cumulative work in linear s order
     // counts reported by gd_ctx_info
     int64_t pair_products = 0, contraction_terms = 0, scatter_terms = 0;
+    int gain_path = GD_GAIN_PAIR;    // gain algorithm for gd_collision / gd_step
+    gd_cmatrix *cmatrix = nullptr;   // collision matrices when gain_path is a GD_GAIN_CMATRIX_*
     int gain_cb = 32;                // cells per lane row of the gain kernel (fixed per grid)
     size_t gain_smem = 0;            // its dynamic shared memory
     // scratch owned by the context (grown on demand)
@@ -122,6 +124,8 @@ int build_weight_rows(Context &c, const float *a_dense, cudaStream_t st);
 // kernels -------------------------------------------------------------------
 int run_loss(Context &c, const float *f, int ncells, int ld, float *nu, cudaStream_t st);
 int run_gain(Context &c, const float *f, int ncells, int ld, float *gain, cudaStream_t st);
+// gain by the context's selected path
+int run_gain_path(Context &c, const float *f, int ncells, int ld, float *gain, cudaStream_t st);
 int run_project(Context &c, const float *f, const float *nu, const float *gain, int ncells,
                 int ld, float *nu_corr, double *q, double *x, int fixed_dt_mode, float dt,
                 float *f_out, double *m5, cudaStream_t st);

@@ -162,6 +162,11 @@ enum { GD_CMATRIX_BF16 = 0, GD_CMATRIX_BF16X3 = 1 };
 int gd_cmatrix_create(gd_ctx *ctx, int mode, gd_cmatrix **out);
 int gd_cmatrix_gain(gd_cmatrix *cm, const float *f, int ncells, int ld, float *gain, gd_stream stream);
 int gd_cmatrix_destroy(gd_cmatrix *cm);
+/* Gain algorithm used by gd_collision and gd_step for this context:
+ * GD_GAIN_PAIR (default, FP32 pair-product kernel), GD_GAIN_CMATRIX_BF16 or
+ * GD_GAIN_CMATRIX_BF16X3 (builds the context's collision matrices). */
+enum { GD_GAIN_PAIR = 0, GD_GAIN_CMATRIX_BF16 = 1, GD_GAIN_CMATRIX_BF16X3 = 2 };
+int gd_ctx_set_gain_path(gd_ctx *ctx, int path);
 
 /* Layout conversion between the full box [nx*ny*nz][ld_box] of the reference
  * (determ.cu:107-120) and the compact in-sphere layout [n_pnt][ld]; nodes

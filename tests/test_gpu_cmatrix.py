@@ -34,3 +34,31 @@ def test_cmatrix_gain_matches_oracle(cuda, gdlib, n, R, ncells, ld):
         rel = np.linalg.norm(got[:, :ncells] - ref) / np.linalg.norm(ref)
         assert rel <= tol, (mode, rel)
         cm.close()
+
+
+@pytest.mark.parametrize("path,tol", [(2, 1e-4), (1, 2e-2)])
+def test_step_with_cmatrix_gain_path(cuda, gdlib, path, tol):
+    """gd_step with the tensor-core gain: the FP64 projection still conserves
+    mass, momentum and energy to 1e-12, and Q stays within tol (relative L2)
+    of the FP64 oracle's projected Q (BF16 x3: 1e-4, BF16: 2e-2)."""
+    torch = cuda
+    n, R, nc = 12, 4.8, 64
+    spec = gdlib.GridSpec(n, R=R)
+    ctx = gdlib.Context(spec)
+    ctx.set_gain_path(path)
+    f = inputs.mixtures(spec.fill(), nc, seed=31)
+    ft = torch.from_numpy(f).cuda()
+    q = torch.zeros(ft.shape, dtype=torch.float64, device="cuda")
+    gain = torch.zeros_like(ft)
+    ctx.step(ft, nc, nc, gdlib.DT_COURANT, 0.5, gain=gain, q=q)
+    torch.cuda.synchronize()
+    o = Oracle(n, R=R)
+    qh = q.cpu().numpy()
+    mom = o.phi().T @ qh
+    scale = np.abs(o.phi()).T @ np.abs(gain.cpu().numpy().astype(np.float64))
+    assert np.all(np.abs(mom) <= 1e-12 * scale)
+    fb = o.to_box(f)
+    _, q64, _, _ = o.project(f, o.loss_f64(fb).astype(np.float32), o.gain_f64(fb).astype(np.float32))
+    rel = np.linalg.norm(qh - q64) / np.linalg.norm(q64)
+    print(f"gain path {path}: Q relative L2 vs FP64 oracle = {rel:.3e}")
+    assert rel <= tol
