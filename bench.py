@@ -30,7 +30,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 
-METRIC = "cells*steps/s at 20^3 grid (plain deterministic collision step)"
+METRIC = "cells*steps/s at 20^3 grid (deterministic collision step, Q rel-L2 <= 1e-3)"
 UNIT = "cell-steps/s"
 PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
 FALLBACK_BF16_TFLOPS = 1900.0
@@ -50,9 +50,9 @@ def parse():
     p.add_argument("--cpu-seconds", type=float, default=15.0,
                    help="target length of the bounded CPU-baseline sample")
     p.add_argument("--no-cpu-baseline", action="store_true")
-    p.add_argument("--gain", choices=["pair", "bf16", "bf16x3"], default="pair",
+    p.add_argument("--gain", choices=["pair", "bf16", "bf16x3"], default="bf16",
                    help="gain algorithm of the timed step (FP32 pair-product kernel or tensor-core collision matrices)")
-    p.add_argument("--alternatives", default="bf16",
+    p.add_argument("--alternatives", default="pair,bf16x3",
                    help="comma list of other gain paths to time after the main run ('' for none)")
     return p.parse_args()
 
@@ -162,7 +162,8 @@ def run_reference(args):
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 / v,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic", "config": workload(args, 1), "cpu_baseline": info,
+            "data": "synthetic", "config": dict(workload(args, 1), gain="oracle FP32 OpenMP host path"),
+            "cpu_baseline": info,
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -247,9 +248,41 @@ def run_ours(args):
     e2e = world * nc * args.steps / (ms_e2e / 1000.0)
     nbytes = n * nc * 4
 
-    # dominant kernel: the gain (pair-product kernel + chunk reduction)
+    # dominant kernel: the gain
+    peak, peak_kind = peaks()
+    roof = gain_roofline(args.gain, ctx, f0, nc, stream, flush, peak, peak_kind, max(2, args.steps))
+
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None,
+            "dtype": {"pair": "f32", "bf16": "bf16 (FP32 accumulate)", "bf16x3": "bf16x3 (FP32 accumulate)"}[args.gain]
+            + ", FP64 projection",
+            "data": "synthetic", "config": workload(args, nc),
+            "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
+                    "ms_per_step": ms_e2e / args.steps},
+            "gpu_launches": (7 if args.gain == "pair" else 6) * args.steps,
+            "clocks": clk.summary(), "roofline": roof}
+    alts = {}
+    if rank == 0 and world == 1:
+        alts = alternatives(args, ctx, f0, nc, stream, flush, peak, peak_kind)
+        if alts:
+            line["alternatives"] = alts
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(args, args.cpu_seconds)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def gain_roofline(name, ctx, f0, nc, stream, flush, peak, peak_kind, reps):
+    """Average duration of the gain call (CUDA events on the launching stream,
+    L2 flushed before each) and its throughput against the BF16 tensor peak:
+    algorithmic FLOP of the pair-product formulation for the FP32 kernel,
+    dense tile FLOP for the tensor-core collision-matrix kernel."""
+    import torch
     gain = torch.empty_like(f0)
-    reps = max(2, args.steps)
     for _ in range(2):
         ctx.collision(f0, nc, nc, None, gain, stream=stream)
     torch.cuda.synchronize()
@@ -264,36 +297,19 @@ def run_ours(args):
         a1.synchronize()
         g_ms.append(a0.elapsed_time(a1))
     g_avg = statistics.mean(g_ms) / 1000.0
-    inf = ctx.info
-    flop_cell = 7 * inf["pair_products"] + 2 * inf["contraction_terms"] + inf["scatter_terms"]
-    achieved = flop_cell * nc / g_avg / 1e12
-    peak, peak_kind = peaks()
-    roof = {"bound": "tensor", "kernel": "gain_pair_kernel (+ chunk reduction)",
-            "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
-            "peak_source": f"{peak_kind} bf16 dense (MEASURED_PEAKS.json)",
-            "work": "7 FLOP per pair product + 2 per nonzero-weight term + 1 per scatter update",
-            "flop_per_cell": flop_cell, "traffic": None, "launch_ms": g_avg * 1000.0}
-
-    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32 (FP64 projection)",
-            "data": "synthetic", "config": workload(args, nc),
-            "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
-                    "ms_per_step": ms_e2e / args.steps},
-            "gpu_launches": 7 * args.steps,
-            "clocks": clk.summary(), "roofline": roof}
-    alts = {}
-    if rank == 0 and world == 1:
-        alts = alternatives(args, ctx, f0, nc, stream, flush, peak, peak_kind)
-        if alts:
-            line["alternatives"] = alts
-    if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(args, args.cpu_seconds)
-    if rank == 0:
-        print(json.dumps(line), flush=True)
-    ctx.close()
-    if dist is not None:
-        dist.destroy_process_group()
+    if name == "pair":
+        inf = ctx.info
+        flop = nc * (7 * inf["pair_products"] + 2 * inf["contraction_terms"] + inf["scatter_terms"])
+        kernel, work = "gain_pair_kernel (+ chunk reduction)", \
+            "7 FLOP per pair product + 2 per nonzero-weight term + 1 per scatter update"
+    else:
+        ns, ns_k = ctx.n_pnt, (ctx.n_pnt + 63) // 64 * 64
+        flop = 2.0 * ns * ((nc + 127) // 128 * 128) * ((ns + 255) // 256 * 256) * ns_k * (3 if name == "bf16x3" else 1)
+        kernel, work = "cmatrix_gain_kernel (tcgen05)", "dense tile MACs x 2 (x3 passes for bf16x3)"
+    ach = flop / g_avg / 1e12
+    return {"bound": "tensor", "kernel": kernel, "achieved": ach, "peak": peak, "unit": "TFLOP/s",
+            "frac": ach / peak, "peak_source": f"{peak_kind} bf16 dense (MEASURED_PEAKS.json)", "work": work,
+            "flop_per_launch": flop, "traffic": None, "launch_ms": g_avg * 1000.0}
 
 
 def one_step_q(gd, ctx, f0, nc):
@@ -337,26 +353,10 @@ def alternatives(args, ctx, f0, nc, stream, flush, peak, peak_kind):
         ms = e0.elapsed_time(e1)
         q = one_step_q(gd, ctx, f0, nc)
         rel = float(torch.linalg.norm(q - q_main) / torch.linalg.norm(q_main))
-        gain = torch.empty_like(f0)
-        g_ms = []
-        for _ in range(max(2, args.steps)):
-            a0 = torch.cuda.Event(enable_timing=True)
-            a1 = torch.cuda.Event(enable_timing=True)
-            a0.record(stream)
-            ctx.collision(f0, nc, nc, None, gain, stream=stream)
-            a1.record(stream)
-            a1.synchronize()
-            g_ms.append(a0.elapsed_time(a1))
-        g_avg = statistics.mean(g_ms[1:]) / 1000.0
-        ns, ns_k = ctx.n_pnt, (ctx.n_pnt + 63) // 64 * 64
-        dense = 2.0 * ns * ((nc + 127) // 128 * 128) * ((ns + 255) // 256 * 256) * ns_k * (3 if name == "bf16x3" else 1)
-        ach = dense / g_avg / 1e12
         out[name] = {"value": nc * args.steps / (ms / 1000.0), "unit": UNIT, "ms_per_step": ms / args.steps,
                      "q_rel_l2_vs_main": rel,
-                     "roofline": {"bound": "tensor", "kernel": "cmatrix_gain_kernel (tcgen05)", "achieved": ach,
-                                  "peak": peak, "unit": "TFLOP/s", "frac": ach / peak,
-                                  "peak_source": f"{peak_kind} bf16 dense (MEASURED_PEAKS.json)",
-                                  "work": "dense tile MACs x 2 (x3 passes for bf16x3)", "launch_ms": g_avg * 1e3}}
+                     "roofline": gain_roofline(name, ctx, f0, nc, stream, flush, peak, peak_kind,
+                                               max(2, args.steps))}
     ctx.set_gain_path(GAIN_PATHS[args.gain])
     return out
 

@@ -271,6 +271,7 @@ static void destroy_context(Context &c)
     cudaFree(c.d_s_bounds);
     cudaFree(c.d_reduce);
     cudaFree(c.scratch.ptr);
+    cudaFree(c.step_buf.ptr);
 }
 
 static int create_context(Context &c, const gd_grid_spec &spec, int device)
@@ -535,29 +536,30 @@ int gd_step(gd_ctx *ctx, float *f, int ncells, int ld, int mode, float param, fl
     gd::DeviceGuard g(ctx->c.device);
     gd::Context &c = ctx->c;
     cudaStream_t st = (cudaStream_t)stream;
-    // step buffers: nu, gain (FP32) and Q (FP64) unless the caller provides them
+    // step buffers: nu, gain (FP32) and Q (FP64) unless the caller provides
+    // them; context-owned and grown on demand (no allocation per step)
     const size_t n = (size_t)c.d.n_pnt * ld;
     float *nu_b = nu, *gain_b = gain;
     double *q_b = q;
-    std::vector<void *> tmp;
-    auto alloc = [&](size_t bytes) -> void * {
-        void *p = nullptr;
-        if (cudaMallocAsync(&p, bytes, st) != cudaSuccess) return nullptr;
-        tmp.push_back(p);
-        return p;
-    };
-    if (!nu_b) nu_b = static_cast<float *>(alloc(n * sizeof(float)));
-    if (!gain_b) gain_b = static_cast<float *>(alloc(n * sizeof(float)));
-    if (!q_b) q_b = static_cast<double *>(alloc(n * sizeof(double)));
     if (!nu_b || !gain_b || !q_b) {
-        for (void *p : tmp) cudaFreeAsync(p, st);
-        return set_error(GD_ERR_OUT_OF_MEMORY, "step buffers");
+        const size_t need = n * (2 * sizeof(float) + sizeof(double));
+        if (c.step_buf.bytes < need) {
+            GD_CUDA(cudaStreamSynchronize(st));
+            cudaFree(c.step_buf.ptr);
+            c.step_buf.ptr = nullptr;
+            c.step_buf.bytes = 0;
+            GD_CUDA(cudaMalloc(&c.step_buf.ptr, need));
+            c.step_buf.bytes = need;
+        }
+        unsigned char *p = static_cast<unsigned char *>(c.step_buf.ptr);
+        if (!q_b) q_b = reinterpret_cast<double *>(p);
+        if (!nu_b) nu_b = reinterpret_cast<float *>(p + n * sizeof(double));
+        if (!gain_b) gain_b = reinterpret_cast<float *>(p + n * (sizeof(double) + sizeof(float)));
     }
     rc = gd::run_loss(c, f, ncells, ld, nu_b, st);
     if (!rc) rc = gd::run_gain_path(c, f, ncells, ld, gain_b, st);
     if (!rc) rc = gd::run_project(c, f, nu_b, gain_b, ncells, ld, nu_b, q_b, nullptr, 0, 0.f, nullptr, m5, st);
     if (!rc) rc = gd::run_relax_q(c, f, nu_b, gain_b, q_b, ncells, ld, mode, param, time_dev, dt_dev, st);
-    for (void *p : tmp) cudaFreeAsync(p, st);
     return rc;
 }
 

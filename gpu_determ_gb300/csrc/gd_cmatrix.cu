@@ -29,6 +29,7 @@
 #include <vector>
 
 #include "gd_internal.h"
+#include "gd_tc.cuh"
 
 struct gd_ctx {
     gd::Context c;
@@ -43,7 +44,8 @@ constexpr int BK = 64;   // a per stage (128 bytes of BF16: one swizzle row)
 constexpr int kThreads = 192;
 constexpr uint32_t kTileA = BM * BK * 2;  // 16 KB
 constexpr uint32_t kTileB = BN * BK * 2;  // 32 KB
-constexpr uint32_t kWaitLimit = 1u << 20;  // bounded mbarrier polls per wait
+constexpr uint32_t kIdesc = tc::umma_idesc_bf16(BM, BN);
+using namespace tc;
 
 struct CmParams {
     int ns;       // in-sphere nodes
@@ -53,118 +55,6 @@ struct CmParams {
     float *gain;     // [ns][ld]
     int *err;        // set to 1 when a wait times out
 };
-
-__device__ __forceinline__ uint32_t smem_u32(const void *p)
-{
-    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-}
-
-__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count)
-{
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
-}
-
-__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes)
-{
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
-}
-
-__device__ __forceinline__ void mbar_arrive(uint32_t bar)
-{
-    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
-}
-
-__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity)
-{
-    uint32_t ok;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(ok)
-        : "r"(bar), "r"(parity)
-        : "memory");
-    return ok != 0;
-}
-
-// Bounded wait for the phase with the given parity; false (and *err = 1)
-// when it did not complete.  Also gives up as soon as another CTA has
-// recorded a time-out, so a failing launch ends quickly.
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int *err)
-{
-    for (uint32_t it = 0; it < kWaitLimit; it++) {
-        if (mbar_try_wait(bar, parity)) return true;
-        if ((it & 255u) == 255u && *(volatile int *)err) return false;
-    }
-    atomicExch(err, 1);
-    return false;
-}
-
-__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap *map, int c0, int c1, uint32_t bar)
-{
-    asm volatile(
-        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];"
-        ::"r"(dst), "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(bar)
-        : "memory");
-}
-
-__device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap *map, int c0, int c1, int c2,
-                                            uint32_t bar)
-{
-    asm volatile(
-        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];"
-        ::"r"(dst), "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(bar)
-        : "memory");
-}
-
-// Shared-memory matrix descriptor: K-major operand in the 128-byte swizzle
-// layout TMA writes (rows of 128 bytes, 8-row groups 1024 bytes apart).
-__device__ __forceinline__ uint64_t umma_desc(uint32_t addr)
-{
-    uint64_t d = (uint64_t)((addr & 0x3FFFFu) >> 4);  // start address
-    d |= (uint64_t)1 << 16;                           // leading byte offset (unused for this layout)
-    d |= (uint64_t)(1024u >> 4) << 32;                // stride byte offset: 8 rows x 128 B
-    d |= (uint64_t)1 << 46;                           // descriptor version
-    d |= (uint64_t)2 << 61;                           // 128-byte swizzle
-    return d;
-}
-
-// Instruction descriptor, kind::f16: A, B BF16 (K-major), D FP32, M = BM, N = BN.
-constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) |
-                            ((uint32_t)(BM >> 4) << 24);
-
-__device__ __forceinline__ void umma_bf16(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t accum)
-{
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "setp.ne.b32 p, %4, 0;\n\t"
-        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}"
-        ::"r"(d_tmem), "l"(adesc), "l"(bdesc), "r"(kIdesc), "r"(accum)
-        : "memory");
-}
-
-__device__ __forceinline__ void umma_commit(uint32_t bar)
-{
-    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
-                 : "memory");
-}
-
-__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float *v)
-{
-    uint32_t r[32];
-    asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
-        "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, "
-        "%16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
-        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
-          "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
-          "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
-        : "r"(taddr));
-    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-    for (int j = 0; j < 32; j++) v[j] = __uint_as_float(r[j]);
-}
 
 // NPASS = 1: D = F_hi G_hi.  NPASS = 3: D = F_hi G_hi + F_hi G_lo + F_lo G_hi.
 template <int NPASS>
@@ -268,10 +158,10 @@ __global__ void __launch_bounds__(kThreads, 1)
                     for (int kk = 0; kk < BK / 16; kk++) {
                         const uint32_t off = (uint32_t)kk * 32u;  // 16 BF16 along K
                         const uint32_t acc = (k > 0 || kk > 0) ? 1u : 0u;
-                        umma_bf16(d_tmem, umma_desc(aH + off), umma_desc(bH + off), acc);
+                        umma_bf16(d_tmem, umma_desc(aH + off), umma_desc(bH + off), kIdesc, acc);
                         if (NPASS == 3) {
-                            umma_bf16(d_tmem, umma_desc(aH + off), umma_desc(bL + off), 1u);
-                            umma_bf16(d_tmem, umma_desc(aL + off), umma_desc(bH + off), 1u);
+                            umma_bf16(d_tmem, umma_desc(aH + off), umma_desc(bL + off), kIdesc, 1u);
+                            umma_bf16(d_tmem, umma_desc(aL + off), umma_desc(bH + off), kIdesc, 1u);
                         }
                     }
                     umma_commit(smem_u32(&empty_bar[s]));

@@ -95,6 +95,7 @@ struct Context {
     size_t gain_smem = 0;            // its dynamic shared memory
     // scratch owned by the context (grown on demand)
     Scratch scratch;
+    Scratch step_buf;  // gd_step's nu, gain (FP32) and Q (FP64) when the caller passes none
     int *d_s_bounds = nullptr;  // chunk boundaries for the current launch shape
     int s_bounds_cap = 0;
     float *d_reduce = nullptr;  // small device scalars (max nu, dt)
