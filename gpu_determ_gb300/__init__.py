@@ -13,8 +13,9 @@ from __future__ import annotations
 import ctypes as C
 import os
 
-__all__ = ["GDError", "GridSpec", "Context", "CollisionMatrix", "lib", "library_path", "load_options",
-           "DT_COURANT", "DT_FIXED", "CMATRIX_BF16", "CMATRIX_BF16X3"]
+__all__ = ["GDError", "GridSpec", "Context", "CollisionMatrix", "Mlp", "Surrogate", "Batch", "cell_rel_l2", "lib", "library_path", "load_options",
+           "DT_COURANT", "DT_FIXED", "CMATRIX_BF16", "CMATRIX_BF16X3",
+           "MLP_SCALE_INPUT", "MLP_SCALE_OUTPUT", "MLP_LOSS_MSE", "MLP_LOSS_BATCH"]
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 _LIB_PATH = os.path.join(_HERE, "libgpu_determ.so")
@@ -27,6 +28,10 @@ CMATRIX_BF16X3 = 1
 GAIN_PAIR = 0
 GAIN_CMATRIX_BF16 = 1
 GAIN_CMATRIX_BF16X3 = 2
+MLP_SCALE_INPUT = 1
+MLP_SCALE_OUTPUT = 2
+MLP_LOSS_MSE = 4
+MLP_LOSS_BATCH = 8
 
 _ERRORS = {1: "invalid argument", 2: "CUDA error", 3: "out of memory", 4: "unsupported",
            5: "singular system", 6: "I/O error"}
@@ -54,6 +59,17 @@ class _Info(C.Structure):
                 ("nonzero_weights", C.c_int64), ("table_a_elems", C.c_int64),
                 ("pair_products", C.c_int64), ("contraction_terms", C.c_int64),
                 ("scatter_terms", C.c_int64)]
+
+
+class _MlpInfo(C.Structure):
+    _fields_ = [("n_in", C.c_int), ("n_out", C.c_int), ("n_in_padded", C.c_int), ("n_out_padded", C.c_int),
+                ("batch_cap", C.c_int), ("flags", C.c_int), ("steps", C.c_int64), ("num_params", C.c_int64),
+                ("forward_flop_per_cell", C.c_double), ("in_gain", C.c_float), ("out_gain", C.c_float)]
+
+
+class _Autotune(C.Structure):
+    _fields_ = [("path", C.c_int), ("waves", C.c_int), ("best_ms", C.c_float), ("n_candidates", C.c_int),
+                ("cand_path", C.c_int * 8), ("cand_waves", C.c_int * 8), ("cand_ms", C.c_float * 8)]
 
 
 def library_path() -> str:
@@ -93,11 +109,39 @@ def lib():
     L.gd_ctx_set_gain_path.argtypes = [vp, i]
     L.gd_box_to_compact.argtypes = [vp, vp, i, i, vp, i, vp]
     L.gd_compact_to_box.argtypes = [vp, vp, i, i, vp, i, vp]
+    L.gd_mlp_create.argtypes = [i, i, i, i, C.c_uint64, P(vp)]
+    L.gd_mlp_destroy.argtypes = [vp]
+    L.gd_mlp_set_io_scale.argtypes = [vp, f, f]
+    L.gd_mlp_info.argtypes = [vp, P(_MlpInfo)]
+    L.gd_mlp_forward.argtypes = [vp, vp, i, i, vp, i, vp]
+    L.gd_mlp_train_step.argtypes = [vp, vp, i, vp, i, vp, i, i, f, f, vp, vp]
+    L.gd_mlp_loss.argtypes = [vp, vp, i, vp, i, vp, i, i, vp, vp]
+    L.gd_mlp_check.argtypes = [vp, vp]
+    L.gd_mlp_get_params.argtypes = [vp, vp]
+    L.gd_mlp_set_params.argtypes = [vp, vp]
+    L.gd_mlp_get_grads.argtypes = [vp, vp]
+    L.gd_surrogate_create.argtypes = [vp, vp, vp, i, P(vp)]
+    L.gd_surrogate_destroy.argtypes = [vp]
+    L.gd_surrogate_gain.argtypes = [vp, vp, i, i, f, vp, vp, vp, P(i), vp]
+    L.gd_cell_rel_l2.argtypes = [vp, i, vp, i, i, i, vp, vp]
+    L.gd_cmatrix_check.argtypes = [vp, vp]
+    L.gd_batch_create.argtypes = [P(vp)]
+    L.gd_batch_destroy.argtypes = [vp]
+    L.gd_batch_add.argtypes = [vp, vp, vp, i, i, i, f, vp, vp, vp]
+    L.gd_batch_step.argtypes = [vp, i, vp]
+    L.gd_batch_check.argtypes = [vp]
+    L.gd_batch_info.argtypes = [vp, P(i), P(i), P(i), P(C.c_int64)]
+    L.gd_ctx_autotune.argtypes = [vp, vp, i, i, i, C.c_double, P(_Autotune), vp]
     for name in ("gd_grid_count", "gd_grid_fill", "gd_ctx_create", "gd_ctx_destroy", "gd_ctx_info",
                  "gd_export_tables", "gd_correction_basis", "gd_collision", "gd_project",
                  "gd_relax", "gd_step", "gd_moments", "gd_gain_noalloc",
                  "gd_box_to_compact", "gd_compact_to_box", "gd_load_options", "gd_cmatrix_create",
-                 "gd_cmatrix_gain", "gd_cmatrix_destroy", "gd_ctx_set_gain_path"):
+                 "gd_cmatrix_gain", "gd_cmatrix_destroy", "gd_ctx_set_gain_path",
+                 "gd_mlp_create", "gd_mlp_destroy", "gd_mlp_set_io_scale", "gd_mlp_info", "gd_mlp_forward", "gd_mlp_train_step",
+                 "gd_mlp_loss", "gd_mlp_check", "gd_mlp_get_params", "gd_mlp_set_params", "gd_mlp_get_grads",
+                 "gd_surrogate_create", "gd_surrogate_destroy", "gd_surrogate_gain", "gd_cell_rel_l2",
+                 "gd_cmatrix_check", "gd_batch_create", "gd_batch_destroy", "gd_batch_add", "gd_batch_step",
+                 "gd_batch_check", "gd_batch_info", "gd_ctx_autotune"):
         getattr(L, name).restype = i
     _lib = L
     return L
@@ -220,6 +264,16 @@ class Context:
                              _ptr(nu), _ptr(gain), _ptr(q), _ptr(m5), _ptr(time), _ptr(dt),
                              _stream(stream)))
 
+    def autotune(self, f, ncells, ld, path_mask=1 << GAIN_PAIR, mem_budget=0.0, stream=None) -> dict:
+        """Time the gain candidates on these cells and keep the fastest."""
+        r = _Autotune()
+        _check(lib().gd_ctx_autotune(self._h, _ptr(f), int(ncells), int(ld), int(path_mask), float(mem_budget),
+                                     C.byref(r), _stream(stream)))
+        names = {GAIN_PAIR: "pair", GAIN_CMATRIX_BF16: "cmatrix_bf16", GAIN_CMATRIX_BF16X3: "cmatrix_bf16x3"}
+        cands = [{"path": names[r.cand_path[k]], "waves": r.cand_waves[k], "ms": r.cand_ms[k]}
+                 for k in range(r.n_candidates)]
+        return {"path": names[r.path], "waves": r.waves, "best_ms": r.best_ms, "candidates": cands}
+
     def box_to_compact(self, box, ncells, ld_box, compact, ld, stream=None):
         _check(lib().gd_box_to_compact(self._h, _ptr(box), int(ncells), int(ld_box), _ptr(compact), int(ld),
                                        _stream(stream)))
@@ -248,6 +302,147 @@ class CollisionMatrix:
     def close(self):
         if self._h:
             lib().gd_cmatrix_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Mlp:
+    """Surrogate network n_in -> 256 -> 512 -> 512 -> 256 (+residual) -> n_out
+    on the tensor cores (BF16 weights, FP32 accumulation); arrays are
+    [feature][cell] device tensors with leading dimension ld."""
+
+    def __init__(self, n_in: int, n_out: int, batch_cap: int, flags: int = MLP_SCALE_INPUT | MLP_SCALE_OUTPUT,
+                 seed: int = 0):
+        self._h = C.c_void_p()
+        _check(lib().gd_mlp_create(int(n_in), int(n_out), int(batch_cap), int(flags), int(seed),
+                                   C.byref(self._h)))
+        inf = _MlpInfo()
+        _check(lib().gd_mlp_info(self._h, C.byref(inf)))
+        self.info = {k: getattr(inf, k) for k, _ in _MlpInfo._fields_}
+        self.n_in, self.n_out, self.cap = n_in, n_out, batch_cap
+
+    def set_io_scale(self, in_gain: float, out_gain: float):
+        """Global gains on the scaled input and on the network output."""
+        _check(lib().gd_mlp_set_io_scale(self._h, float(in_gain), float(out_gain)))
+        self.info["in_gain"], self.info["out_gain"] = float(in_gain), float(out_gain)
+
+    def layer_shapes(self):
+        """[(out, in)] of the five layers with the padded feature counts."""
+        i, o = self.info["n_in_padded"], self.info["n_out_padded"]
+        return [(256, i), (512, 256), (512, 512), (256, 512), (o, 256)]
+
+    def forward(self, x, ldx, batch, y, ldy, stream=None):
+        _check(lib().gd_mlp_forward(self._h, _ptr(x), int(ldx), int(batch), _ptr(y), int(ldy), _stream(stream)))
+
+    def train_step(self, x, ldx, t, ldt, batch, lr, weight_decay=0.0, loss=None, tden=None, ldd=0, stream=None):
+        _check(lib().gd_mlp_train_step(self._h, _ptr(x), int(ldx), _ptr(t), int(ldt), _ptr(tden), int(ldd),
+                                       int(batch), float(lr), float(weight_decay), _ptr(loss), _stream(stream)))
+
+    def loss(self, x, ldx, t, ldt, batch, row_loss, tden=None, ldd=0, stream=None):
+        _check(lib().gd_mlp_loss(self._h, _ptr(x), int(ldx), _ptr(t), int(ldt), _ptr(tden), int(ldd),
+                                 int(batch), _ptr(row_loss), _stream(stream)))
+
+    def check(self, stream=None):
+        _check(lib().gd_mlp_check(self._h, _stream(stream)))
+
+    def get_params(self):
+        import numpy as np
+        out = np.zeros(self.info["num_params"], np.float32)
+        _check(lib().gd_mlp_get_params(self._h, out.ctypes.data))
+        return out
+
+    def set_params(self, p):
+        import numpy as np
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        assert p.size == self.info["num_params"]
+        _check(lib().gd_mlp_set_params(self._h, p.ctypes.data))
+
+    def get_grads(self):
+        import numpy as np
+        out = np.zeros(self.info["num_params"], np.float32)
+        _check(lib().gd_mlp_get_grads(self._h, out.ctypes.data))
+        return out
+
+    def close(self):
+        if self._h:
+            lib().gd_mlp_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Surrogate:
+    """Gain from the trained network `net` for cells whose estimated error
+    (network `est`) is within tol, the context's plain gain for the rest."""
+
+    def __init__(self, ctx: Context, net: Mlp, est: Mlp | None, max_cells: int):
+        self.ctx, self.net, self.est = ctx, net, est
+        self._h = C.c_void_p()
+        _check(lib().gd_surrogate_create(ctx._h, net._h, est._h if est is not None else None, int(max_cells),
+                                         C.byref(self._h)))
+
+    def gain(self, f, ncells, ld, tol, nu, gain, est_out=None, stream=None) -> int:
+        """Returns the number of cells that took the plain method."""
+        n = C.c_int(0)
+        _check(lib().gd_surrogate_gain(self._h, _ptr(f), int(ncells), int(ld), float(tol), _ptr(nu), _ptr(gain),
+                                       _ptr(est_out), C.byref(n), _stream(stream)))
+        return n.value
+
+    def close(self):
+        if self._h:
+            lib().gd_surrogate_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def cell_rel_l2(a, lda, b, ldb, n, ncells, out, stream=None):
+    """out[c] = ||a[:,c] - b[:,c]|| / ||b[:,c]|| (FP64 device arrays)."""
+    _check(lib().gd_cell_rel_l2(_ptr(a), int(lda), _ptr(b), int(ldb), int(n), int(ncells), _ptr(out),
+                                _stream(stream)))
+
+
+class Batch:
+    """Groups (context, cells) stepped together; with use_graph every step
+    after the second is one CUDA graph launch."""
+
+    def __init__(self):
+        self._h = C.c_void_p()
+        _check(lib().gd_batch_create(C.byref(self._h)))
+        self._keep = []
+
+    def add(self, ctx: Context, f, ncells, ld, mode, param, m5=None, time=None, dt=None):
+        _check(lib().gd_batch_add(self._h, ctx._h, _ptr(f), int(ncells), int(ld), int(mode), float(param),
+                                  _ptr(m5), _ptr(time), _ptr(dt)))
+        self._keep.append((ctx, f, m5, time, dt))
+
+    def step(self, use_graph=True, stream=None):
+        _check(lib().gd_batch_step(self._h, int(bool(use_graph)), _stream(stream)))
+
+    def check(self):
+        _check(lib().gd_batch_check(self._h))
+
+    def info(self) -> dict:
+        g, s, n, k = C.c_int(0), C.c_int(0), C.c_int(0), C.c_int64(0)
+        _check(lib().gd_batch_info(self._h, C.byref(g), C.byref(s), C.byref(n), C.byref(k)))
+        return {"groups": g.value, "streams": s.value, "graph_nodes": n.value, "steps": k.value}
+
+    def close(self):
+        if self._h:
+            lib().gd_batch_destroy(self._h)
             self._h = C.c_void_p()
 
     def __del__(self):

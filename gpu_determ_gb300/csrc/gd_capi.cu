@@ -12,10 +12,6 @@
 
 #include "gd_internal.h"
 
-struct gd_ctx {
-    gd::Context c;
-};
-
 namespace gd {
 
 namespace {
@@ -268,7 +264,8 @@ static void destroy_context(Context &c)
     cudaFree(c.d_D_item_off);
     cudaFree(c.d_D_items);
     cudaFree(c.d_D_members);
-    cudaFree(c.d_s_bounds);
+    for (auto &kv : c.s_bounds_dev) cudaFree(kv.second);
+    c.s_bounds_dev.clear();
     cudaFree(c.d_reduce);
     cudaFree(c.scratch.ptr);
     cudaFree(c.step_buf.ptr);

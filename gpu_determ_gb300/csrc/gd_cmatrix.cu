@@ -31,9 +31,6 @@
 #include "gd_internal.h"
 #include "gd_tc.cuh"
 
-struct gd_ctx {
-    gd::Context c;
-};
 
 namespace gd {
 namespace {
@@ -441,7 +438,19 @@ extern "C" int gd_cmatrix_gain(gd_cmatrix *h, const float *f, int ncells, int ld
         cmatrix_gain_kernel<1><<<grid, kThreads, smem, st>>>(tFh, tFl, tGh, tGl, prm);
     }
     GD_CUDA(cudaGetLastError());
-    // the kernel records a time-out instead of hanging; report it
+    // the kernel records a time-out instead of hanging; report it (inside a
+    // stream capture the flag stays set for gd_cmatrix_check after replay)
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    GD_CUDA(cudaStreamIsCapturing(st, &cap));
+    if (cap != cudaStreamCaptureStatusNone) return GD_OK;
+    return gd_cmatrix_check(h, stream);
+}
+
+extern "C" int gd_cmatrix_check(gd_cmatrix *h, gd_stream stream)
+{
+    using namespace gd;
+    if (!h) return set_error(GD_ERR_INVALID_ARG, "NULL argument");
+    cudaStream_t st = (cudaStream_t)stream;
     int flag = 0;
     GD_CUDA(cudaMemcpyAsync(&flag, h->err, sizeof(int), cudaMemcpyDeviceToHost, st));
     GD_CUDA(cudaStreamSynchronize(st));

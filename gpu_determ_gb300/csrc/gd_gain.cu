@@ -232,13 +232,14 @@ size_t gain_smem_bytes(const Dims &d, int cb)
     return (size_t)d.nclass * cb * sizeof(float) + (size_t)((d.nxyz * 2 + 15) & ~15);
 }
 
-// Number of s-chunks for nblk cell blocks: at least 2 CTAs per SM, then the
+// Number of s-chunks for nblk cell blocks: at least gain_waves CTAs per SM
+// (2 unless the autotuner chose otherwise), then the
 // count (up to 64 chunks, or 512 when a few blocks must fill the GPU) whose
 // CTA total fills the last wave best; ties go to fewer chunks.
 int gain_chunk_count(const Context &c, int nblk)
 {
     const int sms = std::max(1, c.sm_count);
-    const int lo = std::max(1, (2 * sms + nblk - 1) / nblk);
+    const int lo = std::max(1, (std::max(1, c.gain_waves) * sms + nblk - 1) / nblk);
     const int hi = std::max(lo, std::min(lo + 64, 512));
     int best = lo;
     double best_fill = -1.0;
@@ -271,6 +272,28 @@ int gain_plan_cells(Context &c)
     return GD_OK;
 }
 
+// Device copy of the chunk boundaries for nchunks chunks, built and uploaded
+// on first use (a synchronous copy: the first call of a new launch shape must
+// not be inside a stream capture).
+int gain_bounds_device(Context &c, int nchunks, const int **out)
+{
+    auto it = c.s_bounds_dev.find(nchunks);
+    if (it == c.s_bounds_dev.end()) {
+        std::vector<int> bounds(nchunks + 1);
+        gain_chunk_bounds(c, nchunks, bounds.data());
+        int *d = nullptr;
+        GD_CUDA(cudaMalloc(&d, sizeof(int) * (nchunks + 1)));
+        cudaError_t e = cudaMemcpy(d, bounds.data(), sizeof(int) * (nchunks + 1), cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) {
+            cudaFree(d);
+            return cuda_error(e, "gain chunk bounds");
+        }
+        it = c.s_bounds_dev.emplace(nchunks, d).first;
+    }
+    *out = it->second;
+    return GD_OK;
+}
+
 int run_gain(Context &c, const float *f, int ncells, int ld, float *gain, cudaStream_t st)
 {
     const Dims &d = c.d;
@@ -282,33 +305,18 @@ int run_gain(Context &c, const float *f, int ncells, int ld, float *gain, cudaSt
     // per SM fits), bounded by the partial buffer
     int nchunks = gain_chunk_count(c, nblk);
     while (nchunks > 1 && (size_t)nchunks * d.n_pnt * cells_pad * sizeof(float) > ((size_t)16 << 30)) nchunks--;
-    // work-balanced chunk boundaries over the linear s order
-    std::vector<int> bounds(nchunks + 1);
-    const int64_t total = c.s_work_prefix[d.ns];
-    bounds[0] = 0;
-    for (int k = 1; k < nchunks; k++) {
-        const int64_t target = total * k / nchunks;
-        bounds[k] = (int)(std::lower_bound(c.s_work_prefix.begin(), c.s_work_prefix.end(), target) -
-                          c.s_work_prefix.begin());
-        bounds[k] = std::max(bounds[k], bounds[k - 1]);
-    }
-    bounds[nchunks] = (int)d.ns;
-    if (c.s_bounds_cap < nchunks + 1) {
-        if (c.d_s_bounds) cudaFree(c.d_s_bounds);
-        c.d_s_bounds = nullptr;
-        GD_CUDA(cudaMalloc(&c.d_s_bounds, sizeof(int) * (nchunks + 1)));
-        c.s_bounds_cap = nchunks + 1;
-    }
-    GD_CUDA(cudaMemcpyAsync(c.d_s_bounds, bounds.data(), sizeof(int) * (nchunks + 1),
-                            cudaMemcpyHostToDevice, st));
+    // work-balanced chunk boundaries over the linear s order, cached per count
+    const int *d_bounds = nullptr;
+    int rc = gain_bounds_device(c, nchunks, &d_bounds);
+    if (rc) return rc;
     const size_t part_bytes = (size_t)nchunks * d.n_pnt * cells_pad * sizeof(float);
-    int rc = ensure_scratch(c, part_bytes);
+    rc = ensure_scratch(c, part_bytes);
     if (rc) return rc;
     float *part = static_cast<float *>(c.scratch.ptr);
     GD_CUDA(cudaMemsetAsync(part, 0, part_bytes, st));
 
     GainArgs a{d, f, ld, ncells, cells_pad, c.d_cmap, c.d_grp_row_off, c.d_grp_rows, c.d_D_item_off,
-               c.d_D_items, c.d_D_members, c.d_s_bounds, part};
+               c.d_D_items, c.d_D_members, d_bounds, part};
     dim3 grid(nblk, nchunks);
     switch (cb) {
 #define GD_GAIN_CASE(CBV)                                                                       \

@@ -5,6 +5,7 @@
 
 #include <cstdint>
 #include <string>
+#include <map>
 #include <vector>
 
 #include "gpu_determ.h"
@@ -96,8 +97,10 @@ struct Context {
     // scratch owned by the context (grown on demand)
     Scratch scratch;
     Scratch step_buf;  // gd_step's nu, gain (FP32) and Q (FP64) when the caller passes none
-    int *d_s_bounds = nullptr;  // chunk boundaries for the current launch shape
-    int s_bounds_cap = 0;
+    // chunk boundaries on the device per chunk count, uploaded once (a
+    // replayed CUDA graph reads them without any host copy)
+    std::map<int, int *> s_bounds_dev;
+    int gain_waves = 2;         // gain launch: at least this many CTAs per SM (autotuned)
     float *d_reduce = nullptr;  // small device scalars (max nu, dt)
     int sm_count = 0;
 };
@@ -153,3 +156,8 @@ int launch_gain_pair(Context &c, const float *f, int ncells, int ld, float *gain
 int ensure_scratch(Context &c, size_t bytes);
 
 }  // namespace gd
+
+// the opaque handle of the C ABI
+struct gd_ctx {
+    gd::Context c;
+};

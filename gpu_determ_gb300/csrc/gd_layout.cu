@@ -4,9 +4,6 @@
 
 #include <algorithm>
 
-struct gd_ctx {
-    gd::Context c;
-};
 
 namespace gd {
 namespace {

@@ -28,9 +28,6 @@
 
 #include "gd_internal.h"
 
-struct gd_ctx {
-    gd::Context c;
-};
 
 namespace gd {
 namespace {

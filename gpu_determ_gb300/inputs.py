@@ -52,3 +52,87 @@ def mixtures(grid: dict, ncells: int, seed: int = 0, kmax: int = 3, u_sigma: flo
             T = float(rng.uniform(*T_range))
             out[:, c] += maxwellian(grid, n, u, T)
     return out.astype(np.float32)
+
+
+def dirichlet_mixture_params(ncells: int, seed: int = 0, kmax: int = 4, u_sigma: float = 1.0,
+                             T_range=(0.5, 2.0)):
+    """Per cell k ~ U{1..kmax} Maxwellians with weights ~ Dirichlet(1, .., 1)
+    (total density 1), u ~ N(0, u_sigma^2 I), T ~ U[T_range] (seeded numpy
+    default_rng): weights [ncells][kmax] (0 past k), u [ncells][kmax][3], T."""
+    rng = np.random.default_rng(seed)
+    k = rng.integers(1, kmax + 1, ncells)
+    wts = rng.dirichlet(np.ones(kmax), ncells)
+    wts = np.where(np.arange(kmax)[None, :] < k[:, None], wts, 0.0)
+    wts /= wts.sum(axis=1, keepdims=True)
+    u = rng.normal(0.0, u_sigma, (ncells, kmax, 3))
+    T = rng.uniform(T_range[0], T_range[1], (ncells, kmax))
+    return wts, u, T
+
+
+def dirichlet_mixtures(grid: dict, ncells: int, seed: int = 0, kmax: int = 4, u_sigma: float = 1.0,
+                       T_range=(0.5, 2.0), chunk: int = 2048, device=None):
+    """Surrogate training distributions (dirichlet_mixture_params), evaluated
+    in FP64 on the host, or on a torch device when one is given (same values
+    up to the exponential's rounding); float32 [n_pnt][ncells]."""
+    wts, u, T = dirichlet_mixture_params(ncells, seed, kmax, u_sigma, T_range)
+    xu, xv, xw = node_velocities(grid)
+    if device is not None:
+        import torch
+        X = torch.from_numpy(np.stack([xu, xv, xw])).to(device)
+        W, U, TT = (torch.from_numpy(a).to(device) for a in (wts, u, T))
+        out = torch.zeros((len(xu), ncells), dtype=torch.float32, device=device)
+        for c0 in range(0, ncells, chunk):
+            c1 = min(ncells, c0 + chunk)
+            acc = torch.zeros((len(xu), c1 - c0), dtype=torch.float64, device=device)
+            for j in range(kmax):
+                uu, tt, w = U[c0:c1, j], TT[c0:c1, j], W[c0:c1, j]
+                c2 = sum((X[a][:, None] - uu[None, :, a]) ** 2 for a in range(3))
+                acc += w[None, :] * (np.pi * tt[None, :]) ** -1.5 * torch.exp(-c2 / tt[None, :])
+            out[:, c0:c1] = acc.float()
+        return out
+    out = np.zeros((len(xu), ncells), np.float32)
+    for c0 in range(0, ncells, chunk):
+        c1 = min(ncells, c0 + chunk)
+        acc = np.zeros((len(xu), c1 - c0))
+        for j in range(kmax):
+            w = wts[c0:c1, j]
+            live = w > 0
+            if not live.any():
+                continue
+            uu, tt = u[c0:c1, j], T[c0:c1, j]
+            c2 = ((xu[:, None] - uu[None, :, 0]) ** 2 + (xv[:, None] - uu[None, :, 1]) ** 2
+                  + (xw[:, None] - uu[None, :, 2]) ** 2)
+            acc += np.where(live[None, :], w[None, :] * (np.pi * tt[None, :]) ** -1.5 * np.exp(-c2 / tt[None, :]), 0.0)
+        out[:, c0:c1] = acc
+    return out
+
+
+def rankine_hugoniot(mach: float = 3.0, gamma: float = 5.0 / 3.0, n1: float = 1.0, T1: float = 1.0) -> dict:
+    """Upstream/downstream states of a normal shock in the convention
+    f ~ n (pi T)^{-3/2} exp(-|xi - u|^2 / T), where T = 2 k T_phys / m and the
+    sound speed is sqrt(gamma T / 2).  Ratios (monatomic gamma = 5/3):
+    n2/n1 = (g+1) M^2 / ((g-1) M^2 + 2), u2 = u1 n1/n2,
+    T2/T1 = (2 g M^2 - (g-1)) ((g-1) M^2 + 2) / ((g+1)^2 M^2).
+    Velocities are along x in the frame moving with (u1 + u2) / 2, so the
+    upstream and downstream bulk speeds are +-(u1 - u2) / 2."""
+    g, M2 = gamma, mach * mach
+    u1 = mach * np.sqrt(g * T1 / 2.0)
+    r = (g + 1) * M2 / ((g - 1) * M2 + 2)
+    tr = (2 * g * M2 - (g - 1)) * ((g - 1) * M2 + 2) / ((g + 1) ** 2 * M2)
+    u2 = u1 / r
+    shift = 0.5 * (u1 + u2)
+    return {"n1": n1, "T1": T1, "u1": u1 - shift, "n2": n1 * r, "T2": T1 * tr, "u2": u2 - shift,
+            "lab_u1": u1, "lab_u2": u2, "density_ratio": r, "temperature_ratio": tr, "frame_shift": shift}
+
+
+def shock_profile(grid: dict, ncells: int, mach: float = 3.0, gamma: float = 5.0 / 3.0, half_width: float = 8.0,
+                  thickness: float = 1.0) -> np.ndarray:
+    """Cells at x_c = -half_width + (c + 1/2) 2 half_width / ncells across a
+    normal shock: f = (1 - w) M(n1, u1, T1) + w M(n2, u2, T2) with
+    w = (1 + tanh(x / thickness)) / 2 (the bimodal Mott-Smith form); float32."""
+    s = rankine_hugoniot(mach, gamma)
+    x = -half_width + (np.arange(ncells) + 0.5) * (2 * half_width / ncells)
+    w = 0.5 * (1 + np.tanh(x / thickness))
+    m1 = maxwellian(grid, s["n1"], (s["u1"], 0, 0), s["T1"])
+    m2 = maxwellian(grid, s["n2"], (s["u2"], 0, 0), s["T2"])
+    return ((1 - w)[None, :] * m1[:, None] + w[None, :] * m2[:, None]).astype(np.float32)

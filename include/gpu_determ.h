@@ -162,6 +162,10 @@ enum { GD_CMATRIX_BF16 = 0, GD_CMATRIX_BF16X3 = 1 };
 int gd_cmatrix_create(gd_ctx *ctx, int mode, gd_cmatrix **out);
 int gd_cmatrix_gain(gd_cmatrix *cm, const float *f, int ncells, int ld, float *gain, gd_stream stream);
 int gd_cmatrix_destroy(gd_cmatrix *cm);
+/* gd_cmatrix_gain synchronises the stream and reports a pipeline time-out of
+ * its kernel, except inside a stream capture; after replaying a captured
+ * graph, gd_cmatrix_check (synchronising) reports it instead. */
+int gd_cmatrix_check(gd_cmatrix *cm, gd_stream stream);
 /* Gain algorithm used by gd_collision and gd_step for this context:
  * GD_GAIN_PAIR (default, FP32 pair-product kernel), GD_GAIN_CMATRIX_BF16 or
  * GD_GAIN_CMATRIX_BF16X3 (builds the context's collision matrices). */
@@ -188,6 +192,115 @@ int gd_compact_to_box(gd_ctx *ctx, const float *compact, int ncells, int ld, flo
  * up (make it before any stream capture).  All calls share the array: calls
  * that overlap on the GPU race, so order them. */
 int gd_gain_noalloc(gd_ctx *ctx, const float *f, int ncells, int ld, float *gain, gd_stream stream);
+
+/* ---- batches of grids, CUDA graphs, autotuning --------------------------- */
+/* A batch steps several (context, cells) groups together: groups on distinct
+ * contexts run concurrently on their own streams, groups on one context in
+ * order.  gd_batch_step performs one gd_step (collision, FP64 projection,
+ * relaxation; moments into m5 when given) for every group.  Its first call
+ * runs eagerly and sizes every buffer; with use_graph each later call replays
+ * one CUDA graph captured on the second call (one cudaGraphLaunch per step).
+ * Adding a group drops the graph.  Steps are ordered after earlier work on
+ * `stream`, and later work on `stream` after them.  Inside the graph the
+ * collision-matrix kernels do not report pipeline time-outs; gd_batch_check
+ * (synchronising) does.  No reference counterpart: the reference steps one
+ * grid, one batch of npx <= 1024 cells, from a host loop (determ.cu:62-80). */
+typedef struct gd_batch gd_batch;
+int gd_batch_create(gd_batch **out);
+int gd_batch_destroy(gd_batch *b);
+int gd_batch_add(gd_batch *b, gd_ctx *ctx, float *f, int ncells, int ld, int mode, float param, double *m5,
+                 float *time_dev, float *dt_dev);
+int gd_batch_step(gd_batch *b, int use_graph, gd_stream stream);
+int gd_batch_check(gd_batch *b);
+int gd_batch_info(const gd_batch *b, int *groups, int *streams, int *graph_nodes, int64_t *steps);
+
+/* Times the gain candidates of a context on the given cells and keeps the
+ * fastest (gain path, and for the pair kernel the minimum CTAs per SM of its
+ * s-chunk split).  path_mask: bits (1 << GD_GAIN_*) that may be chosen; the
+ * collision-matrix paths only when their n_pnt^3 matrices (2 bytes per entry
+ * in BF16, 4 in BF16X3) fit mem_budget bytes.  Allocates a gain buffer for
+ * the duration of the call.  Candidates that run out of memory are skipped
+ * (cand_ms = -1). */
+#define GD_AUTOTUNE_MAX 8
+typedef struct {
+    int path, waves;
+    float best_ms;
+    int n_candidates;
+    int cand_path[GD_AUTOTUNE_MAX], cand_waves[GD_AUTOTUNE_MAX];
+    float cand_ms[GD_AUTOTUNE_MAX];
+} gd_autotune_result;
+int gd_ctx_autotune(gd_ctx *ctx, const float *f, int ncells, int ld, int path_mask, double mem_budget,
+                    gd_autotune_result *res, gd_stream stream);
+
+/* ---- learned surrogate ---------------------------------------------------- */
+/* A small network trained on (f, Q(f)) pairs of the plain method, with BF16
+ * weights, FP32 accumulation and every product on the tcgen05 tensor cores:
+ *   h0 = W0 x + b0 (n_in -> 256), h1 = GELU(W1 h0 + b1) (-> 512),
+ *   h2 = GELU(W2 h1 + b2) (-> 512), z = W3 h2 + b3 + h0 (-> 256),
+ *   y = W4 z + b4 (-> n_out).
+ * x and y use the library layout [feature][cell] with stride ld.
+ * GD_MLP_SCALE_INPUT divides each cell's x by its mean over the n_in
+ * features; GD_MLP_SCALE_OUTPUT multiplies y by the square of that mean (Q is
+ * quadratic in f).  Training minimises the mean over the batch of
+ * sum_i (y_i - t_i)^2 / den, den = sum_i tden_i^2 (tden defaults to t;
+ * scaled like y), den = the batch mean of that sum with GD_MLP_LOSS_BATCH, or
+ * den = n_out with GD_MLP_LOSS_MSE, with Adam (beta 0.9, 0.999, eps 1e-8,
+ * decoupled weight decay).  Global gains (gd_mlp_set_io_scale, default 1)
+ * multiply the scaled input before the first layer and the network output
+ * before the per-cell output scaling, so the weights work on O(1) values.
+ * No reference counterpart. */
+typedef struct gd_mlp gd_mlp;
+enum { GD_MLP_SCALE_INPUT = 1, GD_MLP_SCALE_OUTPUT = 2, GD_MLP_LOSS_MSE = 4, GD_MLP_LOSS_BATCH = 8 };
+typedef struct {
+    int n_in, n_out, n_in_padded, n_out_padded, batch_cap, flags;
+    int64_t steps, num_params;
+    double forward_flop_per_cell;
+    float in_gain, out_gain;
+} gd_mlp_info_t;
+/* batch_cap: largest batch, a multiple of 64.  Weights ~ U(-1/sqrt(fan_in),
+ * 1/sqrt(fan_in)) from a 64-bit LCG seeded by seed, biases 0. */
+int gd_mlp_create(int n_in, int n_out, int batch_cap, int flags, uint64_t seed, gd_mlp **out);
+int gd_mlp_destroy(gd_mlp *mlp);
+int gd_mlp_set_io_scale(gd_mlp *mlp, float in_gain, float out_gain);
+int gd_mlp_info(const gd_mlp *mlp, gd_mlp_info_t *info);
+/* y[n_out][ldy] = net(x[n_in][ldx]) for batch cells (1 <= batch <= cap). */
+int gd_mlp_forward(gd_mlp *mlp, const float *x, int ldx, int batch, float *y, int ldy, gd_stream stream);
+/* One Adam step on batch cells (a multiple of 64); *loss (device, may be
+ * NULL) receives the batch's mean loss before the update. */
+int gd_mlp_train_step(gd_mlp *mlp, const float *x, int ldx, const float *t, int ldt, const float *tden, int ldd,
+                      int batch, float lr, float weight_decay, float *loss, gd_stream stream);
+/* Per-cell loss row_loss[batch] (device) without an update. */
+int gd_mlp_loss(gd_mlp *mlp, const float *x, int ldx, const float *t, int ldt, const float *tden, int ldd, int batch,
+                float *row_loss, gd_stream stream);
+/* Synchronises the stream and reports a tensor-core pipeline time-out. */
+int gd_mlp_check(gd_mlp *mlp, gd_stream stream);
+/* FP32 host block of num_params floats: W_k [out][in] then b_k [out] for
+ * k = 0..4, n_in and n_out padded to multiples of 64 (pads are zero).
+ * gd_mlp_get_grads gives the gradients of the last training step. */
+int gd_mlp_get_params(gd_mlp *mlp, float *host);
+int gd_mlp_set_params(gd_mlp *mlp, const float *host);
+int gd_mlp_get_grads(gd_mlp *mlp, float *host);
+
+/* Surrogate gain with plain-method fallback.  net maps f (n_pnt) to Q
+ * (n_pnt); est (may be NULL) maps f to an estimate of log10 of the relative
+ * L2 error of the surrogate's Q for that cell.  gd_surrogate_gain writes the
+ * exact loss frequency nu, and the gain I = net(f) + nu f for every cell
+ * whose estimate is <= log10(tol); every other cell (all of them when
+ * tol <= 0, none when est is NULL and tol > 0) gets the plain gain of the
+ * context's gain path.  *n_fallback receives that count; est_out (device,
+ * ncells, may be NULL) the estimates.  The call synchronises the stream once
+ * (the fallback count sizes the plain launch).  Follow with gd_project for
+ * the FP64 conservation projection, exactly as after gd_collision.  All
+ * buffers are allocated by gd_surrogate_create for max_cells cells; nothing
+ * is allocated per call.  No reference counterpart. */
+typedef struct gd_surrogate gd_surrogate;
+int gd_surrogate_create(gd_ctx *ctx, gd_mlp *net, gd_mlp *est, int max_cells, gd_surrogate **out);
+int gd_surrogate_destroy(gd_surrogate *s);
+int gd_surrogate_gain(gd_surrogate *s, const float *f, int ncells, int ld, float tol, float *nu, float *gain,
+                      float *est_out, int *n_fallback, gd_stream stream);
+/* out[c] = ||a[:,c] - b[:,c]||_2 / ||b[:,c]||_2 over n rows (FP64). */
+int gd_cell_rel_l2(const double *a, int lda, const double *b, int ldb, int n, int ncells, double *out,
+                   gd_stream stream);
 
 #ifdef __cplusplus
 }

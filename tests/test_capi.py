@@ -70,6 +70,21 @@ def test_null_arguments_rejected(gdlib):
     assert L.gd_ctx_create(None, 0, None) == 1
     assert L.gd_collision(None, None, 1, 1, None, None, None) == 1
     assert L.gd_ctx_destroy(None) == 0
+    out = C.c_void_p()
+    # surrogate, batch and autotuner arguments are checked before any CUDA call
+    assert L.gd_mlp_create(0, 10, 64, 0, 0, C.byref(out)) == 1
+    assert L.gd_mlp_create(10, 10, 100, 0, 0, C.byref(out)) == 1        # cap not a multiple of 64
+    assert L.gd_mlp_create(10, 10, 64, 2, 0, C.byref(out)) == 1         # output scaling needs input scaling
+    assert L.gd_mlp_create(10, 10, 64, 64, 0, C.byref(out)) == 1        # unknown flag
+    assert L.gd_mlp_forward(None, None, 1, 1, None, 1, None) == 1
+    assert L.gd_mlp_train_step(None, None, 64, None, 64, None, 0, 64, 0.0, 0.0, None, None) == 1
+    assert L.gd_surrogate_create(None, None, None, 1, C.byref(out)) == 1
+    assert L.gd_surrogate_gain(None, None, 1, 1, 1.0, None, None, None, None, None) == 1
+    assert L.gd_cell_rel_l2(None, 1, None, 1, 1, 1, None, None) == 1
+    assert L.gd_batch_add(None, None, None, 1, 1, 0, 1.0, None, None, None) == 1
+    assert L.gd_batch_step(None, 1, None) == 1
+    assert L.gd_ctx_autotune(None, None, 1, 1, 1, 0.0, None, None) == 1
+    assert L.gd_mlp_destroy(None) == 0 and L.gd_surrogate_destroy(None) == 0 and L.gd_batch_destroy(None) == 0
 
 
 def test_missing_library_fails_loudly(gdlib, monkeypatch):

@@ -1,0 +1,95 @@
+"""Batches of uneven grids (gd_batch_*) and the autotuner (gd_ctx_autotune).
+
+Steps of a batch, eager or replayed from the captured CUDA graph, must give
+bitwise the same distributions and times as stepping each group alone with
+gd_step: the graph holds the same launches in the same order per context."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+STEPS = 4
+
+
+def _groups(gd, torch):
+    from gpu_determ_gb300 import inputs
+    out = []
+    for n, cells, seed in ((8, 64, 1), (12, 96, 2)):
+        spec = gd.GridSpec(n, R=4.8)
+        ctx = gd.Context(spec)
+        g = spec.fill()
+        out.append((ctx, inputs.shock_profile(g, cells), cells))
+        out.append((ctx, inputs.mixtures(g, 40, seed=seed), 40))   # second group on the same context
+    return out
+
+
+def _run_single(gd, torch, groups):
+    fs, ts = [], []
+    for ctx, f0, cells in groups:
+        f = torch.from_numpy(f0).cuda()
+        t = torch.zeros(1, dtype=torch.float32, device="cuda")
+        for _ in range(STEPS):
+            ctx.step(f, cells, cells, gd.DT_COURANT, 0.5, time=t)
+        fs.append(f)
+        ts.append(t)
+    torch.cuda.synchronize()
+    return [f.cpu().numpy() for f in fs], [float(t.item()) for t in ts]
+
+
+def _run_batch(gd, torch, groups, use_graph):
+    b = gd.Batch()
+    fs, ts, ms = [], [], []
+    for ctx, f0, cells in groups:
+        f = torch.from_numpy(f0).cuda()
+        t = torch.zeros(1, dtype=torch.float32, device="cuda")
+        m5 = torch.zeros((cells, 5), dtype=torch.float64, device="cuda")
+        b.add(ctx, f, cells, cells, gd.DT_COURANT, 0.5, m5=m5, time=t)
+        fs.append(f)
+        ts.append(t)
+        ms.append(m5)
+    for _ in range(STEPS):
+        b.step(use_graph)
+    b.check()
+    info = b.info()
+    b.close()
+    return [f.cpu().numpy() for f in fs], [float(t.item()) for t in ts], info
+
+
+def test_batch_matches_single_steps(gdlib, cuda):
+    torch = cuda
+    groups = _groups(gdlib, torch)
+    f_ref, t_ref = _run_single(gdlib, torch, groups)
+    for use_graph in (False, True):
+        f_b, t_b, info = _run_batch(gdlib, torch, groups, use_graph)
+        assert info["groups"] == 4 and info["streams"] == 2 and info["steps"] == STEPS
+        if use_graph:
+            assert info["graph_nodes"] > 0
+        for a, b in zip(f_ref, f_b):
+            assert np.array_equal(a, b)
+        assert t_ref == t_b
+    assert all(t > 0 for t in t_ref)
+
+
+def test_autotune_picks_a_measured_candidate(gdlib, cuda):
+    torch = cuda
+    from gpu_determ_gb300 import inputs
+    spec = gdlib.GridSpec(12, R=4.8)
+    ctx = gdlib.Context(spec)
+    g = spec.fill()
+    cells = 128
+    f = torch.from_numpy(inputs.mixtures(g, cells, seed=3)).cuda()
+    ref = torch.empty_like(f)
+    ctx.collision(f, cells, cells, None, ref)
+    mask = (1 << gdlib.GAIN_PAIR) | (1 << gdlib.GAIN_CMATRIX_BF16X3)
+    r = ctx.autotune(f, cells, cells, path_mask=mask, mem_budget=8e9)
+    ms = [c["ms"] for c in r["candidates"]]
+    assert len(ms) == 4 and all(m > 0 for m in ms)
+    assert r["best_ms"] == pytest.approx(min(ms))
+    gain = torch.empty_like(f)
+    ctx.collision(f, cells, cells, None, gain)
+    torch.cuda.synchronize()
+    rel = float((gain - ref).norm() / ref.norm())
+    assert rel < (1e-5 if r["path"] == "cmatrix_bf16x3" else 1e-6)
+    # a budget too small for the matrices leaves only the pair kernel
+    r2 = ctx.autotune(f, cells, cells, path_mask=mask, mem_budget=1e3)
+    assert r2["path"] == "pair" and len(r2["candidates"]) == 3
