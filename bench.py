@@ -1,18 +1,26 @@
-"""Throughput of the plain collision step on one GB300 (cells*steps/s).
+"""Collision-step throughput on one GB300 (cells*steps/s): surrogate+fallback vs plain.
 
 Workload: 20^3 velocity lattice on [-5,5]^3 cut to the sphere R=4.8 (3648
-nodes), a batch of spatial cells of seeded Maxwellian mixtures; one step =
-loss nu + gain I + FP64 conservation projection + relaxation (Courant dt).
+nodes), a batch of spatial cells of seeded mixtures of 1-4 Maxwellians
+(Dirichlet(1) weights, u ~ N(0, I), T ~ U[0.5, 2]); one step = loss nu +
+gain I + FP64 conservation projection + relaxation (Courant dt).  The plain
+step computes the gain with the context's gain path (BF16 collision matrices
+on the tensor cores by default); the surrogate step takes the gain from the
+learned network for every cell whose estimated error is within --tol and
+from the plain path for the others (gd_surrogate_gain).  The network is
+trained before the timed region on pairs the plain path generates.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
-Prints one JSON line (rank 0).  `value` times K steps with f resident in HBM
-(CUDA events on the launching stream, L2 flushed between steps); `e2e` times
-the same steps through the C ABI with the distribution copied host->device
-before and device->host after every step; `roofline` covers the gain kernel;
-`cpu_baseline` times the oracle's OpenMP FP32 host path on a bounded sample.
-Under torchrun each rank runs its own batch (weak scaling, no collective on
-the data path) and the time is the maximum over ranks.
+Prints one JSON line (rank 0).  `value` times K surrogate+fallback steps with
+f resident in HBM (CUDA events on the launching stream, L2 flushed between
+steps), `plain` the same for the plain step; `e2e` times the surrogate steps
+through the C ABI with the distribution copied host->device before and
+device->host after every step; `accuracy` compares the step's projected Q with
+the FP32 pair kernel's on the same cells; `roofline` covers the plain gain
+kernel; `cpu_baseline` times the oracle's OpenMP FP32 host path on a bounded
+sample.  Under torchrun each rank runs its own batch (weak scaling, no
+collective on the data path) and the time is the maximum over ranks.
 """
 from __future__ import annotations
 
@@ -30,7 +38,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 
-METRIC = "cells*steps/s at 20^3 grid (deterministic collision step, Q rel-L2 <= 1e-3)"
+METRIC = "cells*steps/s at 20^3 grid: surrogate+fallback vs plain on GB300, rel-L2<=1e-3"
 UNIT = "cell-steps/s"
 PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
 FALLBACK_BF16_TFLOPS = 1900.0
@@ -54,6 +62,10 @@ def parse():
                    help="gain algorithm of the timed step (FP32 pair-product kernel or tensor-core collision matrices)")
     p.add_argument("--alternatives", default="pair,bf16x3",
                    help="comma list of other gain paths to time after the main run ('' for none)")
+    p.add_argument("--no-surrogate", action="store_true", help="time the plain step only")
+    p.add_argument("--tol", type=float, default=1e-3, help="surrogate acceptance tolerance (relative L2 of Q)")
+    p.add_argument("--pairs", type=int, default=65536, help="surrogate training pairs")
+    p.add_argument("--train-steps", type=int, default=6000)
     return p.parse_args()
 
 
@@ -61,10 +73,12 @@ GAIN_PATHS = {"pair": 0, "bf16": 1, "bf16x3": 2}
 
 
 def workload(args, ncells):
-    return {"workload": f"plain collision step, {args.grid}^3 lattice [-5,5]^3 cut to R={args.radius}",
+    kind = "plain collision step" if args.no_surrogate else \
+        f"surrogate+fallback collision step (tol {args.tol:g})"
+    return {"workload": f"{kind}, {args.grid}^3 lattice [-5,5]^3 cut to R={args.radius}",
             "gain": args.gain,
             "cells": ncells, "dt_mode": f"courant {args.courant} (dt = courant / max nu, as relax_f)",
-            "inputs": "seeded Maxwellian mixtures: 1-3 components, n~LogN(0,0.3), u~N(0,0.7^2), T~U[0.6,1.8]",
+            "inputs": "seeded mixtures of 1-4 Maxwellians: Dirichlet(1) weights, u~N(0,I), T~U[0.5,2]",
             "l2": "256 MiB buffer written between timed steps (inside the timed region)"}
 
 
@@ -188,80 +202,108 @@ def run_ours(args):
     n = ctx.n_pnt
     nc = args.cells
     grid = spec.fill()
-    f_host = inputs.mixtures(grid, nc, seed=args.seed + rank)
+    f_host = inputs.dirichlet_mixtures(grid, nc, seed=args.seed + 17 + rank)
     f0 = torch.from_numpy(f_host).cuda()
-    f = f0.clone()
     stream = torch.cuda.current_stream()
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
-
-    def step():
-        ctx.step(f, nc, nc, gd.DT_COURANT, args.courant, stream=stream)
-
-    for _ in range(args.warmup):
-        step()
-    torch.cuda.synchronize()
 
     def barrier():
         if dist is not None:
             dist.barrier()
         torch.cuda.synchronize()
 
-    # device-resident timed region
-    f.copy_(f0)
-    barrier()
-    with Clocks(local) as clk:
-        ev0 = torch.cuda.Event(enable_timing=True)
-        ev1 = torch.cuda.Event(enable_timing=True)
-        ev0.record(stream)
-        for _ in range(args.steps):
-            flush.fill_(1)
-            step()
-        ev1.record(stream)
-        barrier()
-    ms = ev0.elapsed_time(ev1)
-    if dist is not None:
+    def max_over_ranks(ms):
+        if dist is None:
+            return ms
         t = torch.tensor([ms], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    value = world * nc * args.steps / (ms / 1000.0)
+        return float(t.item())
 
-    # end to end through the C ABI with host buffers (pinned), copies timed
-    pinned_in = torch.from_numpy(f_host).pin_memory()
-    pinned_out = torch.empty_like(pinned_in).pin_memory()
-    fdev = torch.empty_like(f0)
-    barrier()
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    for _ in range(args.steps):
-        flush.fill_(1)
-        fdev.copy_(pinned_in, non_blocking=True)
-        ctx.step(fdev, nc, nc, gd.DT_COURANT, args.courant, stream=stream)
-        pinned_out.copy_(fdev, non_blocking=True)
-    e1.record(stream)
-    barrier()
-    ms_e2e = e0.elapsed_time(e1)
-    if dist is not None:
-        t = torch.tensor([ms_e2e], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_e2e = float(t.item())
+    def plain_step(fb):
+        ctx.step(fb, nc, nc, gd.DT_COURANT, args.courant, stream=stream)
+
+    model = None
+    nu = torch.empty_like(f0)
+    gain = torch.empty_like(f0)
+    fallbacks = []
+    if not args.no_surrogate:
+        from gpu_determ_gb300 import surrogate as sg
+        t0 = time.perf_counter()
+        model = sg.fit(ctx, grid, pairs=args.pairs, steps=args.train_steps, max_cells=nc, seed=args.seed)
+        fit_s = time.perf_counter() - t0
+        tol_arg = model.tol_arg(args.tol)
+
+        def sur_step(fb):
+            fallbacks.append(model.surrogate.gain(fb, nc, nc, tol_arg, nu, gain, stream=stream))
+            ctx.project(fb, nu, gain, nc, nc, nu_corr=nu, stream=stream)
+            ctx.relax(fb, nu, gain, nc, nc, gd.DT_COURANT, args.courant, stream=stream)
+
+    def timed(step_fn, host_copies=False):
+        """K steps from f0 (device-resident, or copied from/to pinned host
+        buffers inside the timed region); returns ms."""
+        fb = f0.clone()
+        for _ in range(args.warmup):
+            step_fn(fb)
+        fb.copy_(f0)
+        if host_copies:
+            pin_in = torch.from_numpy(f_host).pin_memory()
+            pin_out = torch.empty_like(pin_in).pin_memory()
+        barrier()
+        with Clocks(local) as clk:
+            ev0 = torch.cuda.Event(enable_timing=True)
+            ev1 = torch.cuda.Event(enable_timing=True)
+            ev0.record(stream)
+            for _ in range(args.steps):
+                flush.fill_(1)
+                if host_copies:
+                    fb.copy_(pin_in, non_blocking=True)
+                step_fn(fb)
+                if host_copies:
+                    pin_out.copy_(fb, non_blocking=True)
+            ev1.record(stream)
+            barrier()
+        return max_over_ranks(ev0.elapsed_time(ev1)), clk
+
+    ms_plain, clk_plain = timed(plain_step)
+    plain_value = world * nc * args.steps / (ms_plain / 1000.0)
+    main_step = plain_step if model is None else sur_step
+    if model is None:
+        ms, clk = ms_plain, clk_plain
+    else:
+        fallbacks.clear()
+        ms, clk = timed(sur_step)
+        fb_timed = fallbacks[args.warmup:] if len(fallbacks) > args.warmup else fallbacks
+    value = world * nc * args.steps / (ms / 1000.0)
+    ms_e2e, _ = timed(main_step, host_copies=True)
     e2e = world * nc * args.steps / (ms_e2e / 1000.0)
     nbytes = n * nc * 4
 
-    # dominant kernel: the gain
+    # dominant kernel: the plain gain (the fallback path)
     peak, peak_kind = peaks()
     roof = gain_roofline(args.gain, ctx, f0, nc, stream, flush, peak, peak_kind, max(2, args.steps))
 
+    dtype = {"pair": "f32", "bf16": "bf16 (FP32 accumulate)", "bf16x3": "bf16x3 (FP32 accumulate)"}[args.gain]
+    plain_launches = 7 if args.gain == "pair" else 6
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None,
-            "dtype": {"pair": "f32", "bf16": "bf16 (FP32 accumulate)", "bf16x3": "bf16x3 (FP32 accumulate)"}[args.gain]
-            + ", FP64 projection",
+            "dtype": dtype + ", FP64 projection" + ("" if model is None else "; surrogate bf16 (FP32 accumulate)"),
             "data": "synthetic", "config": workload(args, nc),
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
                     "ms_per_step": ms_e2e / args.steps},
-            "gpu_launches": (7 if args.gain == "pair" else 6) * args.steps,
-            "clocks": clk.summary(), "roofline": roof}
+            "clocks": clk.summary(), "roofline": roof,
+            "plain": {"value": plain_value, "unit": UNIT, "ms_per_step": ms_plain / args.steps,
+                      "gain": args.gain, "clocks": clk_plain.summary()}}
+    if model is None:
+        line["gpu_launches"] = plain_launches * args.steps
+    else:
+        # loss 1, network 8, nu f 1, error network 8, selection 1, projection 1,
+        # relaxation 3; with fallback cells also gather 1, plain gain 2, scatter 1
+        line["gpu_launches"] = sum(23 + (4 if k > 0 else 0) for k in fb_timed)
+        rep = surrogate_report(args, gd, ctx, model, f0, nc, stream, fit_s, fb_timed, plain_value)
+        rep["speedup_vs_plain"] = value / plain_value
+        line["accuracy"] = next(c for c in rep["tolerance_curve"] if c["tol"] == args.tol)
+        line["surrogate"] = rep
     alts = {}
     if rank == 0 and world == 1:
         alts = alternatives(args, ctx, f0, nc, stream, flush, peak, peak_kind)
@@ -274,6 +316,73 @@ def run_ours(args):
     ctx.close()
     if dist is not None:
         dist.destroy_process_group()
+
+
+def projected_q(gd, ctx, f, nc, gain_fn=None):
+    """FP64 projected Q of one evaluation on f (plain gain, or gain_fn's)."""
+    import torch
+    nu = torch.empty_like(f)
+    gain = torch.empty_like(f)
+    q = torch.zeros(f.shape, dtype=torch.float64, device=f.device)
+    nfb = None
+    if gain_fn is None:
+        ctx.collision(f, nc, nc, nu, gain)
+    else:
+        nfb = gain_fn(f, nu, gain)
+    ctx.project(f, nu, gain, nc, nc, q=q)
+    torch.cuda.synchronize()
+    return q, nfb
+
+
+def surrogate_report(args, gd, ctx, model, f0, nc, stream, fit_s, fb_timed, plain_value):
+    """Accuracy of surrogate+fallback on the timed cells against the FP32 pair
+    kernel's projected Q, and the fallback fraction / throughput trade-off
+    over looser tolerances."""
+    import torch
+    from gpu_determ_gb300 import surrogate as sg
+    ref_ctx = gd.Context(ctx.spec, device=ctx.device)          # FP32 pair kernel (rel-L2 ~1e-6 vs FP64)
+    q_ref, _ = projected_q(gd, ref_ctx, f0, nc)
+    q_plain, _ = projected_q(gd, ctx, f0, nc)
+    phi = sg._basis(ctx, f0.device)
+    err = torch.empty(nc, dtype=torch.float64, device=f0.device)
+
+    def stats(q):
+        gd.cell_rel_l2(q, nc, q_ref, nc, ctx.n_pnt, nc, err)
+        e = err.cpu().numpy()
+        mom = (phi @ q).abs() / (phi.abs() @ q.abs()).clamp_min(1e-300)
+        return {"batch_rel_l2": float(torch.linalg.norm(q - q_ref) / torch.linalg.norm(q_ref)),
+                "cell_rel_l2_median": float(np.median(e)), "cell_rel_l2_p99": float(np.quantile(e, 0.99)),
+                "cell_rel_l2_max": float(e.max()), "conservation_max": float(mom.max())}
+
+    curve = []
+    for tol in sorted({args.tol, 1e-2, 3e-2, 1e-1, 3e-1, 1.0}):
+        ta = model.tol_arg(tol)
+        q, nfb = projected_q(gd, ctx, f0, nc, lambda f, nu, g: model.surrogate.gain(f, nc, nc, ta, nu, g))
+        # one timed step at this tolerance (gain + projection + relaxation)
+        fb = f0.clone()
+        nu = torch.empty_like(f0)
+        g = torch.empty_like(f0)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        model.surrogate.gain(fb, nc, nc, ta, nu, g, stream=stream)
+        ctx.project(fb, nu, g, nc, nc, nu_corr=nu, stream=stream)
+        ctx.relax(fb, nu, g, nc, nc, gd.DT_COURANT, args.courant, stream=stream)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        v = nc / (e0.elapsed_time(e1) / 1000.0)
+        curve.append(dict({"tol": tol, "fallback_fraction": nfb / nc, "value": v, "speedup_vs_plain": v / plain_value},
+                          **stats(q)))
+    q_sur, _ = projected_q(gd, ctx, f0, nc, lambda f, nu, g: model.surrogate.gain(f, nc, nc, float("inf"), nu, g))
+    ref_ctx.close()
+    return {"tol": args.tol, "fallback_fraction": float(np.mean(fb_timed)) / nc if fb_timed else None,
+            "speedup_vs_plain": None, "reference": "FP32 pair kernel + FP64 projection on the same cells",
+            "plain_path": stats(q_plain), "surrogate_only": stats(q_sur), "tolerance_curve": curve,
+            "training": dict(model.report, fit_total_s=round(fit_s, 1)),
+            "network": {"layers": "n->256, 256->512 GELU, 512->512 GELU, 512->256 +residual, 256->n",
+                        "params": model.net.info["num_params"],
+                        "forward_flop_per_cell": model.net.info["forward_flop_per_cell"]}}
 
 
 def gain_roofline(name, ctx, f0, nc, stream, flush, peak, peak_kind, reps):
@@ -304,8 +413,11 @@ def gain_roofline(name, ctx, f0, nc, stream, flush, peak, peak_kind, reps):
             "7 FLOP per pair product + 2 per nonzero-weight term + 1 per scatter update"
     else:
         ns, ns_k = ctx.n_pnt, (ctx.n_pnt + 63) // 64 * 64
-        flop = 2.0 * ns * ((nc + 127) // 128 * 128) * ((ns + 255) // 256 * 256) * ns_k * (3 if name == "bf16x3" else 1)
-        kernel, work = "cmatrix_gain_kernel (tcgen05)", "dense tile MACs x 2 (x3 passes for bf16x3)"
+        num_n, num_k = (ns + 255) // 256, ns_k // 64
+        tiles = sum(min(num_k, ((n + 1) * 256 + 63) // 64) for n in range(num_n))  # block upper triangle
+        flop = 2.0 * ns * ((nc + 127) // 128 * 128) * 256 * 64 * tiles * (3 if name == "bf16x3" else 1)
+        kernel, work = "cmatrix_gain_kernel (tcgen05)", \
+            "MACs x 2 of the 128x256x64 tiles issued (block upper triangle of each symmetric G_i; x3 for bf16x3)"
     ach = flop / g_avg / 1e12
     return {"bound": "tensor", "kernel": kernel, "achieved": ach, "peak": peak, "unit": "TFLOP/s",
             "frac": ach / peak, "peak_source": f"{peak_kind} bf16 dense (MEASURED_PEAKS.json)", "work": work,

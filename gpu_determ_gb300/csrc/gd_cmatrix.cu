@@ -53,6 +53,16 @@ struct CmParams {
     int *err;        // set to 1 when a wait times out
 };
 
+// G_i is symmetric in (a, b), so only its block upper triangle is stored and
+// contracted: entries with a < b doubled, the diagonal kept, a > b zero.  The
+// b-tile n (rows b in [n BN, (n+1) BN)) then needs the a-tiles up to the end
+// of its own b range.
+__host__ __device__ __forceinline__ int k_end(int n, int num_k)
+{
+    const int e = ((n + 1) * BN + BK - 1) / BK;
+    return e < num_k ? e : num_k;
+}
+
 // NPASS = 1: D = F_hi G_hi.  NPASS = 3: D = F_hi G_hi + F_hi G_lo + F_lo G_hi.
 template <int NPASS>
 __global__ void __launch_bounds__(kThreads, 1)
@@ -105,24 +115,30 @@ __global__ void __launch_bounds__(kThreads, 1)
     if (warp == 0) {
         // ---- TMA producer ----------------------------------------------------
         if (lane == 0) {
-            const int total = num_n * num_k;
-            for (int it = 0; it < total; it++) {
+            int it = 0;
+            bool stop = false;
+            for (int n = 0; n < num_n && !stop; n++)
+                for (int k = 0; k < k_end(n, num_k); k++, it++) {
                 const int s = it % S;
                 const uint32_t ph = (uint32_t)(it / S) & 1u;
                 if (!mbar_wait(smem_u32(&empty_bar[s]), ph ^ 1u, p.err)) {
                     abort_flag = 1;
+                    stop = true;
                     break;
                 }
-                if (*(volatile int *)&abort_flag) break;
-                const int n = it / num_k, k = it % num_k;
+                if (*(volatile int *)&abort_flag) {
+                    stop = true;
+                    break;
+                }
                 unsigned char *st = base + (size_t)s * kStage;
                 const uint32_t fb = smem_u32(&full_bar[s]);
                 mbar_expect_tx(fb, kStage);
                 tma_load_2d(smem_u32(st), &tmFh, k * BK, m_tile * BM, fb);
-                tma_load_3d(smem_u32(st + kTileA), &tmGh, k * BK, n * BN, node, fb);
+                // G tile it of node's triangle ([node][tile][BN rows][BK])
+                tma_load_4d(smem_u32(st + kTileA), &tmGh, 0, 0, it, node, fb);
                 if (NPARTS == 2) {
                     tma_load_2d(smem_u32(st + kTileA + kTileB), &tmFl, k * BK, m_tile * BM, fb);
-                    tma_load_3d(smem_u32(st + 2 * kTileA + kTileB), &tmGl, k * BK, n * BN, node, fb);
+                    tma_load_4d(smem_u32(st + 2 * kTileA + kTileB), &tmGl, 0, 0, it, node, fb);
                 }
             }
         }
@@ -130,6 +146,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         // ---- MMA issuer --------------------------------------------------------
         if (lane == 0) {
             bool ok = true;
+            int it = 0;
             for (int n = 0; n < num_n && ok; n++) {
                 const int buf = n & 1;
                 const uint32_t use = (uint32_t)(n >> 1);
@@ -139,8 +156,8 @@ __global__ void __launch_bounds__(kThreads, 1)
                 }
                 asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
                 const uint32_t d_tmem = tmem + (uint32_t)(buf * BN);
-                for (int k = 0; k < num_k; k++) {
-                    const int it = n * num_k + k;
+                const int kn = k_end(n, num_k);
+                for (int k = 0; k < kn; k++, it++) {
                     const int s = it % S;
                     const uint32_t ph = (uint32_t)(it / S) & 1u;
                     if (!mbar_wait(smem_u32(&full_bar[s]), ph, p.err)) {
@@ -209,19 +226,27 @@ __global__ void __launch_bounds__(kThreads, 1)
     }
 }
 
-// G[i][b][a] for i < ns, b, a < ns_k (zero for padding): hi = bf16(v),
-// lo = bf16(v - hi) with v = m(d) w(|2i - s|, |d|) [s - i in box].
-__global__ void assemble_g_kernel(Dims d, int ns_k, const uint32_t *__restrict__ nodes,
-                                  const float *__restrict__ w_dense, __nv_bfloat16 *__restrict__ gh,
-                                  __nv_bfloat16 *__restrict__ gl)
+// G_i in tiles of BN rows (b) x BK columns (a): tile t of the block upper
+// triangle is (n, k) = tile_nk[t], stored at [i][t][b - n BN][a - k BK];
+// hi = bf16(v), lo = bf16(v - hi), v = u(a, b) m(d) w(|2i - s|, |d|) [s - i in
+// box] with u = 2 above the diagonal (a < b), 1 on it, 0 below (G_i is
+// symmetric, so the triangle carries the whole bilinear form).  Zero for
+// padding rows and columns.
+__global__ void assemble_g_kernel(Dims d, int tiles, const int2 *__restrict__ tile_nk,
+                                  const uint32_t *__restrict__ nodes, const float *__restrict__ w_dense,
+                                  __nv_bfloat16 *__restrict__ gh, __nv_bfloat16 *__restrict__ gl)
 {
-    const int64_t rows = (int64_t)d.n_pnt * ns_k;  // (i, b) rows of ns_k entries
-    const int vec = ns_k / 8;
-    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < rows * vec;
-         t += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t r = t / vec;
-        const int a0 = (int)(t % vec) * 8;
-        const int i = (int)(r / ns_k), b = (int)(r % ns_k);
+    const int64_t rows = (int64_t)d.n_pnt * tiles * BN;  // (i, t, b) rows of BK entries
+    constexpr int vec = BK / 8;
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < rows * vec;
+         q += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t r = q / vec;
+        const int rr = (int)(r % BN);
+        const int64_t it = r / BN;
+        const int t = (int)(it % tiles), i = (int)(it / tiles);
+        const int2 nk = tile_nk[t];
+        const int b = nk.x * BN + rr;
+        const int a0 = nk.y * BK + (int)(q % vec) * 8;
         __align__(16) __nv_bfloat16 hv[8], lv[8];
         const uint32_t qi = nodes[i];
         const int ix = qi & 1023, iy = (qi >> 10) & 1023, iz = qi >> 20;
@@ -232,7 +257,7 @@ __global__ void assemble_g_kernel(Dims d, int ns_k, const uint32_t *__restrict__
         for (int j = 0; j < 8; j++) {
             const int a = a0 + j;
             float v = 0.f;
-            if (bin && a < d.n_pnt) {
+            if (bin && a < d.n_pnt && a <= b) {
                 const uint32_t qa = nodes[a];
                 const int ax = qa & 1023, ay = (qa >> 10) & 1023, az = qa >> 20;
                 const int sx = ax + bx, sy = ay + by, sz = az + bz;
@@ -244,13 +269,14 @@ __global__ void assemble_g_kernel(Dims d, int ns_k, const uint32_t *__restrict__
                         ((int64_t)((dx >> 1) * d.nx + gx) * (d.hy * d.hz) + (dy >> 1) * d.hz + (dz >> 1)) * d.nyz +
                         gy * d.nz + gz;
                     const float m = (dx == 0 ? 1.f : 0.5f) * (dy == 0 ? 2.f : 1.f) * (dz == 0 ? 2.f : 1.f);
-                    v = m * w_dense[widx];
+                    const float g = m * w_dense[widx];
+                    v = a < b ? 2.f * g : g;  // exact factor 2
                 }
             }
             hv[j] = __float2bfloat16_rn(v);
             lv[j] = __float2bfloat16_rn(v - __bfloat162float(hv[j]));
         }
-        const size_t o = (size_t)r * ns_k + a0;
+        const size_t o = (size_t)r * BK + (size_t)(q % vec) * 8;
         *reinterpret_cast<uint4 *>(gh + o) = *reinterpret_cast<const uint4 *>(hv);
         if (gl) *reinterpret_cast<uint4 *>(gl + o) = *reinterpret_cast<const uint4 *>(lv);
     }
@@ -300,7 +326,7 @@ int get_encoder(EncodeTiled *out)
 int encode(EncodeTiled fn, CUtensorMap *m, void *ptr, int rank, const cuuint64_t *dims, const cuuint64_t *strides,
            const cuuint32_t *box)
 {
-    const cuuint32_t es[3] = {1, 1, 1};
+    const cuuint32_t es[4] = {1, 1, 1, 1};
     CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, (cuuint32_t)rank, ptr, dims, strides, box, es,
                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
@@ -315,6 +341,7 @@ struct gd_cmatrix {
     gd_ctx *ctx = nullptr;
     int mode = 0;  // GD_CMATRIX_BF16 or GD_CMATRIX_BF16X3
     int ns = 0, ns_k = 0;
+    int tiles = 0;  // BN x BK tiles of one node's block upper triangle
     __nv_bfloat16 *gh = nullptr, *gl = nullptr;
     __nv_bfloat16 *fh = nullptr, *fl = nullptr;
     int f_cells = 0;
@@ -337,7 +364,12 @@ extern "C" int gd_cmatrix_create(gd_ctx *ctx, int mode, gd_cmatrix **out)
     h->mode = mode;
     h->ns = d.n_pnt;
     h->ns_k = (d.n_pnt + BK - 1) / BK * BK;
-    const size_t elems = (size_t)h->ns * h->ns_k * h->ns_k;
+    const int num_n = (h->ns + BN - 1) / BN, num_k = h->ns_k / BK;
+    std::vector<int2> tile_nk;
+    for (int n = 0; n < num_n; n++)
+        for (int k = 0; k < k_end(n, num_k); k++) tile_nk.push_back(make_int2(n, k));
+    h->tiles = (int)tile_nk.size();
+    const size_t elems = (size_t)h->ns * h->tiles * BN * BK;
     size_t free_b = 0, total_b = 0;
     GD_CUDA(cudaMemGetInfo(&free_b, &total_b));
     const size_t need = elems * 2 * (mode == GD_CMATRIX_BF16X3 ? 2 : 1);
@@ -347,24 +379,29 @@ extern "C" int gd_cmatrix_create(gd_ctx *ctx, int mode, gd_cmatrix **out)
                                                    " MiB; free device memory is " + std::to_string(free_b >> 20) + " MiB");
     }
     float *w = nullptr;
+    int2 *d_tiles = nullptr;
     const size_t na = (size_t)d.hx * d.nx * d.hy * d.hz * d.nyz;
     cudaError_t e = cudaMalloc(&h->gh, elems * 2);
     if (e == cudaSuccess && mode == GD_CMATRIX_BF16X3) e = cudaMalloc(&h->gl, elems * 2);
     if (e == cudaSuccess) e = cudaMalloc(&h->err, sizeof(int));
     if (e == cudaSuccess) e = cudaMalloc(&w, na * sizeof(float));
+    if (e == cudaSuccess) e = cudaMalloc(&d_tiles, sizeof(int2) * tile_nk.size());
+    if (e == cudaSuccess)
+        e = cudaMemcpy(d_tiles, tile_nk.data(), sizeof(int2) * tile_nk.size(), cudaMemcpyHostToDevice);
     int rc = GD_OK;
     if (e != cudaSuccess) rc = cuda_error(e, "collision-matrix allocation");
     if (!rc) rc = launch_dense_tables(d, nullptr, w, nullptr);
     if (!rc) {
-        const int64_t work = (int64_t)h->ns * h->ns_k * (h->ns_k / 8);
+        const int64_t work = (int64_t)h->ns * h->tiles * BN * (BK / 8);
         const int blocks = (int)std::min<int64_t>((work + 255) / 256, (int64_t)c.sm_count * 64);
-        assemble_g_kernel<<<blocks, 256>>>(d, h->ns_k, c.d_nodes, w, h->gh, h->gl);
+        assemble_g_kernel<<<blocks, 256>>>(d, h->tiles, d_tiles, c.d_nodes, w, h->gh, h->gl);
         e = cudaGetLastError();
         if (e == cudaSuccess) e = cudaMemset(h->err, 0, sizeof(int));
         if (e == cudaSuccess) e = cudaDeviceSynchronize();
         if (e != cudaSuccess) rc = cuda_error(e, "collision-matrix assembly");
     }
     cudaFree(w);
+    cudaFree(d_tiles);
     if (rc) {
         cudaFree(h->gh);
         cudaFree(h->gl);
@@ -415,14 +452,14 @@ extern "C" int gd_cmatrix_gain(gd_cmatrix *h, const float *f, int ncells, int ld
     const cuuint64_t fdims[2] = {(cuuint64_t)h->ns_k, (cuuint64_t)ncells};
     const cuuint64_t fstr[1] = {(cuuint64_t)h->ns_k * 2};
     const cuuint32_t fbox[2] = {BK, BM};
-    const cuuint64_t gdims[3] = {(cuuint64_t)h->ns_k, (cuuint64_t)h->ns_k, (cuuint64_t)h->ns};
-    const cuuint64_t gstr[2] = {(cuuint64_t)h->ns_k * 2, (cuuint64_t)h->ns_k * h->ns_k * 2};
-    const cuuint32_t gbox[3] = {BK, BN, 1};
+    const cuuint64_t gdims[4] = {(cuuint64_t)BK, (cuuint64_t)BN, (cuuint64_t)h->tiles, (cuuint64_t)h->ns};
+    const cuuint64_t gstr[3] = {(cuuint64_t)BK * 2, (cuuint64_t)BN * BK * 2, (cuuint64_t)h->tiles * BN * BK * 2};
+    const cuuint32_t gbox[4] = {BK, BN, 1, 1};
     if ((rc = encode(enc, &tFh, h->fh, 2, fdims, fstr, fbox))) return rc;
-    if ((rc = encode(enc, &tGh, h->gh, 3, gdims, gstr, gbox))) return rc;
+    if ((rc = encode(enc, &tGh, h->gh, 4, gdims, gstr, gbox))) return rc;
     if (split) {
         if ((rc = encode(enc, &tFl, h->fl, 2, fdims, fstr, fbox))) return rc;
-        if ((rc = encode(enc, &tGl, h->gl, 3, gdims, gstr, gbox))) return rc;
+        if ((rc = encode(enc, &tGl, h->gl, 4, gdims, gstr, gbox))) return rc;
     } else {
         tFl = tFh;
         tGl = tGh;

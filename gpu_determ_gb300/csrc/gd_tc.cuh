@@ -74,6 +74,41 @@ __device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap *map
         : "memory");
 }
 
+__device__ __forceinline__ void tma_load_4d(uint32_t dst, const CUtensorMap *map, int c0, int c1, int c2, int c3,
+                                            uint32_t bar)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], [%6];"
+        ::"r"(dst), "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(bar)
+        : "memory");
+}
+
+// Multicast variant: the box lands at the same shared-memory offset in every
+// CTA of the cluster named in cta_mask, each CTA's mbarrier at `bar` receiving
+// the complete_tx of the bytes written there.
+__device__ __forceinline__ void tma_load_3d_mc(uint32_t dst, const CUtensorMap *map, int c0, int c1, int c2,
+                                               uint32_t bar, uint16_t cta_mask)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes.multicast::cluster"
+        " [%0], [%1, {%2, %3, %4}], [%5], %6;"
+        ::"r"(dst), "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(bar), "h"(cta_mask)
+        : "memory");
+}
+
+__device__ __forceinline__ uint32_t cluster_rank()
+{
+    uint32_t r;
+    asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+    return r;
+}
+
+// All threads of all CTAs of the cluster (release/acquire).
+__device__ __forceinline__ void cluster_sync()
+{
+    asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+
 // Shared-memory matrix descriptor: K-major operand in the 128-byte swizzle
 // layout TMA writes (rows of 128 bytes, 8-row groups 1024 bytes apart).
 __device__ __forceinline__ uint64_t umma_desc(uint32_t addr)
@@ -107,6 +142,16 @@ __device__ __forceinline__ void umma_commit(uint32_t bar)
 {
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
                  : "memory");
+}
+
+// Arrive once on the mbarrier at `bar` in every CTA of cta_mask when the
+// issuing thread's earlier tcgen05 operations complete.
+__device__ __forceinline__ void umma_commit_mc(uint32_t bar, uint16_t cta_mask)
+{
+    asm volatile(
+        "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 [%0], %1;"
+        ::"r"(bar), "h"(cta_mask)
+        : "memory");
 }
 
 __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float *v)
