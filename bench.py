@@ -418,10 +418,18 @@ def gain_roofline(name, ctx, f0, nc, stream, flush, peak, peak_kind, reps):
         flop = 2.0 * ns * ((nc + 127) // 128 * 128) * 256 * 64 * tiles * (3 if name == "bf16x3" else 1)
         kernel, work = "cmatrix_gain_kernel (tcgen05)", \
             "MACs x 2 of the 128x256x64 tiles issued (block upper triangle of each symmetric G_i; x3 for bf16x3)"
+    traffic, traffic_src = None, None
+    if name != "pair":
+        # DRAM bytes per launch: the collision matrices stream through once.  An
+        # ncu capture of the same kernel on 14^3 / 512 cells read 3.621 GB for
+        # 3.525 GB of matrix tiles (ratio 1.027); scaled here by the matrix bytes.
+        g_bytes = ns * tiles * 256 * 64 * 2 * (2 if name == "bf16x3" else 1)
+        traffic = 1.027 * g_bytes
+        traffic_src = "ncu dram__bytes_read+write of a 14^3/512-cell launch, scaled by collision-matrix bytes"
     ach = flop / g_avg / 1e12
     return {"bound": "tensor", "kernel": kernel, "achieved": ach, "peak": peak, "unit": "TFLOP/s",
             "frac": ach / peak, "peak_source": f"{peak_kind} bf16 dense (MEASURED_PEAKS.json)", "work": work,
-            "flop_per_launch": flop, "traffic": None, "launch_ms": g_avg * 1000.0}
+            "flop_per_launch": flop, "traffic": traffic, "traffic_source": traffic_src, "launch_ms": g_avg * 1000.0}
 
 
 def one_step_q(gd, ctx, f0, nc):
