@@ -412,18 +412,17 @@ def gain_roofline(name, ctx, f0, nc, stream, flush, peak, peak_kind, reps):
         kernel, work = "gain_pair_kernel (+ chunk reduction)", \
             "7 FLOP per pair product + 2 per nonzero-weight term + 1 per scatter update"
     else:
-        ns, ns_k = ctx.n_pnt, (ctx.n_pnt + 63) // 64 * 64
-        num_n, num_k = (ns + 255) // 256, ns_k // 64
-        tiles = sum(min(num_k, ((n + 1) * 256 + 63) // 64) for n in range(num_n))  # block upper triangle
-        flop = 2.0 * ns * ((nc + 127) // 128 * 128) * 256 * 64 * tiles * (3 if name == "bf16x3" else 1)
+        # stored tiles: the nonzero 256 x 64 tiles of each G_i's block upper triangle
+        tiles = ctx._info()["cmatrix_tiles"]
+        flop = 2.0 * ((nc + 127) // 128 * 128) * 256 * 64 * tiles * (3 if name == "bf16x3" else 1)
         kernel, work = "cmatrix_gain_kernel (tcgen05)", \
-            "MACs x 2 of the 128x256x64 tiles issued (block upper triangle of each symmetric G_i; x3 for bf16x3)"
+            "MACs x 2 of the 128x256x64 tiles issued (nonzero tiles of the block upper triangle of each symmetric G_i; x3 for bf16x3)"
     traffic, traffic_src = None, None
     if name != "pair":
         # DRAM bytes per launch: the collision matrices stream through once.  An
         # ncu capture of the same kernel on 14^3 / 512 cells read 3.621 GB for
         # 3.525 GB of matrix tiles (ratio 1.027); scaled here by the matrix bytes.
-        g_bytes = ns * tiles * 256 * 64 * 2 * (2 if name == "bf16x3" else 1)
+        g_bytes = tiles * 256 * 64 * 2 * (2 if name == "bf16x3" else 1)
         traffic = 1.027 * g_bytes
         traffic_src = "ncu dram__bytes_read+write of a 14^3/512-cell launch, scaled by collision-matrix bytes"
     ach = flop / g_avg / 1e12

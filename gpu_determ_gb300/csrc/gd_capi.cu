@@ -471,6 +471,7 @@ int gd_ctx_info(const gd_ctx *ctx, gd_info *out)
     out->pair_products = ctx->c.pair_products;
     out->contraction_terms = ctx->c.contraction_terms;
     out->scatter_terms = ctx->c.scatter_terms;
+    out->cmatrix_tiles = gd::cmatrix_stored_tiles(ctx->c.cmatrix);
     return GD_OK;
 }
 
@@ -494,7 +495,7 @@ int gd_collision(gd_ctx *ctx, const float *f, int ncells, int ld, float *nu, flo
     if (rc) return rc;
     gd::DeviceGuard g(ctx->c.device);
     cudaStream_t st = (cudaStream_t)stream;
-    if (nu && (rc = gd::run_loss(ctx->c, f, ncells, ld, nu, st))) return rc;
+    if (nu && (rc = gd::run_loss_path(ctx->c, f, ncells, ld, nu, st))) return rc;
     if (gain && (rc = gd::run_gain_path(ctx->c, f, ncells, ld, gain, st))) return rc;
     return GD_OK;
 }
@@ -553,7 +554,7 @@ int gd_step(gd_ctx *ctx, float *f, int ncells, int ld, int mode, float param, fl
         if (!nu_b) nu_b = reinterpret_cast<float *>(p + n * sizeof(double));
         if (!gain_b) gain_b = reinterpret_cast<float *>(p + n * (sizeof(double) + sizeof(float)));
     }
-    rc = gd::run_loss(c, f, ncells, ld, nu_b, st);
+    rc = gd::run_loss_path(c, f, ncells, ld, nu_b, st);
     if (!rc) rc = gd::run_gain_path(c, f, ncells, ld, gain_b, st);
     if (!rc) rc = gd::run_project(c, f, nu_b, gain_b, ncells, ld, nu_b, q_b, nullptr, 0, 0.f, nullptr, m5, st);
     if (!rc) rc = gd::run_relax_q(c, f, nu_b, gain_b, q_b, ncells, ld, mode, param, time_dev, dt_dev, st);

@@ -51,6 +51,8 @@ struct CmParams {
     const float *f;  // [ns][ld] FP32 distribution (epilogue)
     float *gain;     // [ns][ld]
     int *err;        // set to 1 when a wait times out
+    const int *node_off;     // [ns + 1] each node's range of stored tiles
+    const uint32_t *tiles;   // stored tiles, n << 16 | k, n-major then k within each node
 };
 
 // G_i is symmetric in (a, b), so only its block upper triangle is stored and
@@ -83,8 +85,6 @@ __global__ void __launch_bounds__(kThreads, 1)
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int m_tile = blockIdx.x, node = blockIdx.y;
-    const int num_k = p.ns_k / BK;
-    const int num_n = (p.ns + BN - 1) / BN;
 
     if (threadIdx.x == 0) abort_flag = *(volatile int *)p.err;
     __syncthreads();
@@ -115,30 +115,25 @@ __global__ void __launch_bounds__(kThreads, 1)
     if (warp == 0) {
         // ---- TMA producer ----------------------------------------------------
         if (lane == 0) {
-            int it = 0;
-            bool stop = false;
-            for (int n = 0; n < num_n && !stop; n++)
-                for (int k = 0; k < k_end(n, num_k); k++, it++) {
+            const int l0 = __ldg(p.node_off + node), cnt = __ldg(p.node_off + node + 1) - l0;
+            for (int it = 0; it < cnt; it++) {
                 const int s = it % S;
                 const uint32_t ph = (uint32_t)(it / S) & 1u;
                 if (!mbar_wait(smem_u32(&empty_bar[s]), ph ^ 1u, p.err)) {
                     abort_flag = 1;
-                    stop = true;
                     break;
                 }
-                if (*(volatile int *)&abort_flag) {
-                    stop = true;
-                    break;
-                }
+                if (*(volatile int *)&abort_flag) break;
+                const int k = (int)(__ldg(p.tiles + l0 + it) & 0xffffu);
                 unsigned char *st = base + (size_t)s * kStage;
                 const uint32_t fb = smem_u32(&full_bar[s]);
                 mbar_expect_tx(fb, kStage);
                 tma_load_2d(smem_u32(st), &tmFh, k * BK, m_tile * BM, fb);
-                // G tile it of node's triangle ([node][tile][BN rows][BK])
-                tma_load_4d(smem_u32(st + kTileA), &tmGh, 0, 0, it, node, fb);
+                // stored tile l0 + it ([slot][BN rows][BK])
+                tma_load_3d(smem_u32(st + kTileA), &tmGh, 0, 0, l0 + it, fb);
                 if (NPARTS == 2) {
                     tma_load_2d(smem_u32(st + kTileA + kTileB), &tmFl, k * BK, m_tile * BM, fb);
-                    tma_load_4d(smem_u32(st + 2 * kTileA + kTileB), &tmGl, 0, 0, it, node, fb);
+                    tma_load_3d(smem_u32(st + 2 * kTileA + kTileB), &tmGl, 0, 0, l0 + it, fb);
                 }
             }
         }
@@ -146,18 +141,20 @@ __global__ void __launch_bounds__(kThreads, 1)
         // ---- MMA issuer --------------------------------------------------------
         if (lane == 0) {
             bool ok = true;
-            int it = 0;
-            for (int n = 0; n < num_n && ok; n++) {
-                const int buf = n & 1;
-                const uint32_t use = (uint32_t)(n >> 1);
+            const int l0 = __ldg(p.node_off + node), cnt = __ldg(p.node_off + node + 1) - l0;
+            int it = 0, grp = 0;  // stored tile, group of tiles sharing one b-tile n
+            while (ok && it < cnt) {
+                const uint32_t n = __ldg(p.tiles + l0 + it) >> 16;
+                const int buf = grp & 1;
+                const uint32_t use = (uint32_t)(grp >> 1);
                 if (!mbar_wait(smem_u32(&acce_bar[buf]), (use & 1u) ^ 1u, p.err)) {
                     ok = false;
                     break;
                 }
                 asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
                 const uint32_t d_tmem = tmem + (uint32_t)(buf * BN);
-                const int kn = k_end(n, num_k);
-                for (int k = 0; k < kn; k++, it++) {
+                bool first = true;
+                for (; it < cnt && (__ldg(p.tiles + l0 + it) >> 16) == n; it++) {
                     const int s = it % S;
                     const uint32_t ph = (uint32_t)(it / S) & 1u;
                     if (!mbar_wait(smem_u32(&full_bar[s]), ph, p.err)) {
@@ -171,7 +168,7 @@ __global__ void __launch_bounds__(kThreads, 1)
 #pragma unroll
                     for (int kk = 0; kk < BK / 16; kk++) {
                         const uint32_t off = (uint32_t)kk * 32u;  // 16 BF16 along K
-                        const uint32_t acc = (k > 0 || kk > 0) ? 1u : 0u;
+                        const uint32_t acc = (!first || kk > 0) ? 1u : 0u;
                         umma_bf16(d_tmem, umma_desc(aH + off), umma_desc(bH + off), kIdesc, acc);
                         if (NPASS == 3) {
                             umma_bf16(d_tmem, umma_desc(aH + off), umma_desc(bL + off), kIdesc, 1u);
@@ -179,9 +176,11 @@ __global__ void __launch_bounds__(kThreads, 1)
                         }
                     }
                     umma_commit(smem_u32(&empty_bar[s]));
+                    first = false;
                 }
                 if (!ok) break;
                 umma_commit(smem_u32(&accf_bar[buf]));
+                grp++;
             }
             if (!ok) abort_flag = 1;
         }
@@ -192,9 +191,13 @@ __global__ void __launch_bounds__(kThreads, 1)
         const int cell = m_tile * BM + row;
         const bool live = cell < p.ncells;
         float sum = 0.f;
-        for (int n = 0; n < num_n; n++) {
-            const int buf = n & 1;
-            const uint32_t use = (uint32_t)(n >> 1);
+        const int l0 = __ldg(p.node_off + node), cnt = __ldg(p.node_off + node + 1) - l0;
+        for (int it = 0, grp = 0; it < cnt; grp++) {
+            // b-tiles without stored tiles contribute nothing and are skipped
+            const int n = (int)(__ldg(p.tiles + l0 + it) >> 16);
+            while (it < cnt && (int)(__ldg(p.tiles + l0 + it) >> 16) == n) it++;
+            const int buf = grp & 1;
+            const uint32_t use = (uint32_t)(grp >> 1);
             bool ok = true;
             if (lane == 0) ok = mbar_wait(smem_u32(&accf_bar[buf]), use & 1u, p.err);
             ok = __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
@@ -235,8 +238,13 @@ __global__ void __launch_bounds__(kThreads, 1)
 // box] with u = 2 above the diagonal (a < b), 1 on it, 0 below (G_i is
 // symmetric, so the triangle carries the whole bilinear form).  Zero for
 // padding rows and columns.
+//
+// Two passes: with nz set, only mark the triangle tiles holding a nonzero
+// entry (every writer stores 1); otherwise write each entry into the stored
+// slot slot_of[i * tiles + t] of its tile (tiles that are all zero have no slot).
 __global__ void assemble_g_kernel(Dims d, int tiles, const int2 *__restrict__ tile_nk,
                                   const uint32_t *__restrict__ nodes, const float *__restrict__ w_dense,
+                                  uint8_t *__restrict__ nz, const int *__restrict__ slot_of,
                                   __nv_bfloat16 *__restrict__ gh, __nv_bfloat16 *__restrict__ gl)
 {
     const int64_t rows = (int64_t)d.n_pnt * tiles * BN;  // (i, t, b) rows of BK entries
@@ -247,6 +255,8 @@ __global__ void assemble_g_kernel(Dims d, int tiles, const int2 *__restrict__ ti
         const int rr = (int)(r % BN);
         const int64_t it = r / BN;
         const int t = (int)(it % tiles), i = (int)(it / tiles);
+        const int slot = nz ? 0 : slot_of[it];
+        if (slot < 0) continue;
         const int2 nk = tile_nk[t];
         const int b = nk.x * BN + rr;
         const int a0 = nk.y * BK + (int)(q % vec) * 8;
@@ -279,9 +289,38 @@ __global__ void assemble_g_kernel(Dims d, int tiles, const int2 *__restrict__ ti
             hv[j] = __float2bfloat16_rn(v);
             lv[j] = __float2bfloat16_rn(v - __bfloat162float(hv[j]));
         }
-        const size_t o = (size_t)r * BK + (size_t)(q % vec) * 8;
+        if (nz) {
+            bool any = false;
+#pragma unroll
+            for (int j = 0; j < 8; j++) any |= __bfloat162float(hv[j]) != 0.f;
+            if (any) nz[it] = 1;
+            continue;
+        }
+        const size_t o = ((size_t)slot * BN + rr) * BK + (size_t)(q % vec) * 8;
         *reinterpret_cast<uint4 *>(gh + o) = *reinterpret_cast<const uint4 *>(hv);
         if (gl) *reinterpret_cast<uint4 *>(gl + o) = *reinterpret_cast<const uint4 *>(lv);
+    }
+}
+
+// Loss matrix B[i][j] = b(|i - j|) (hi/lo BF16, j padded to ns_k with zeros),
+// so that nu = B f is a GEMM: nu[i][c] = sum_j B[i][j] f[j][c].
+__global__ void assemble_b_kernel(Dims d, int ns_k, const uint32_t *__restrict__ nodes, const float *__restrict__ b,
+                                  __nv_bfloat16 *__restrict__ bh, __nv_bfloat16 *__restrict__ bl)
+{
+    const int64_t total = (int64_t)d.n_pnt * ns_k;
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < total; q += (int64_t)gridDim.x * blockDim.x) {
+        const int i = (int)(q / ns_k), j = (int)(q % ns_k);
+        float v = 0.f;
+        if (j < d.n_pnt) {
+            const uint32_t pi = nodes[i], pj = nodes[j];
+            const int dx = abs((int)(pi & 1023) - (int)(pj & 1023));
+            const int dy = abs((int)((pi >> 10) & 1023) - (int)((pj >> 10) & 1023));
+            const int dz = abs((int)(pi >> 20) - (int)(pj >> 20));
+            v = b[dx * d.nyz + dy * d.nz + dz];
+        }
+        const __nv_bfloat16 h = __float2bfloat16_rn(v);
+        bh[q] = h;
+        bl[q] = __float2bfloat16_rn(v - __bfloat162float(h));
     }
 }
 
@@ -344,12 +383,20 @@ struct gd_cmatrix {
     gd_ctx *ctx = nullptr;
     int mode = 0;  // GD_CMATRIX_BF16 or GD_CMATRIX_BF16X3
     int ns = 0, ns_k = 0;
-    int tiles = 0;  // BN x BK tiles of one node's block upper triangle
+    int tiles = 0;       // BN x BK tiles of one node's block upper triangle
+    int64_t slots = 0;   // stored (not all-zero) tiles over all nodes
+    int *node_off = nullptr;    // [ns + 1] into list
+    uint32_t *list = nullptr;   // stored tiles per node, n << 16 | k
     __nv_bfloat16 *gh = nullptr, *gl = nullptr;
-    __nv_bfloat16 *fh = nullptr, *fl = nullptr;
+    __nv_bfloat16 *fh = nullptr, *fl = nullptr;  // f as [cell][node] BF16 hi / lo
     int f_cells = 0;
+    __nv_bfloat16 *bh = nullptr, *bl = nullptr;  // loss matrix [node][ns_k] BF16 hi / lo
     int *err = nullptr;
 };
+
+namespace gd {
+int ensure_f(gd_cmatrix *h, int ncells);
+}
 
 extern "C" int gd_cmatrix_create(gd_ctx *ctx, int mode, gd_cmatrix **out)
 {
@@ -372,42 +419,99 @@ extern "C" int gd_cmatrix_create(gd_ctx *ctx, int mode, gd_cmatrix **out)
     for (int n = 0; n < num_n; n++)
         for (int k = 0; k < k_end(n, num_k); k++) tile_nk.push_back(make_int2(n, k));
     h->tiles = (int)tile_nk.size();
-    const size_t elems = (size_t)h->ns * h->tiles * BN * BK;
-    size_t free_b = 0, total_b = 0;
-    GD_CUDA(cudaMemGetInfo(&free_b, &total_b));
-    const size_t need = elems * 2 * (mode == GD_CMATRIX_BF16X3 ? 2 : 1);
-    if (need + ((size_t)1 << 30) > free_b) {
-        delete h;
-        return set_error(GD_ERR_OUT_OF_MEMORY, "collision matrices need " + std::to_string(need >> 20) +
-                                                   " MiB; free device memory is " + std::to_string(free_b >> 20) + " MiB");
-    }
+    const size_t ntri = (size_t)h->ns * h->tiles;  // triangle tiles over all nodes
     float *w = nullptr;
     int2 *d_tiles = nullptr;
+    uint8_t *d_nz = nullptr;
+    int *d_slot = nullptr;
     const size_t na = (size_t)d.hx * d.nx * d.hy * d.hz * d.nyz;
-    cudaError_t e = cudaMalloc(&h->gh, elems * 2);
-    if (e == cudaSuccess && mode == GD_CMATRIX_BF16X3) e = cudaMalloc(&h->gl, elems * 2);
-    if (e == cudaSuccess) e = cudaMalloc(&h->err, sizeof(int));
+    const int64_t work = (int64_t)ntri * BN * (BK / 8);
+    const int blocks = (int)std::min<int64_t>((work + 255) / 256, (int64_t)c.sm_count * 64);
+    int rc = GD_OK;
+    // pass 1: which triangle tiles hold a nonzero entry
+    cudaError_t e = cudaMalloc(&h->err, sizeof(int));
     if (e == cudaSuccess) e = cudaMalloc(&w, na * sizeof(float));
     if (e == cudaSuccess) e = cudaMalloc(&d_tiles, sizeof(int2) * tile_nk.size());
+    if (e == cudaSuccess) e = cudaMalloc(&d_nz, ntri);
+    if (e == cudaSuccess) e = cudaMemset(d_nz, 0, ntri);
     if (e == cudaSuccess)
         e = cudaMemcpy(d_tiles, tile_nk.data(), sizeof(int2) * tile_nk.size(), cudaMemcpyHostToDevice);
-    int rc = GD_OK;
     if (e != cudaSuccess) rc = cuda_error(e, "collision-matrix allocation");
     if (!rc) rc = launch_dense_tables(d, nullptr, w, nullptr);
+    std::vector<uint8_t> nz(ntri);
     if (!rc) {
-        const int64_t work = (int64_t)h->ns * h->tiles * BN * (BK / 8);
-        const int blocks = (int)std::min<int64_t>((work + 255) / 256, (int64_t)c.sm_count * 64);
-        assemble_g_kernel<<<blocks, 256>>>(d, h->tiles, d_tiles, c.d_nodes, w, h->gh, h->gl);
+        assemble_g_kernel<<<blocks, 256>>>(d, h->tiles, d_tiles, c.d_nodes, w, d_nz, nullptr, nullptr, nullptr);
         e = cudaGetLastError();
+        if (e == cudaSuccess) e = cudaMemcpy(nz.data(), d_nz, ntri, cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) rc = cuda_error(e, "collision-matrix tile scan");
+    }
+    // per-node lists of the stored tiles (n-major, k ascending) and their slots
+    std::vector<int> node_off(h->ns + 1, 0), slot_of(ntri, -1);
+    std::vector<uint32_t> list;
+    if (!rc) {
+        for (int i = 0; i < h->ns; i++) {
+            node_off[i] = (int)list.size();
+            for (int t = 0; t < h->tiles; t++)
+                if (nz[(size_t)i * h->tiles + t]) {
+                    slot_of[(size_t)i * h->tiles + t] = (int)list.size();
+                    list.push_back(((uint32_t)tile_nk[t].x << 16) | (uint32_t)tile_nk[t].y);
+                }
+        }
+        node_off[h->ns] = (int)list.size();
+        h->slots = (int64_t)list.size();
+    }
+    const size_t elems = (size_t)h->slots * BN * BK;
+    if (!rc) {
+        size_t free_b = 0, total_b = 0;
+        e = cudaMemGetInfo(&free_b, &total_b);
+        const size_t need = elems * 2 * (mode == GD_CMATRIX_BF16X3 ? 2 : 1);
+        if (e != cudaSuccess)
+            rc = cuda_error(e, "cudaMemGetInfo");
+        else if (need + ((size_t)1 << 30) > free_b)
+            rc = set_error(GD_ERR_OUT_OF_MEMORY, "collision matrices need " + std::to_string(need >> 20) +
+                                                     " MiB; free device memory is " + std::to_string(free_b >> 20) +
+                                                     " MiB");
+    }
+    if (!rc) {
+        e = cudaMalloc(&h->gh, std::max<size_t>(elems, 1) * 2);
+        if (e == cudaSuccess && mode == GD_CMATRIX_BF16X3) e = cudaMalloc(&h->gl, std::max<size_t>(elems, 1) * 2);
+        if (e == cudaSuccess) e = cudaMalloc(&h->node_off, sizeof(int) * node_off.size());
+        if (e == cudaSuccess) e = cudaMalloc(&h->list, sizeof(uint32_t) * std::max<size_t>(list.size(), 1));
+        if (e == cudaSuccess) e = cudaMalloc(&d_slot, sizeof(int) * ntri);
+        if (e == cudaSuccess)
+            e = cudaMemcpy(h->node_off, node_off.data(), sizeof(int) * node_off.size(), cudaMemcpyHostToDevice);
+        if (e == cudaSuccess && !list.empty())
+            e = cudaMemcpy(h->list, list.data(), sizeof(uint32_t) * list.size(), cudaMemcpyHostToDevice);
+        if (e == cudaSuccess) e = cudaMemcpy(d_slot, slot_of.data(), sizeof(int) * ntri, cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) rc = cuda_error(e, "collision-matrix allocation");
+    }
+    // pass 2: the stored tiles, and the loss matrix
+    if (!rc) {
+        assemble_g_kernel<<<blocks, 256>>>(d, h->tiles, d_tiles, c.d_nodes, w, nullptr, d_slot, h->gh, h->gl);
+        e = cudaGetLastError();
+        const size_t nb = (size_t)h->ns * h->ns_k;
+        if (e == cudaSuccess) e = cudaMalloc(&h->bh, nb * 2);
+        if (e == cudaSuccess) e = cudaMalloc(&h->bl, nb * 2);
+        if (e == cudaSuccess) {
+            assemble_b_kernel<<<(int)std::min<size_t>((nb + 255) / 256, (size_t)c.sm_count * 64), 256>>>(
+                d, h->ns_k, c.d_nodes, c.d_b, h->bh, h->bl);
+            e = cudaGetLastError();
+        }
         if (e == cudaSuccess) e = cudaMemset(h->err, 0, sizeof(int));
         if (e == cudaSuccess) e = cudaDeviceSynchronize();
         if (e != cudaSuccess) rc = cuda_error(e, "collision-matrix assembly");
     }
     cudaFree(w);
     cudaFree(d_tiles);
+    cudaFree(d_nz);
+    cudaFree(d_slot);
     if (rc) {
+        cudaFree(h->bh);
+        cudaFree(h->bl);
         cudaFree(h->gh);
         cudaFree(h->gl);
+        cudaFree(h->node_off);
+        cudaFree(h->list);
         cudaFree(h->err);
         delete h;
         return rc;
@@ -419,6 +523,10 @@ extern "C" int gd_cmatrix_create(gd_ctx *ctx, int mode, gd_cmatrix **out)
 extern "C" int gd_cmatrix_destroy(gd_cmatrix *h)
 {
     if (!h) return GD_OK;
+    cudaFree(h->node_off);
+    cudaFree(h->list);
+    cudaFree(h->bh);
+    cudaFree(h->bl);
     cudaFree(h->gh);
     cudaFree(h->gl);
     cudaFree(h->fh);
@@ -435,15 +543,8 @@ extern "C" int gd_cmatrix_gain(gd_cmatrix *h, const float *f, int ncells, int ld
     if (ncells < 1 || ld < ncells) return set_error(GD_ERR_INVALID_ARG, "need 1 <= ncells <= ld");
     cudaStream_t st = (cudaStream_t)stream;
     const bool split = h->mode == GD_CMATRIX_BF16X3;
-    if (h->f_cells < ncells) {
-        cudaFree(h->fh);
-        cudaFree(h->fl);
-        h->fh = h->fl = nullptr;
-        h->f_cells = 0;
-        GD_CUDA(cudaMalloc(&h->fh, (size_t)ncells * h->ns_k * 2));
-        if (split) GD_CUDA(cudaMalloc(&h->fl, (size_t)ncells * h->ns_k * 2));
-        h->f_cells = ncells;
-    }
+    int rc0 = gd::ensure_f(h, ncells);
+    if (rc0) return rc0;
     dim3 cb(32, 8), cg((h->ns_k + 31) / 32, (ncells + 31) / 32);
     convert_f_kernel<<<cg, cb, 0, st>>>(f, h->ns, h->ns_k, ncells, ld, h->fh, split ? h->fl : nullptr);
     GD_CUDA(cudaGetLastError());
@@ -455,19 +556,19 @@ extern "C" int gd_cmatrix_gain(gd_cmatrix *h, const float *f, int ncells, int ld
     const cuuint64_t fdims[2] = {(cuuint64_t)h->ns_k, (cuuint64_t)ncells};
     const cuuint64_t fstr[1] = {(cuuint64_t)h->ns_k * 2};
     const cuuint32_t fbox[2] = {BK, BM};
-    const cuuint64_t gdims[4] = {(cuuint64_t)BK, (cuuint64_t)BN, (cuuint64_t)h->tiles, (cuuint64_t)h->ns};
-    const cuuint64_t gstr[3] = {(cuuint64_t)BK * 2, (cuuint64_t)BN * BK * 2, (cuuint64_t)h->tiles * BN * BK * 2};
-    const cuuint32_t gbox[4] = {BK, BN, 1, 1};
+    const cuuint64_t gdims[3] = {(cuuint64_t)BK, (cuuint64_t)BN, (cuuint64_t)std::max<int64_t>(h->slots, 1)};
+    const cuuint64_t gstr[2] = {(cuuint64_t)BK * 2, (cuuint64_t)BN * BK * 2};
+    const cuuint32_t gbox[3] = {BK, BN, 1};
     if ((rc = encode(enc, &tFh, h->fh, 2, fdims, fstr, fbox))) return rc;
-    if ((rc = encode(enc, &tGh, h->gh, 4, gdims, gstr, gbox))) return rc;
+    if ((rc = encode(enc, &tGh, h->gh, 3, gdims, gstr, gbox))) return rc;
     if (split) {
         if ((rc = encode(enc, &tFl, h->fl, 2, fdims, fstr, fbox))) return rc;
-        if ((rc = encode(enc, &tGl, h->gl, 4, gdims, gstr, gbox))) return rc;
+        if ((rc = encode(enc, &tGl, h->gl, 3, gdims, gstr, gbox))) return rc;
     } else {
         tFl = tFh;
         tGl = tGh;
     }
-    CmParams prm{h->ns, h->ns_k, ncells, ld, f, gain, h->err};
+    CmParams prm{h->ns, h->ns_k, ncells, ld, f, gain, h->err, h->node_off, h->list};
     dim3 grid((ncells + BM - 1) / BM, h->ns);
     const size_t smem = (split ? 2 * 2 * (kTileA + kTileB) : 4 * (kTileA + kTileB)) + 1024;
     if (split) {
@@ -499,6 +600,46 @@ extern "C" int gd_cmatrix_check(gd_cmatrix *h, gd_stream stream)
 }
 
 namespace gd {
+// BF16 hi and lo copies of f for up to ncells cells (grown on demand)
+int ensure_f(gd_cmatrix *h, int ncells)
+{
+    if (h->f_cells >= ncells) return GD_OK;
+    cudaFree(h->fh);
+    cudaFree(h->fl);
+    h->fh = h->fl = nullptr;
+    h->f_cells = 0;
+    GD_CUDA(cudaMalloc(&h->fh, (size_t)ncells * h->ns_k * 2));
+    GD_CUDA(cudaMalloc(&h->fl, (size_t)ncells * h->ns_k * 2));
+    h->f_cells = ncells;
+    return GD_OK;
+}
+
+// nu = B f as three tensor-core GEMMs, B_hi f_hi + B_hi f_lo + B_lo f_hi
+// (the BF16 split keeps ~16 significant bits of both factors).
+int cmatrix_loss(gd_cmatrix *h, const float *f, int ncells, int ld, float *nu, cudaStream_t st)
+{
+    if (!h->bh || (ld & 3) || (reinterpret_cast<uintptr_t>(nu) & 15)) return GD_ERR_UNSUPPORTED;
+    int rc = ensure_f(h, ncells);
+    if (rc) return rc;
+    dim3 cb(32, 8), cg((h->ns_k + 31) / 32, (ncells + 31) / 32);
+    convert_f_kernel<<<cg, cb, 0, st>>>(f, h->ns, h->ns_k, ncells, ld, h->fh, h->fl);
+    GD_CUDA(cudaGetLastError());
+    if ((rc = gemm_bf16_nt_f32(h->bh, h->ns, h->fh, ncells, h->ns_k, nu, ld, false, h->err, st))) return rc;
+    if ((rc = gemm_bf16_nt_f32(h->bh, h->ns, h->fl, ncells, h->ns_k, nu, ld, true, h->err, st))) return rc;
+    return gemm_bf16_nt_f32(h->bl, h->ns, h->fh, ncells, h->ns_k, nu, ld, true, h->err, st);
+}
+
+int64_t cmatrix_stored_tiles(const gd_cmatrix *cm) { return cm ? cm->slots : 0; }
+
+int run_loss_path(Context &c, const float *f, int ncells, int ld, float *nu, cudaStream_t st)
+{
+    if (c.gain_path != GD_GAIN_PAIR && c.cmatrix) {
+        const int rc = cmatrix_loss(c.cmatrix, f, ncells, ld, nu, st);
+        if (rc != GD_ERR_UNSUPPORTED) return rc;
+    }
+    return run_loss(c, f, ncells, ld, nu, st);
+}
+
 int run_gain_path(Context &c, const float *f, int ncells, int ld, float *gain, cudaStream_t st)
 {
     if (c.gain_path == GD_GAIN_PAIR || !c.cmatrix) return run_gain(c, f, ncells, ld, gain, st);

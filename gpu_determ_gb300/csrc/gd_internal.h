@@ -155,6 +155,20 @@ int launch_gain_pair(Context &c, const float *f, int ncells, int ld, float *gain
 // scratch -------------------------------------------------------------------
 int ensure_scratch(Context &c, size_t bytes);
 
+// tensor-core GEMM (gd_mlp.cu): C[M][N] = (accumulate ? C : 0) + A B^T, A [M][K]
+// and B [N][K] K-major BF16 (K a multiple of 64), C FP32 with ldc % 4 == 0 and
+// 16-byte aligned rows.
+int gemm_bf16_nt_f32(const void *A, int M, const void *B, int N, int K, float *C, int ldc, bool accumulate, int *err,
+                     cudaStream_t st);
+// loss on the tensor cores when the context uses collision matrices
+// (gd_cmatrix.cu); GD_ERR_UNSUPPORTED when the layout does not allow it.
+int cmatrix_loss(gd_cmatrix *cm, const float *f, int ncells, int ld, float *nu, cudaStream_t st);
+// loss for the context's gain path: tensor cores with collision matrices (when
+// the layout allows), else the FP32 kernel
+int run_loss_path(Context &c, const float *f, int ncells, int ld, float *nu, cudaStream_t st);
+// stored tiles of a context's collision matrices (0 for NULL)
+int64_t cmatrix_stored_tiles(const gd_cmatrix *cm);
+
 }  // namespace gd
 
 // the opaque handle of the C ABI

@@ -480,6 +480,23 @@ int transpose(const bf16 *in, int R, int Cc, int ldi, bf16 *out, int ldo, cudaSt
 int pad64(int n) { return (n + 63) / 64 * 64; }
 
 }  // namespace
+
+// C[M][N] (FP32, row stride ldc) = (accumulate ? C : 0) + A B^T for K-major BF16
+// A [M][K] and B [N][K]; the collision-matrix path computes the loss with it.
+int gemm_bf16_nt_f32(const void *A, int M, const void *B, int N, int K, float *C, int ldc, bool accumulate, int *err,
+                     cudaStream_t st)
+{
+    GemmArgs a{};
+    a.M = M;
+    a.N = N;
+    a.K = K;
+    a.err = err;
+    a.c32 = C;
+    a.ld32 = ldc;
+    a.add = accumulate ? C : nullptr;
+    return gemm_nt(EPI_NONE, static_cast<const bf16 *>(A), static_cast<const bf16 *>(B), a, st);
+}
+
 }  // namespace gd
 
 using gd::bf16;

@@ -61,6 +61,7 @@ typedef struct {
     int64_t pair_products;     /* (s, n) pair products formed per cell-eval */
     int64_t contraction_terms; /* nonzero-weight x pair-product terms per cell-eval */
     int64_t scatter_terms;     /* (s, g, sign) output updates per cell-eval */
+    int64_t cmatrix_tiles;     /* stored 256 x 64 tiles of the collision matrices (0 without) */
 } gd_info;
 
 /* Library version (major*10000 + minor*100 + patch). */

@@ -62,3 +62,38 @@ def test_step_with_cmatrix_gain_path(cuda, gdlib, path, tol):
     rel = np.linalg.norm(qh - q64) / np.linalg.norm(q64)
     print(f"gain path {path}: Q relative L2 vs FP64 oracle = {rel:.3e}")
     assert rel <= tol
+
+
+@pytest.mark.parametrize("n,R,ncells,ld", [(12, 4.8, 300, 300), (12, 4.8, 100, 103), (16, 4.8, 64, 64)])
+def test_tensor_core_loss(cuda, gdlib, n, R, ncells, ld):
+    """With collision matrices selected, nu = B f runs as three BF16 GEMMs
+    (hi/lo split).  The tensor cores' FP32 accumulation leaves nu slightly low
+    (mean relative bias ~8e-6 at 16^3, growing with the node count), so the
+    bound is 4e-5 per node and cell (the FP32 kernel meets 1e-5) and 2e-5 on
+    the mean; the FP64 projection restores exact conservation either way.  A
+    leading dimension that is not a multiple of 4 falls back to the FP32 kernel
+    (bitwise equal to the pair path's nu)."""
+    torch = cuda
+    spec = gdlib.GridSpec(n, R=R)
+    ctx = gdlib.Context(spec)
+    f = inputs.mixtures(spec.fill(), ncells, seed=n + 11)
+    ft = torch.zeros((ctx.n_pnt, ld), dtype=torch.float32, device="cuda")
+    ft[:, :ncells] = torch.from_numpy(f).cuda()
+    o = Oracle(n, R=R)
+    ref = o.loss_f64(o.to_box(f))
+    nu_pair = torch.zeros_like(ft)
+    ctx.collision(ft, ncells, ld, nu_pair, None)
+    ctx.set_gain_path(gdlib.GAIN_CMATRIX_BF16)
+    nu = torch.full_like(ft, -1.0)
+    ctx.collision(ft, ncells, ld, nu, None)
+    nu2 = torch.full_like(ft, -1.0)
+    ctx.collision(ft, ncells, ld, nu2, None)
+    torch.cuda.synchronize()
+    got = nu.cpu().numpy()
+    assert np.array_equal(got, nu2.cpu().numpy())
+    assert np.all(got[:, ncells:] == -1.0)
+    rel = (got[:, :ncells] - ref) / ref
+    assert np.max(np.abs(rel)) < 4e-5
+    assert abs(np.mean(rel)) < 2e-5
+    if ld % 4:
+        assert np.array_equal(got[:, :ncells], nu_pair.cpu().numpy()[:, :ncells])
