@@ -283,7 +283,10 @@ def run_ours(args):
     roof = gain_roofline(args.gain, ctx, f0, nc, stream, flush, peak, peak_kind, max(2, args.steps))
 
     dtype = {"pair": "f32", "bf16": "bf16 (FP32 accumulate)", "bf16x3": "bf16x3 (FP32 accumulate)"}[args.gain]
-    plain_launches = 7 if args.gain == "pair" else 6
+    # per plain step: pair path = loss, gain, chunk reduction, projection, max, dt,
+    # relax (7); collision matrices = f conversion + 3 loss GEMMs, f conversion +
+    # gain, projection, max, dt, relax (10)
+    plain_launches = 7 if args.gain == "pair" else 10
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None,
@@ -297,9 +300,10 @@ def run_ours(args):
     if model is None:
         line["gpu_launches"] = plain_launches * args.steps
     else:
-        # loss 1, network 8, nu f 1, error network 8, selection 1, projection 1,
-        # relaxation 3; with fallback cells also gather 1, plain gain 2, scatter 1
-        line["gpu_launches"] = sum(23 + (4 if k > 0 else 0) for k in fb_timed)
+        # loss 4 (f conversion + 3 GEMMs), network 8, nu f 1, error network 8,
+        # selection 1, projection 1, relaxation 3; with fallback cells also
+        # gather 1, plain gain 2 (f conversion + matrices), scatter 1
+        line["gpu_launches"] = sum(26 + (4 if k > 0 else 0) for k in fb_timed)
         rep = surrogate_report(args, gd, ctx, model, f0, nc, stream, fit_s, fb_timed, plain_value)
         rep["speedup_vs_plain"] = value / plain_value
         line["accuracy"] = next(c for c in rep["tolerance_curve"] if c["tol"] == args.tol)

@@ -67,21 +67,6 @@ int enqueue_steps(gd_batch *b)
     return GD_OK;
 }
 
-struct DeviceScope {
-    int prev = -1;
-    explicit DeviceScope(int dev)
-    {
-        cudaGetDevice(&prev);
-        if (prev != dev) cudaSetDevice(dev);
-    }
-    ~DeviceScope()
-    {
-        int cur = -1;
-        cudaGetDevice(&cur);
-        if (prev >= 0 && cur != prev) cudaSetDevice(prev);
-    }
-};
-
 }  // namespace
 
 extern "C" int gd_batch_create(gd_batch **out)
@@ -105,7 +90,7 @@ extern "C" int gd_batch_create(gd_batch **out)
 extern "C" int gd_batch_destroy(gd_batch *b)
 {
     if (!b) return GD_OK;
-    DeviceScope ds(b->device);
+    gd::DeviceGuard ds(b->device);
     cudaStreamSynchronize(b->main);
     drop_graph(b);
     for (cudaStream_t s : b->streams) cudaStreamDestroy(s);
@@ -126,7 +111,7 @@ extern "C" int gd_batch_add(gd_batch *b, gd_ctx *ctx, float *f, int ncells, int 
     if (mode != GD_DT_COURANT && mode != GD_DT_FIXED) return set_error(GD_ERR_INVALID_ARG, "unknown dt mode");
     if (!(param > 0.f) || !std::isfinite(param)) return set_error(GD_ERR_INVALID_ARG, "dt parameter must be > 0");
     if (ctx->c.device != b->device) return set_error(GD_ERR_INVALID_ARG, "context on another device");
-    DeviceScope ds(b->device);
+    gd::DeviceGuard ds(b->device);
     int slot = -1;
     for (size_t s = 0; s < b->slot_ctx.size(); s++)
         if (b->slot_ctx[s] == ctx) slot = (int)s;
@@ -153,7 +138,7 @@ extern "C" int gd_batch_step(gd_batch *b, int use_graph, gd_stream stream)
     using namespace gd;
     if (!b) return set_error(GD_ERR_INVALID_ARG, "NULL argument");
     if (b->groups.empty()) return set_error(GD_ERR_INVALID_ARG, "empty batch");
-    DeviceScope ds(b->device);
+    gd::DeviceGuard ds(b->device);
     cudaStream_t user = (cudaStream_t)stream;
     // order after the caller's stream, and the caller's stream after the step
     GD_CUDA(cudaEventRecord(b->joined, user));
@@ -193,7 +178,7 @@ extern "C" int gd_batch_check(gd_batch *b)
 {
     using namespace gd;
     if (!b) return set_error(GD_ERR_INVALID_ARG, "NULL argument");
-    DeviceScope ds(b->device);
+    gd::DeviceGuard ds(b->device);
     GD_CUDA(cudaStreamSynchronize(b->main));
     for (gd_ctx *c : b->slot_ctx)
         if (c->c.cmatrix) {
@@ -235,7 +220,7 @@ extern "C" int gd_ctx_autotune(gd_ctx *ctx, const float *f, int ncells, int ld, 
     if (ncells < 1 || ld < ncells) return set_error(GD_ERR_INVALID_ARG, "need 1 <= ncells <= ld");
     if (!(path_mask & 7)) return set_error(GD_ERR_INVALID_ARG, "path_mask admits no gain path");
     Context &c = ctx->c;
-    DeviceScope ds(c.device);
+    gd::DeviceGuard ds(c.device);
     cudaStream_t st = (cudaStream_t)stream;
     std::memset(res, 0, sizeof(*res));
     struct Cand {

@@ -17,23 +17,6 @@ namespace gd {
 namespace {
 thread_local std::string g_last_error;
 
-// Makes the context's device current for the duration of a call and restores
-// the caller's device afterwards.
-struct DeviceGuard {
-    int prev = -1;
-    bool ok = true;
-    explicit DeviceGuard(int dev)
-    {
-        if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
-        if (prev != dev) ok = cudaSetDevice(dev) == cudaSuccess;
-    }
-    ~DeviceGuard()
-    {
-        int cur = -1;
-        if (prev >= 0 && cudaGetDevice(&cur) == cudaSuccess && cur != prev) cudaSetDevice(prev);
-    }
-};
-
 int check_spec(const gd_grid_spec *s)
 {
     if (!s) return set_error(GD_ERR_INVALID_ARG, "grid spec is NULL");

@@ -192,32 +192,40 @@ __global__ void __launch_bounds__(kThreads, 1)
         const bool live = cell < p.ncells;
         float sum = 0.f;
         const int l0 = __ldg(p.node_off + node), cnt = __ldg(p.node_off + node + 1) - l0;
+        // f[b][cell] for 32 consecutive b; rows b >= ns of G are zero, so T[b] = 0
+        // there and clamping b keeps every load in bounds without a branch
+        const float *fcell = p.f + (live ? cell : 0);
+        float fv[32], fn[32];
+        auto load_f = [&](float *dst, int b0) {
+#pragma unroll
+            for (int j = 0; j < 32; j++) dst[j] = __ldg(fcell + (size_t)min(b0 + j, p.ns - 1) * p.ld);
+        };
         for (int it = 0, grp = 0; it < cnt; grp++) {
             // b-tiles without stored tiles contribute nothing and are skipped
             const int n = (int)(__ldg(p.tiles + l0 + it) >> 16);
             while (it < cnt && (int)(__ldg(p.tiles + l0 + it) >> 16) == n) it++;
             const int buf = grp & 1;
             const uint32_t use = (uint32_t)(grp >> 1);
+            // the first chunk's f loads overlap the wait for the accumulator
+            if (live) load_f(fv, n * BN);
             bool ok = true;
             if (lane == 0) ok = mbar_wait(smem_u32(&accf_bar[buf]), use & 1u, p.err);
             ok = __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
             if (!ok) break;
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
             const uint32_t taddr = tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(buf * BN);
+#pragma unroll
             for (int c0 = 0; c0 < BN; c0 += 32) {
                 float v[32];
                 tmem_ld32(taddr + (uint32_t)c0, v);
-                const int b0 = n * BN + c0;
+                // next chunk's loads are in flight during this chunk's FMAs
+                if (live && c0 + 32 < BN) load_f(fn, n * BN + c0 + 32);
                 if (live) {
-                    // rows b >= ns of G are zero, so T[b] = 0 there: clamping b keeps
-                    // every load in bounds without a branch, and the 32 independent
-                    // loads issue back to back instead of one L2 latency each
-                    float fv[32];
-#pragma unroll
-                    for (int j = 0; j < 32; j++) fv[j] = __ldg(p.f + (size_t)min(b0 + j, p.ns - 1) * p.ld + cell);
 #pragma unroll
                     for (int j = 0; j < 32; j++) sum = __fmaf_rn(v[j], fv[j], sum);
                 }
+#pragma unroll
+                for (int j = 0; j < 32; j++) fv[j] = fn[j];
             }
             asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
             __syncwarp();

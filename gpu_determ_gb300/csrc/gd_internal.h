@@ -105,6 +105,23 @@ struct Context {
     int sm_count = 0;
 };
 
+// Makes an object's device current for the duration of a call and restores
+// the caller's device afterwards.
+struct DeviceGuard {
+    int prev = -1;
+    bool ok = true;
+    explicit DeviceGuard(int dev)
+    {
+        if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+        if (prev != dev) ok = cudaSetDevice(dev) == cudaSuccess;
+    }
+    ~DeviceGuard()
+    {
+        int cur = -1;
+        if (prev >= 0 && cudaGetDevice(&cur) == cudaSuccess && cur != prev) cudaSetDevice(prev);
+    }
+};
+
 // error state -------------------------------------------------------------
 int set_error(int code, const std::string &msg);
 int cuda_error(cudaError_t e, const char *what);

@@ -708,21 +708,6 @@ int check_err(gd_mlp *h, cudaStream_t st)
     return GD_OK;
 }
 
-struct DeviceScope {
-    int prev = -1;
-    explicit DeviceScope(int dev)
-    {
-        cudaGetDevice(&prev);
-        if (prev != dev) cudaSetDevice(dev);
-    }
-    ~DeviceScope()
-    {
-        int cur = -1;
-        cudaGetDevice(&cur);
-        if (prev >= 0 && cur != prev) cudaSetDevice(prev);
-    }
-};
-
 }  // namespace
 
 extern "C" int gd_mlp_create(int n_in, int n_out, int batch_cap, int flags, uint64_t seed, gd_mlp **out)
@@ -836,7 +821,7 @@ extern "C" int gd_mlp_set_io_scale(gd_mlp *h, float in_gain, float out_gain)
 extern "C" int gd_mlp_destroy(gd_mlp *h)
 {
     if (!h) return GD_OK;
-    DeviceScope ds(h->device);
+    gd::DeviceGuard ds(h->device);
     for (void *p : h->allocs) cudaFree(p);
     delete h;
     return GD_OK;
@@ -870,7 +855,7 @@ extern "C" int gd_mlp_forward(gd_mlp *h, const float *x, int ldx, int batch, flo
     using namespace gd;
     if (!h || !x || !y || batch < 1 || batch > h->cap || ldx < batch || ldy < batch)
         return set_error(GD_ERR_INVALID_ARG, "bad surrogate forward arguments (1 <= batch <= cap, ld >= batch)");
-    DeviceScope ds(h->device);
+    gd::DeviceGuard ds(h->device);
     cudaStream_t st = (cudaStream_t)stream;
     int rc = load_input(h, x, ldx, batch, st);
     if (!rc) rc = forward(h, batch, st);
@@ -889,7 +874,7 @@ extern "C" int gd_mlp_train_step(gd_mlp *h, const float *x, int ldx, const float
     if (!h || !x || !t || batch < 64 || batch > h->cap || batch % 64 || ldx < batch || ldt < batch ||
         (tden && ldd < batch))
         return set_error(GD_ERR_INVALID_ARG, "bad surrogate training arguments (batch a multiple of 64, <= cap)");
-    DeviceScope ds(h->device);
+    gd::DeviceGuard ds(h->device);
     cudaStream_t st = (cudaStream_t)stream;
     int rc = load_input(h, x, ldx, batch, st);
     if (!rc) rc = forward(h, batch, st);
@@ -923,7 +908,7 @@ extern "C" int gd_mlp_loss(gd_mlp *h, const float *x, int ldx, const float *t, i
     if (!h || !x || !t || !row_loss || batch < 1 || batch > h->cap || ldx < batch || ldt < batch ||
         (tden && ldd < batch))
         return set_error(GD_ERR_INVALID_ARG, "bad surrogate loss arguments");
-    DeviceScope ds(h->device);
+    gd::DeviceGuard ds(h->device);
     cudaStream_t st = (cudaStream_t)stream;
     int rc = load_input(h, x, ldx, batch, st);
     if (!rc) rc = forward(h, batch, st);
@@ -936,7 +921,7 @@ extern "C" int gd_mlp_loss(gd_mlp *h, const float *x, int ldx, const float *t, i
 extern "C" int gd_mlp_check(gd_mlp *h, gd_stream stream)
 {
     if (!h) return gd::set_error(GD_ERR_INVALID_ARG, "NULL argument");
-    DeviceScope ds(h->device);
+    gd::DeviceGuard ds(h->device);
     return check_err(h, (cudaStream_t)stream);
 }
 
@@ -944,7 +929,7 @@ extern "C" int gd_mlp_check(gd_mlp *h, gd_stream stream)
 // with n_in and n_out padded to multiples of 64 (padding entries are zero).
 static int copy_params(gd_mlp *h, float *host, bool to_host, bool grads)
 {
-    DeviceScope ds(h->device);
+    gd::DeviceGuard ds(h->device);
     size_t off = 0;
     for (int k = 0; k < 5; k++) {
         gd_mlp::Layer &l = h->L[k];
@@ -973,7 +958,7 @@ extern "C" int gd_mlp_set_params(gd_mlp *h, const float *host)
     if (!h || !host) return gd::set_error(GD_ERR_INVALID_ARG, "NULL argument");
     int rc = copy_params(h, const_cast<float *>(host), false, false);
     if (rc) return rc;
-    DeviceScope ds(h->device);
+    gd::DeviceGuard ds(h->device);
     if ((rc = refresh_bf16(h, nullptr))) return rc;
     if (cudaDeviceSynchronize() != cudaSuccess) return gd::set_error(GD_ERR_CUDA, "surrogate parameter refresh");
     return GD_OK;

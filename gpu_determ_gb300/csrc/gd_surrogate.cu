@@ -122,24 +122,9 @@ struct gd_surrogate {
 
 namespace {
 
-struct DeviceScope {
-    int prev = -1;
-    explicit DeviceScope(int dev)
-    {
-        cudaGetDevice(&prev);
-        if (prev != dev) cudaSetDevice(dev);
-    }
-    ~DeviceScope()
-    {
-        int cur = -1;
-        cudaGetDevice(&cur);
-        if (prev >= 0 && cur != prev) cudaSetDevice(prev);
-    }
-};
-
 void free_surrogate(gd_surrogate *s)
 {
-    DeviceScope ds(s->device);
+    gd::DeviceGuard ds(s->device);
     cudaFree(s->est_buf);
     cudaFree(s->fs);
     cudaFree(s->gs);
@@ -204,7 +189,7 @@ extern "C" int gd_surrogate_gain(gd_surrogate *s, const float *f, int ncells, in
     if (ncells < 1 || ncells > s->cap || ld < ncells)
         return set_error(GD_ERR_INVALID_ARG, "need 1 <= ncells <= max_cells and ld >= ncells");
     if (std::isnan(tol)) return set_error(GD_ERR_INVALID_ARG, "tolerance is NaN");
-    DeviceScope ds(s->device);
+    gd::DeviceGuard ds(s->device);
     cudaStream_t st = (cudaStream_t)stream;
     int rc;
     if (tol <= 0.f) {  // the plain method for every cell
