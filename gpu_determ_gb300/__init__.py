@@ -101,6 +101,8 @@ def lib():
     L.gd_relax.argtypes = [vp, vp, vp, vp, i, i, i, f, vp, vp, vp]
     L.gd_step.argtypes = [vp, vp, i, i, i, f, vp, vp, vp, vp, vp, vp, vp]
     L.gd_moments.argtypes = [vp, vp, i, i, vp, vp]
+    L.gd_ctx_check.argtypes = [vp, vp]
+    L.gd_set_memory_limit.argtypes = [C.c_size_t]
     L.gd_gain_noalloc.argtypes = [vp, vp, i, i, vp, vp]
     L.gd_load_options.argtypes = [C.c_char_p, P(_Options)]
     L.gd_cmatrix_create.argtypes = [vp, i, P(vp)]
@@ -134,7 +136,7 @@ def lib():
     L.gd_ctx_autotune.argtypes = [vp, vp, i, i, i, C.c_double, P(_Autotune), vp]
     for name in ("gd_grid_count", "gd_grid_fill", "gd_ctx_create", "gd_ctx_destroy", "gd_ctx_info",
                  "gd_export_tables", "gd_correction_basis", "gd_collision", "gd_project",
-                 "gd_relax", "gd_step", "gd_moments", "gd_gain_noalloc",
+                 "gd_relax", "gd_step", "gd_moments", "gd_ctx_check", "gd_set_memory_limit", "gd_gain_noalloc",
                  "gd_box_to_compact", "gd_compact_to_box", "gd_load_options", "gd_cmatrix_create",
                  "gd_cmatrix_gain", "gd_cmatrix_destroy", "gd_ctx_set_gain_path",
                  "gd_mlp_create", "gd_mlp_destroy", "gd_mlp_set_io_scale", "gd_mlp_info", "gd_mlp_forward", "gd_mlp_train_step",
@@ -167,6 +169,11 @@ def _stream(s):
     if isinstance(s, int):
         return s
     return s.cuda_stream
+
+
+def set_memory_limit(nbytes: int):
+    """Cap the large device allocations of one object (0 = no cap)."""
+    _check(lib().gd_set_memory_limit(int(nbytes)))
 
 
 def load_options(path: str) -> dict:
@@ -281,6 +288,10 @@ class Context:
     def compact_to_box(self, compact, ncells, ld, box, ld_box, stream=None):
         _check(lib().gd_compact_to_box(self._h, _ptr(compact), int(ncells), int(ld), _ptr(box), int(ld_box),
                                        _stream(stream)))
+
+    def check(self, stream=None):
+        """Raise GDError when a projection met non-finite data or a singular system."""
+        _check(lib().gd_ctx_check(self._h, _stream(stream)))
 
     def moments(self, f, ncells, ld, m5, stream=None):
         _check(lib().gd_moments(self._h, _ptr(f), int(ncells), int(ld), _ptr(m5), _stream(stream)))

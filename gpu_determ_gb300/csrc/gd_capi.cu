@@ -2,6 +2,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -16,6 +17,7 @@ namespace gd {
 
 namespace {
 thread_local std::string g_last_error;
+std::atomic<size_t> g_memory_limit{0};
 
 int check_spec(const gd_grid_spec *s)
 {
@@ -119,6 +121,8 @@ int build_s_schedule(Context &c, const std::vector<int> &gid_of_gbox)
 }
 
 }  // namespace
+
+size_t memory_limit() { return g_memory_limit.load(); }
 
 // Group the per-|g| weight rows: rows with the same parity class and
 // byte-identical (offset, weight) entries are one group.  Groups are ordered
@@ -250,6 +254,7 @@ static void destroy_context(Context &c)
     for (auto &kv : c.s_bounds_dev) cudaFree(kv.second);
     c.s_bounds_dev.clear();
     cudaFree(c.d_reduce);
+    cudaFree(c.d_status);
     cudaFree(c.scratch.ptr);
     cudaFree(c.step_buf.ptr);
 }
@@ -319,6 +324,11 @@ static int create_context(Context &c, const gd_grid_spec &spec, int device)
     GD_CUDA(cudaMalloc(&c.d_phi, sizeof(double) * 5 * d.n_pnt));
     GD_CUDA(cudaMalloc(&c.d_b, sizeof(float) * d.nxyz));
     GD_CUDA(cudaMalloc(&c.d_reduce, sizeof(float) * 512));
+    GD_CUDA(cudaMalloc(&c.d_status, sizeof(unsigned int) * 2));
+    {
+        const unsigned int clear[2] = {0u, 0xffffffffu};
+        GD_CUDA(cudaMemcpy(c.d_status, clear, sizeof(clear), cudaMemcpyHostToDevice));
+    }
     GD_CUDA(cudaMemcpy(c.d_cmap, cmap16.data(), sizeof(int16_t) * d.nxyz, cudaMemcpyHostToDevice));
     GD_CUDA(cudaMemcpy(c.d_nodes, nodes.data(), sizeof(uint32_t) * d.n_pnt, cudaMemcpyHostToDevice));
     GD_CUDA(cudaMemcpy(c.d_phi, phi.data(), sizeof(double) * 5 * d.n_pnt, cudaMemcpyHostToDevice));
@@ -542,6 +552,34 @@ int gd_step(gd_ctx *ctx, float *f, int ncells, int ld, int mode, float param, fl
     if (!rc) rc = gd::run_project(c, f, nu_b, gain_b, ncells, ld, nu_b, q_b, nullptr, 0, 0.f, nullptr, m5, st);
     if (!rc) rc = gd::run_relax_q(c, f, nu_b, gain_b, q_b, ncells, ld, mode, param, time_dev, dt_dev, st);
     return rc;
+}
+
+int gd_set_memory_limit(size_t bytes)
+{
+    gd::g_memory_limit.store(bytes);
+    return GD_OK;
+}
+
+int gd_ctx_check(gd_ctx *ctx, gd_stream stream)
+{
+    if (!ctx) return set_error(GD_ERR_INVALID_ARG, "context is NULL");
+    gd::DeviceGuard g(ctx->c.device);
+    gd::Context &c = ctx->c;
+    cudaStream_t st = (cudaStream_t)stream;
+    unsigned int h[2] = {0u, 0u};
+    GD_CUDA(cudaMemcpyAsync(h, c.d_status, sizeof(h), cudaMemcpyDeviceToHost, st));
+    GD_CUDA(cudaStreamSynchronize(st));
+    if (c.cmatrix) {
+        const int rc = gd_cmatrix_check(c.cmatrix, stream);
+        if (rc) return rc;
+    }
+    if (!h[0]) return GD_OK;
+    const unsigned int clear[2] = {0u, 0xffffffffu};
+    GD_CUDA(cudaMemcpy(c.d_status, clear, sizeof(clear), cudaMemcpyHostToDevice));
+    return set_error(GD_ERR_SINGULAR,
+                     std::string(h[0] & 1u ? "non-finite distribution, frequency or gain"
+                                           : "singular conservation system") +
+                         " in the projection (first affected cell " + std::to_string(h[1]) + ")");
 }
 
 int gd_moments(gd_ctx *ctx, const float *f, int ncells, int ld, double *m5, gd_stream stream)

@@ -473,8 +473,13 @@ extern "C" int gd_cmatrix_create(gd_ctx *ctx, int mode, gd_cmatrix **out)
         size_t free_b = 0, total_b = 0;
         e = cudaMemGetInfo(&free_b, &total_b);
         const size_t need = elems * 2 * (mode == GD_CMATRIX_BF16X3 ? 2 : 1);
+        const size_t limit = memory_limit();
         if (e != cudaSuccess)
             rc = cuda_error(e, "cudaMemGetInfo");
+        else if (limit && need > limit)
+            rc = set_error(GD_ERR_OUT_OF_MEMORY, "collision matrices need " + std::to_string(need >> 20) +
+                                                     " MiB; the library's memory limit is " +
+                                                     std::to_string(limit >> 20) + " MiB");
         else if (need + ((size_t)1 << 30) > free_b)
             rc = set_error(GD_ERR_OUT_OF_MEMORY, "collision matrices need " + std::to_string(need >> 20) +
                                                      " MiB; free device memory is " + std::to_string(free_b >> 20) +

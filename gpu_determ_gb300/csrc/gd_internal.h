@@ -102,6 +102,7 @@ struct Context {
     std::map<int, int *> s_bounds_dev;
     int gain_waves = 2;         // gain launch: at least this many CTAs per SM (autotuned)
     float *d_reduce = nullptr;  // small device scalars (max nu, dt)
+    unsigned int *d_status = nullptr;  // numeric status of projections: flags, first failing cell
     int sm_count = 0;
 };
 
@@ -121,6 +122,10 @@ struct DeviceGuard {
         if (prev >= 0 && cudaGetDevice(&cur) == cudaSuccess && cur != prev) cudaSetDevice(prev);
     }
 };
+
+// Limit on the large device allocations of one object (collision matrices,
+// surrogate network), 0 = only the free device memory (gd_set_memory_limit).
+size_t memory_limit();
 
 // error state -------------------------------------------------------------
 int set_error(int code, const std::string &msg);

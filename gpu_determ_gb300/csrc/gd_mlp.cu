@@ -721,6 +721,15 @@ extern "C" int gd_mlp_create(int n_in, int n_out, int batch_cap, int flags, uint
                          "need 1 <= n_in, n_out <= 65536, batch_cap a positive multiple of 64 and known flags");
     if ((flags & GD_MLP_SCALE_OUTPUT) && !(flags & GD_MLP_SCALE_INPUT))
         return set_error(GD_ERR_INVALID_ARG, "GD_MLP_SCALE_OUTPUT needs GD_MLP_SCALE_INPUT");
+    {
+        // parameters (FP32 master, gradient, two Adam moments, BF16 copy and
+        // transpose) and activations, for the memory limit
+        const double np = 256.0 * pad64(n_in) + 512.0 * 256 + 512.0 * 512 + 256.0 * 512 + 256.0 * pad64(n_out);
+        const double acts = (double)batch_cap * (6.0 * pad64(n_in) + 14.0 * pad64(n_out) + 12000.0);
+        const size_t limit = memory_limit();
+        if (limit && np * 20.0 + acts > (double)limit)
+            return set_error(GD_ERR_OUT_OF_MEMORY, "the surrogate network exceeds the library's memory limit");
+    }
     gd_mlp *h = new gd_mlp();
     h->n_in = n_in;
     h->n_out = n_out;

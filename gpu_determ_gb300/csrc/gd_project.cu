@@ -31,6 +31,7 @@ struct ProjArgs {
     float dt;
     float *f_out;
     double *m5;
+    unsigned int *status;  // [0] flags (1 non-finite sums, 2 singular system), [1] first cell
 };
 
 // Gaussian elimination with partial pivoting on a symmetric 5x5 system.
@@ -120,8 +121,19 @@ __global__ void __launch_bounds__(kWarps * 32) project_kernel(ProjArgs a)
                 A[l][k] = tot[t];
                 t++;
             }
-        if (!solve5(A, B, X))
+        bool finite = true;
+#pragma unroll
+        for (int k = 0; k < kSums; k++) finite = finite && isfinite(tot[k]);
+        const bool solved = finite && solve5(A, B, X);
+        if (!solved) {
             for (int k = 0; k < 5; k++) X[k] = 0.;
+            // recorded for gd_ctx_check: the flags OR together, the smallest
+            // failing cell wins, so the record does not depend on scheduling
+            if (live && a.status && (!finite || tot[20] != 0.0)) {  // an empty cell has nothing to correct
+                atomicOr(a.status, finite ? 2u : 1u);
+                atomicMin(a.status + 1, (unsigned int)cell);
+            }
+        }
         for (int k = 0; k < 5; k++) xs[k][lane] = X[k];
         if (live) {
             if (a.x)
@@ -257,7 +269,8 @@ int run_project(Context &c, const float *f, const float *nu, const float *gain, 
                 float *nu_corr, double *q, double *x, int fixed_dt_mode, float dt, float *f_out,
                 double *m5, cudaStream_t st)
 {
-    ProjArgs a{c.d, f, nu, gain, ld, ncells, c.d_phi, nu_corr, q, x, fixed_dt_mode ? 1 : 0, dt, f_out, m5};
+    ProjArgs a{c.d, f, nu, gain, ld, ncells, c.d_phi, nu_corr, q, x, fixed_dt_mode ? 1 : 0, dt, f_out, m5,
+               c.d_status};
     project_kernel<<<(ncells + 31) / 32, kWarps * 32, 0, st>>>(a);
     GD_CUDA(cudaGetLastError());
     return GD_OK;

@@ -90,6 +90,12 @@ typedef struct {
 } gd_options;
 int gd_load_options(const char *path, gd_options *out);
 
+/* Caps the large device allocations of one object (collision matrices,
+ * surrogate network) at `bytes` (0, the default: only the free device memory
+ * limits them); creation beyond the cap fails with GD_ERR_OUT_OF_MEMORY and
+ * changes nothing.  Process-wide. */
+int gd_set_memory_limit(size_t bytes);
+
 /* ---- context ----------------------------------------------------------- */
 /* Binds to `device`, uploads the grid and builds the weight tables on the GPU
  * (FP64 analytic builder, compacted to nonzero entries).  Replaces the
@@ -147,6 +153,13 @@ int gd_step(gd_ctx *ctx, float *f, int ncells, int ld, int mode, float param, fl
  * m5[5*ncells] on the device.  Restates print_moments (determ.cu:123-144)
  * per cell. */
 int gd_moments(gd_ctx *ctx, const float *f, int ncells, int ld, double *m5, gd_stream stream);
+/* Numeric health of the context's work since the last check: synchronises
+ * the stream and returns GD_ERR_SINGULAR when a projection met a cell with
+ * non-finite f, nu or gain sums or a singular 5x5 system (that cell's
+ * frequency was left uncorrected; the message names the first such cell),
+ * or the error of a timed-out tensor-core pipeline wait; clears the record.
+ * The collision, projection and step calls themselves never synchronise. */
+int gd_ctx_check(gd_ctx *ctx, gd_stream stream);
 
 /* ---- collision-matrix path (tensor cores) ------------------------------ */
 /* The gain as the bilinear form I_i = sum_ab G_i[a][b] f_a f_b with the dense

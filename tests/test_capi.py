@@ -85,6 +85,14 @@ def test_null_arguments_rejected(gdlib):
     assert L.gd_batch_step(None, 1, None) == 1
     assert L.gd_ctx_autotune(None, None, 1, 1, 1, 0.0, None, None) == 1
     assert L.gd_mlp_destroy(None) == 0 and L.gd_surrogate_destroy(None) == 0 and L.gd_batch_destroy(None) == 0
+    assert L.gd_ctx_check(None, None) == 1
+    # a memory cap refuses the surrogate network before any CUDA call
+    try:
+        assert L.gd_set_memory_limit(1 << 20) == 0
+        assert L.gd_mlp_create(3648, 3648, 4096, 3, 0, C.byref(out)) == 3
+        assert b"memory limit" in L.gd_last_error()
+    finally:
+        L.gd_set_memory_limit(0)
 
 
 def test_missing_library_fails_loudly(gdlib, monkeypatch):
