@@ -25,7 +25,7 @@ from . import DT_COURANT, GAIN_CMATRIX_BF16X3, GAIN_PAIR, Batch, Context, GridSp
 
 
 def build(cells: int = 4096, grids=(12, 16, 20, 24), radius: float = 4.8, mach: float = 3.0,
-          courant: float = 0.5, autotune: bool = True, mem_budget: float = 100e9, device: int = 0):
+          courant: float = 0.5, autotune: bool = True, mem_budget: float = 120e9, device: int = 0):
     """Contexts, device arrays and the batch; returns a dict of them."""
     import torch
     dev = torch.device("cuda", device)

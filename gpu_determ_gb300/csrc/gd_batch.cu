@@ -208,8 +208,8 @@ extern "C" int gd_batch_info(const gd_batch *b, int *groups, int *streams, int *
 // cells and keeps the fastest.  Candidates: the FP32 pair kernel with 1, 2 or
 // 4 CTAs per SM as the minimum s-chunk fill (trading partial-sum traffic for
 // parallelism), and the tensor-core collision matrices in BF16x3 and BF16
-// mode when the caller's mask admits them and their n_pnt^3 matrices fit the
-// memory budget.  Each candidate: one untimed run, then the median of three
+// mode when the caller's mask admits them and their stored triangle tiles
+// (bounded by every tile of the block upper triangle) fit the memory budget.  Each candidate: one untimed run, then the median of three
 // runs timed with CUDA events on the stream.
 
 extern "C" int gd_ctx_autotune(gd_ctx *ctx, const float *f, int ncells, int ld, int path_mask, double mem_budget,
@@ -229,10 +229,10 @@ extern "C" int gd_ctx_autotune(gd_ctx *ctx, const float *f, int ncells, int ld, 
     std::vector<Cand> cands;
     if (path_mask & (1 << GD_GAIN_PAIR))
         for (int w : {1, 2, 4}) cands.push_back({GD_GAIN_PAIR, w});
-    const double n3 = (double)c.d.n_pnt * c.d.n_pnt * c.d.n_pnt;
-    if ((path_mask & (1 << GD_GAIN_CMATRIX_BF16X3)) && 4.0 * n3 <= mem_budget)
+    if ((path_mask & (1 << GD_GAIN_CMATRIX_BF16X3)) && cmatrix_bytes_bound(c, GD_CMATRIX_BF16X3) <= mem_budget)
         cands.push_back({GD_GAIN_CMATRIX_BF16X3, 0});
-    if ((path_mask & (1 << GD_GAIN_CMATRIX_BF16)) && 2.0 * n3 <= mem_budget) cands.push_back({GD_GAIN_CMATRIX_BF16, 0});
+    if ((path_mask & (1 << GD_GAIN_CMATRIX_BF16)) && cmatrix_bytes_bound(c, GD_CMATRIX_BF16) <= mem_budget)
+        cands.push_back({GD_GAIN_CMATRIX_BF16, 0});
     if (cands.empty()) return set_error(GD_ERR_UNSUPPORTED, "no gain path fits the memory budget");
     if (cands.size() > GD_AUTOTUNE_MAX) cands.resize(GD_AUTOTUNE_MAX);
     float *gain = nullptr;

@@ -644,6 +644,15 @@ int cmatrix_loss(gd_cmatrix *h, const float *f, int ncells, int ld, float *nu, c
 
 int64_t cmatrix_stored_tiles(const gd_cmatrix *cm) { return cm ? cm->slots : 0; }
 
+double cmatrix_bytes_bound(const Context &c, int mode)
+{
+    const int ns = c.d.n_pnt, ns_k = (ns + BK - 1) / BK * BK;
+    const int num_n = (ns + BN - 1) / BN, num_k = ns_k / BK;
+    int64_t tiles = 0;
+    for (int n = 0; n < num_n; n++) tiles += k_end(n, num_k);
+    return (double)tiles * ns * BN * BK * 2.0 * (mode == GD_CMATRIX_BF16X3 ? 2.0 : 1.0);
+}
+
 int run_loss_path(Context &c, const float *f, int ncells, int ld, float *nu, cudaStream_t st)
 {
     if (c.gain_path != GD_GAIN_PAIR && c.cmatrix) {

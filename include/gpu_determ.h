@@ -162,15 +162,19 @@ int gd_moments(gd_ctx *ctx, const float *f, int ncells, int ld, double *m5, gd_s
 int gd_ctx_check(gd_ctx *ctx, gd_stream stream);
 
 /* ---- collision-matrix path (tensor cores) ------------------------------ */
-/* The gain as the bilinear form I_i = sum_ab G_i[a][b] f_a f_b with the dense
- * collision matrices G_i assembled on the GPU from the analytic weights
- * (n_pnt^3 BF16 entries, twice that for GD_CMATRIX_BF16X3) and contracted on
- * the tcgen05 tensor cores with FP32 accumulation.  GD_CMATRIX_BF16 rounds
- * f and G to BF16 (relative error ~1e-3 on I); GD_CMATRIX_BF16X3 splits both
- * into BF16 hi + lo parts and sums hi*hi + hi*lo + lo*hi (~1e-5).  The loss
- * and the FP64 projection are unchanged (gd_collision with gain = NULL, then
- * gd_project).  No reference counterpart: the reference forms these matrices
- * only implicitly in its gain loop (collision_integral.cu:75-188). */
+/* The gain as the bilinear form I_i = sum_ab G_i[a][b] f_a f_b with the
+ * collision matrices G_i assembled on the GPU from the analytic weights and
+ * contracted on the tcgen05 tensor cores with FP32 accumulation.  G_i is
+ * symmetric, so only the 256 x 64 tiles of its block upper triangle that hold
+ * a nonzero entry are stored (off-diagonal entries doubled): 1.39 M tiles,
+ * 45.5 GB in BF16 at 20^3 (R = 4.8), twice that for GD_CMATRIX_BF16X3.
+ * GD_CMATRIX_BF16 rounds f and G to BF16 (relative error ~3e-4 on I);
+ * GD_CMATRIX_BF16X3 splits both into BF16 hi + lo parts and sums
+ * hi*hi + hi*lo + lo*hi (~4e-6).  With a context's gain path set to either
+ * mode, its loss nu = B f also runs on the tensor cores (three BF16 GEMMs,
+ * ~1e-5) when ld is a multiple of 4.  No reference counterpart: the reference
+ * forms these matrices only implicitly in its gain loop
+ * (collision_integral.cu:75-188). */
 typedef struct gd_cmatrix gd_cmatrix;
 enum { GD_CMATRIX_BF16 = 0, GD_CMATRIX_BF16X3 = 1 };
 int gd_cmatrix_create(gd_ctx *ctx, int mode, gd_cmatrix **out);
@@ -231,8 +235,9 @@ int gd_batch_info(const gd_batch *b, int *groups, int *streams, int *graph_nodes
 /* Times the gain candidates of a context on the given cells and keeps the
  * fastest (gain path, and for the pair kernel the minimum CTAs per SM of its
  * s-chunk split).  path_mask: bits (1 << GD_GAIN_*) that may be chosen; the
- * collision-matrix paths only when their n_pnt^3 matrices (2 bytes per entry
- * in BF16, 4 in BF16X3) fit mem_budget bytes.  Allocates a gain buffer for
+ * collision-matrix paths only when their stored tiles (at most every 256 x 64
+ * tile of each G_i's block upper triangle, 2 bytes per entry in BF16, 4 in
+ * BF16X3) fit mem_budget bytes.  Allocates a gain buffer for
  * the duration of the call.  Candidates that run out of memory are skipped
  * (cand_ms = -1). */
 #define GD_AUTOTUNE_MAX 8
