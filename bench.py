@@ -212,12 +212,10 @@ def run_ours(args):
             dist.barrier()
         torch.cuda.synchronize()
 
+    from gpu_determ_gb300.sharding import max_over_ranks as _max
+
     def max_over_ranks(ms):
-        if dist is None:
-            return ms
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
+        return _max(ms, device="cuda")
 
     def plain_step(fb):
         ctx.step(fb, nc, nc, gd.DT_COURANT, args.courant, stream=stream)
