@@ -69,7 +69,8 @@ class _MlpInfo(C.Structure):
 
 class _Autotune(C.Structure):
     _fields_ = [("path", C.c_int), ("waves", C.c_int), ("best_ms", C.c_float), ("n_candidates", C.c_int),
-                ("cand_path", C.c_int * 8), ("cand_waves", C.c_int * 8), ("cand_ms", C.c_float * 8)]
+                ("cand_path", C.c_int * 8), ("cand_waves", C.c_int * 8), ("cand_ms", C.c_float * 8),
+                ("cluster", C.c_int), ("cand_cluster", C.c_int * 8)]
 
 
 def library_path() -> str:
@@ -108,6 +109,7 @@ def lib():
     L.gd_cmatrix_create.argtypes = [vp, i, P(vp)]
     L.gd_cmatrix_gain.argtypes = [vp, vp, i, i, vp, vp]
     L.gd_cmatrix_destroy.argtypes = [vp]
+    L.gd_cmatrix_set_cluster.argtypes = [vp, i]
     L.gd_ctx_set_gain_path.argtypes = [vp, i]
     L.gd_box_to_compact.argtypes = [vp, vp, i, i, vp, i, vp]
     L.gd_compact_to_box.argtypes = [vp, vp, i, i, vp, i, vp]
@@ -138,7 +140,7 @@ def lib():
                  "gd_export_tables", "gd_correction_basis", "gd_collision", "gd_project",
                  "gd_relax", "gd_step", "gd_moments", "gd_ctx_check", "gd_set_memory_limit", "gd_gain_noalloc",
                  "gd_box_to_compact", "gd_compact_to_box", "gd_load_options", "gd_cmatrix_create",
-                 "gd_cmatrix_gain", "gd_cmatrix_destroy", "gd_ctx_set_gain_path",
+                 "gd_cmatrix_gain", "gd_cmatrix_destroy", "gd_cmatrix_set_cluster", "gd_ctx_set_gain_path",
                  "gd_mlp_create", "gd_mlp_destroy", "gd_mlp_set_io_scale", "gd_mlp_info", "gd_mlp_forward", "gd_mlp_train_step",
                  "gd_mlp_loss", "gd_mlp_check", "gd_mlp_get_params", "gd_mlp_set_params", "gd_mlp_get_grads",
                  "gd_surrogate_create", "gd_surrogate_destroy", "gd_surrogate_gain", "gd_cell_rel_l2",
@@ -277,9 +279,10 @@ class Context:
         _check(lib().gd_ctx_autotune(self._h, _ptr(f), int(ncells), int(ld), int(path_mask), float(mem_budget),
                                      C.byref(r), _stream(stream)))
         names = {GAIN_PAIR: "pair", GAIN_CMATRIX_BF16: "cmatrix_bf16", GAIN_CMATRIX_BF16X3: "cmatrix_bf16x3"}
-        cands = [{"path": names[r.cand_path[k]], "waves": r.cand_waves[k], "ms": r.cand_ms[k]}
-                 for k in range(r.n_candidates)]
-        return {"path": names[r.path], "waves": r.waves, "best_ms": r.best_ms, "candidates": cands}
+        cands = [{"path": names[r.cand_path[k]], "waves": r.cand_waves[k], "cluster": r.cand_cluster[k],
+                  "ms": r.cand_ms[k]} for k in range(r.n_candidates)]
+        return {"path": names[r.path], "waves": r.waves, "cluster": r.cluster, "best_ms": r.best_ms,
+                "candidates": cands}
 
     def box_to_compact(self, box, ncells, ld_box, compact, ld, stream=None):
         _check(lib().gd_box_to_compact(self._h, _ptr(box), int(ncells), int(ld_box), _ptr(compact), int(ld),
@@ -309,6 +312,10 @@ class CollisionMatrix:
 
     def gain(self, f, ncells, ld, gain, stream=None):
         _check(lib().gd_cmatrix_gain(self._h, _ptr(f), int(ncells), int(ld), _ptr(gain), _stream(stream)))
+
+    def set_cluster(self, ctas: int):
+        """1 or 2 CTAs per cluster (2: collision-matrix tiles multicast to both)."""
+        _check(lib().gd_cmatrix_set_cluster(self._h, int(ctas)))
 
     def close(self):
         if self._h:

@@ -208,7 +208,8 @@ extern "C" int gd_batch_info(const gd_batch *b, int *groups, int *streams, int *
 // cells and keeps the fastest.  Candidates: the FP32 pair kernel with 1, 2 or
 // 4 CTAs per SM as the minimum s-chunk fill (trading partial-sum traffic for
 // parallelism), and the tensor-core collision matrices in BF16x3 and BF16
-// mode when the caller's mask admits them and their stored triangle tiles
+// mode, each with 1 or 2 CTAs per cluster (multicast of the matrix tiles),
+// when the caller's mask admits them and their stored triangle tiles
 // (bounded by every tile of the block upper triangle) fit the memory budget.  Each candidate: one untimed run, then the median of three
 // runs timed with CUDA events on the stream.
 
@@ -224,15 +225,15 @@ extern "C" int gd_ctx_autotune(gd_ctx *ctx, const float *f, int ncells, int ld, 
     cudaStream_t st = (cudaStream_t)stream;
     std::memset(res, 0, sizeof(*res));
     struct Cand {
-        int path, waves;
+        int path, waves, cluster;
     };
     std::vector<Cand> cands;
     if (path_mask & (1 << GD_GAIN_PAIR))
-        for (int w : {1, 2, 4}) cands.push_back({GD_GAIN_PAIR, w});
+        for (int w : {1, 2, 4}) cands.push_back({GD_GAIN_PAIR, w, 1});
     if ((path_mask & (1 << GD_GAIN_CMATRIX_BF16X3)) && cmatrix_bytes_bound(c, GD_CMATRIX_BF16X3) <= mem_budget)
-        cands.push_back({GD_GAIN_CMATRIX_BF16X3, 0});
+        for (int cl : {1, 2}) cands.push_back({GD_GAIN_CMATRIX_BF16X3, 0, cl});
     if ((path_mask & (1 << GD_GAIN_CMATRIX_BF16)) && cmatrix_bytes_bound(c, GD_CMATRIX_BF16) <= mem_budget)
-        cands.push_back({GD_GAIN_CMATRIX_BF16, 0});
+        for (int cl : {1, 2}) cands.push_back({GD_GAIN_CMATRIX_BF16, 0, cl});
     if (cands.empty()) return set_error(GD_ERR_UNSUPPORTED, "no gain path fits the memory budget");
     if (cands.size() > GD_AUTOTUNE_MAX) cands.resize(GD_AUTOTUNE_MAX);
     float *gain = nullptr;
@@ -247,6 +248,7 @@ extern "C" int gd_ctx_autotune(gd_ctx *ctx, const float *f, int ncells, int ld, 
     for (size_t i = 0; i < cands.size() && !rc; i++) {
         res->cand_path[i] = cands[i].path;
         res->cand_waves[i] = cands[i].waves;
+        res->cand_cluster[i] = cands[i].cluster;
         res->cand_ms[i] = -1.f;
         int r = gd_ctx_set_gain_path(ctx, cands[i].path);
         if (r == GD_ERR_OUT_OF_MEMORY) {  // this candidate does not fit: skip it
@@ -258,6 +260,10 @@ extern "C" int gd_ctx_autotune(gd_ctx *ctx, const float *f, int ncells, int ld, 
             break;
         }
         if (cands[i].waves) c.gain_waves = cands[i].waves;
+        if (c.cmatrix && (r = gd_cmatrix_set_cluster(c.cmatrix, cands[i].cluster))) {
+            rc = r;
+            break;
+        }
         float t[3];
         for (int k = -1; k < 3 && !rc; k++) {
             cudaEventRecord(e0, st);
@@ -284,9 +290,11 @@ extern "C" int gd_ctx_autotune(gd_ctx *ctx, const float *f, int ncells, int ld, 
         return rc ? rc : set_error(GD_ERR_UNSUPPORTED, "no gain candidate could run");
     }
     if ((rc = gd_ctx_set_gain_path(ctx, cands[best_i].path))) return rc;
+    if (c.cmatrix && (rc = gd_cmatrix_set_cluster(c.cmatrix, cands[best_i].cluster))) return rc;
     c.gain_waves = cands[best_i].waves ? cands[best_i].waves : saved_waves;
     res->path = cands[best_i].path;
     res->waves = c.gain_waves;
+    res->cluster = cands[best_i].cluster;
     res->best_ms = best;
     return GD_OK;
 }

@@ -53,6 +53,7 @@ struct CmParams {
     int *err;        // set to 1 when a wait times out
     const int *node_off;     // [ns + 1] each node's range of stored tiles
     const uint32_t *tiles;   // stored tiles, n << 16 | k, n-major then k within each node
+    int m_tiles;             // cell tiles, padded to whole clusters
 };
 
 // G_i is symmetric in (a, b), so only its block upper triangle is stored and
@@ -66,7 +67,10 @@ __host__ __device__ __forceinline__ int k_end(int n, int num_k)
 }
 
 // NPASS = 1: D = F_hi G_hi.  NPASS = 3: D = F_hi G_hi + F_hi G_lo + F_lo G_hi.
-template <int NPASS>
+// CL = 2: a cluster of two CTAs holding adjacent cell tiles of the same node;
+// each loads half of every G tile (BN / 2 rows) and multicasts it to both, so
+// the node's tiles cross L2 once per cluster instead of once per CTA.
+template <int NPASS, int CL>
 __global__ void __launch_bounds__(kThreads, 1)
     cmatrix_gain_kernel(const __grid_constant__ CUtensorMap tmFh, const __grid_constant__ CUtensorMap tmFl,
                         const __grid_constant__ CUtensorMap tmGh, const __grid_constant__ CUtensorMap tmGl,
@@ -84,15 +88,21 @@ __global__ void __launch_bounds__(kThreads, 1)
     __shared__ int abort_flag;
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int m_tile = blockIdx.x, node = blockIdx.y;
 
-    if (threadIdx.x == 0) abort_flag = *(volatile int *)p.err;
-    __syncthreads();
-    if (abort_flag) return;  // an earlier CTA timed out: do no work
+    if (CL == 1) {
+        if (threadIdx.x == 0) abort_flag = *(volatile int *)p.err;
+        __syncthreads();
+        if (abort_flag) return;  // an earlier CTA timed out: do no work
+    } else {
+        // clustered CTAs never leave early: both must reach the cluster barriers
+        if (threadIdx.x == 0) abort_flag = 0;
+    }
+    const uint16_t cta_mask = (uint16_t)((1u << CL) - 1u);
+    const uint32_t crank = CL > 1 ? cluster_rank() : 0u;
     if (threadIdx.x == 0) {
         for (int s = 0; s < S; s++) {
             mbar_init(smem_u32(&full_bar[s]), 1);
-            mbar_init(smem_u32(&empty_bar[s]), 1);
+            mbar_init(smem_u32(&empty_bar[s]), CL);  // released by the MMA of every CTA that reads it
         }
         for (int b = 0; b < 2; b++) {
             mbar_init(smem_u32(&accf_bar[b]), 1);
@@ -109,78 +119,127 @@ __global__ void __launch_bounds__(kThreads, 1)
         asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     }
     __syncthreads();
+    if (CL > 1) cluster_sync();  // the peer's barriers exist before any multicast or commit reaches them
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = tmem_base_holder;
+
+    // work units (node, CL consecutive cell tiles): unit u is node u / m_groups;
+    // the CTAs (clusters) of the persistent grid take the units round-robin, and
+    // every counter below runs on across units, so one unit's pipeline fill and
+    // last epilogue overlap its neighbours
+    const int m_groups = p.m_tiles / CL;
+    const int units = p.ns * m_groups;
+    const int cid = (int)(blockIdx.x / CL), nclusters = (int)(gridDim.x / CL);
 
     if (warp == 0) {
         // ---- TMA producer ----------------------------------------------------
         if (lane == 0) {
-            const int l0 = __ldg(p.node_off + node), cnt = __ldg(p.node_off + node + 1) - l0;
-            for (int it = 0; it < cnt; it++) {
-                const int s = it % S;
-                const uint32_t ph = (uint32_t)(it / S) & 1u;
-                if (!mbar_wait(smem_u32(&empty_bar[s]), ph ^ 1u, p.err)) {
-                    abort_flag = 1;
-                    break;
+            int it = 0;
+            bool stop = false;
+            for (int u = cid; u < units && !stop; u += nclusters) {
+                const int node = u / m_groups, m_tile = (u % m_groups) * CL + (int)crank;
+                const int l0 = __ldg(p.node_off + node), cnt = __ldg(p.node_off + node + 1) - l0;
+                for (int j = 0; j < cnt; j++, it++) {
+                    const int s = it % S;
+                    const uint32_t ph = (uint32_t)(it / S) & 1u;
+                    if (!mbar_wait(smem_u32(&empty_bar[s]), ph ^ 1u, p.err)) {
+                        abort_flag = 1;
+                        stop = true;
+                        break;
+                    }
+                    if (*(volatile int *)&abort_flag) {
+                        stop = true;
+                        break;
+                    }
+                    const int k = (int)(__ldg(p.tiles + l0 + j) & 0xffffu);
+                    unsigned char *st = base + (size_t)s * kStage;
+                    const uint32_t fb = smem_u32(&full_bar[s]);
+                    mbar_expect_tx(fb, kStage);
+                    tma_load_2d(smem_u32(st), &tmFh, k * BK, m_tile * BM, fb);
+                    // stored tile l0 + j ([slot][BN rows][BK]); with CL > 1 this CTA's
+                    // share of its rows, multicast into the same place in every CTA
+                    if (CL == 1) {
+                        tma_load_3d(smem_u32(st + kTileA), &tmGh, 0, 0, l0 + j, fb);
+                    } else {
+                        const uint32_t part = crank * (kTileB / CL);
+                        tma_load_3d_mc(smem_u32(st + kTileA) + part, &tmGh, 0, (int)crank * (BN / CL), l0 + j, fb,
+                                       cta_mask);
+                    }
+                    if (NPARTS == 2) {
+                        tma_load_2d(smem_u32(st + kTileA + kTileB), &tmFl, k * BK, m_tile * BM, fb);
+                        if (CL == 1) {
+                            tma_load_3d(smem_u32(st + 2 * kTileA + kTileB), &tmGl, 0, 0, l0 + j, fb);
+                        } else {
+                            const uint32_t part = crank * (kTileB / CL);
+                            tma_load_3d_mc(smem_u32(st + 2 * kTileA + kTileB) + part, &tmGl, 0,
+                                           (int)crank * (BN / CL), l0 + j, fb, cta_mask);
+                        }
+                    }
                 }
-                if (*(volatile int *)&abort_flag) break;
-                const int k = (int)(__ldg(p.tiles + l0 + it) & 0xffffu);
-                unsigned char *st = base + (size_t)s * kStage;
-                const uint32_t fb = smem_u32(&full_bar[s]);
-                mbar_expect_tx(fb, kStage);
-                tma_load_2d(smem_u32(st), &tmFh, k * BK, m_tile * BM, fb);
-                // stored tile l0 + it ([slot][BN rows][BK])
-                tma_load_3d(smem_u32(st + kTileA), &tmGh, 0, 0, l0 + it, fb);
-                if (NPARTS == 2) {
-                    tma_load_2d(smem_u32(st + kTileA + kTileB), &tmFl, k * BK, m_tile * BM, fb);
-                    tma_load_3d(smem_u32(st + 2 * kTileA + kTileB), &tmGl, 0, 0, l0 + it, fb);
-                }
+            }
+            if (CL > 1) {
+                // tail, bounded like every wait: the copies of the last stages have
+                // landed here, and every stage was released by the MMA of both CTAs
+                // (their commits have arrived here), before this CTA may leave the
+                // cluster; after a time-out the waits give up at once
+                const int j0 = it > S ? it - S : 0;
+                for (int j = j0; j < it; j++)
+                    if (!mbar_wait(smem_u32(&full_bar[j % S]), (uint32_t)(j / S) & 1u, p.err)) break;
+                for (int j = j0; j < it; j++)
+                    if (!mbar_wait(smem_u32(&empty_bar[j % S]), (uint32_t)(j / S) & 1u, p.err)) break;
             }
         }
     } else if (warp == 1) {
         // ---- MMA issuer --------------------------------------------------------
         if (lane == 0) {
             bool ok = true;
-            const int l0 = __ldg(p.node_off + node), cnt = __ldg(p.node_off + node + 1) - l0;
-            int it = 0, grp = 0;  // stored tile, group of tiles sharing one b-tile n
-            while (ok && it < cnt) {
-                const uint32_t n = __ldg(p.tiles + l0 + it) >> 16;
-                const int buf = grp & 1;
-                const uint32_t use = (uint32_t)(grp >> 1);
-                if (!mbar_wait(smem_u32(&acce_bar[buf]), (use & 1u) ^ 1u, p.err)) {
-                    ok = false;
-                    break;
-                }
-                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-                const uint32_t d_tmem = tmem + (uint32_t)(buf * BN);
-                bool first = true;
-                for (; it < cnt && (__ldg(p.tiles + l0 + it) >> 16) == n; it++) {
-                    const int s = it % S;
-                    const uint32_t ph = (uint32_t)(it / S) & 1u;
-                    if (!mbar_wait(smem_u32(&full_bar[s]), ph, p.err)) {
+            int it = 0, grp = 0;  // stage counter; groups of tiles sharing one b-tile n
+            for (int u = cid; u < units && ok; u += nclusters) {
+                const int node = u / m_groups;
+                const int l0 = __ldg(p.node_off + node), cnt = __ldg(p.node_off + node + 1) - l0;
+                int j = 0;
+                while (ok && j < cnt) {
+                    const uint32_t n = __ldg(p.tiles + l0 + j) >> 16;
+                    const int buf = grp & 1;
+                    const uint32_t use = (uint32_t)(grp >> 1);
+                    if (!mbar_wait(smem_u32(&acce_bar[buf]), (use & 1u) ^ 1u, p.err)) {
                         ok = false;
                         break;
                     }
                     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-                    const uint32_t st = smem_u32(base + (size_t)s * kStage);
-                    const uint32_t aH = st, bH = st + kTileA;
-                    const uint32_t aL = st + kTileA + kTileB, bL = st + 2 * kTileA + kTileB;
-#pragma unroll
-                    for (int kk = 0; kk < BK / 16; kk++) {
-                        const uint32_t off = (uint32_t)kk * 32u;  // 16 BF16 along K
-                        const uint32_t acc = (!first || kk > 0) ? 1u : 0u;
-                        umma_bf16(d_tmem, umma_desc(aH + off), umma_desc(bH + off), kIdesc, acc);
-                        if (NPASS == 3) {
-                            umma_bf16(d_tmem, umma_desc(aH + off), umma_desc(bL + off), kIdesc, 1u);
-                            umma_bf16(d_tmem, umma_desc(aL + off), umma_desc(bH + off), kIdesc, 1u);
+                    const uint32_t d_tmem = tmem + (uint32_t)(buf * BN);
+                    bool first = true;
+                    for (; j < cnt && (__ldg(p.tiles + l0 + j) >> 16) == n; j++, it++) {
+                        const int s = it % S;
+                        const uint32_t ph = (uint32_t)(it / S) & 1u;
+                        if (!mbar_wait(smem_u32(&full_bar[s]), ph, p.err)) {
+                            ok = false;
+                            break;
                         }
+                        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                        const uint32_t st = smem_u32(base + (size_t)s * kStage);
+                        const uint32_t aH = st, bH = st + kTileA;
+                        const uint32_t aL = st + kTileA + kTileB, bL = st + 2 * kTileA + kTileB;
+#pragma unroll
+                        for (int kk = 0; kk < BK / 16; kk++) {
+                            const uint32_t off = (uint32_t)kk * 32u;  // 16 BF16 along K
+                            const uint32_t acc = (!first || kk > 0) ? 1u : 0u;
+                            umma_bf16(d_tmem, umma_desc(aH + off), umma_desc(bH + off), kIdesc, acc);
+                            if (NPASS == 3) {
+                                umma_bf16(d_tmem, umma_desc(aH + off), umma_desc(bL + off), kIdesc, 1u);
+                                umma_bf16(d_tmem, umma_desc(aL + off), umma_desc(bH + off), kIdesc, 1u);
+                            }
+                        }
+                        if (CL == 1)
+                            umma_commit(smem_u32(&empty_bar[s]));
+                        else
+                            umma_commit_mc(smem_u32(&empty_bar[s]), cta_mask);
+                        first = false;
                     }
-                    umma_commit(smem_u32(&empty_bar[s]));
-                    first = false;
+                    if (!ok) break;
+                    umma_commit(smem_u32(&accf_bar[buf]));
+                    grp++;
                 }
-                if (!ok) break;
-                umma_commit(smem_u32(&accf_bar[buf]));
-                grp++;
             }
             if (!ok) abort_flag = 1;
         }
@@ -188,52 +247,61 @@ __global__ void __launch_bounds__(kThreads, 1)
         // ---- epilogue: warps 2..5 own TMEM lane quadrants (warp % 4) -------------
         const int quad = warp & 3;
         const int row = quad * 32 + lane;
-        const int cell = m_tile * BM + row;
-        const bool live = cell < p.ncells;
-        float sum = 0.f;
-        const int l0 = __ldg(p.node_off + node), cnt = __ldg(p.node_off + node + 1) - l0;
-        // f[b][cell] for 32 consecutive b; rows b >= ns of G are zero, so T[b] = 0
-        // there and clamping b keeps every load in bounds without a branch
-        const float *fcell = p.f + (live ? cell : 0);
-        float fv[32], fn[32];
-        auto load_f = [&](float *dst, int b0) {
+        int grp = 0;
+        bool failed = false;
+        for (int u = cid; u < units && !failed; u += nclusters) {
+            const int node = u / m_groups, m_tile = (u % m_groups) * CL + (int)crank;
+            const int cell = m_tile * BM + row;
+            const bool live = cell < p.ncells;
+            float sum = 0.f;
+            const int l0 = __ldg(p.node_off + node), cnt = __ldg(p.node_off + node + 1) - l0;
+            // f[b][cell] for 32 consecutive b; rows b >= ns of G are zero, so T[b] = 0
+            // there and clamping b keeps every load in bounds without a branch
+            const float *fcell = p.f + (live ? cell : 0);
+            float fv[32], fn[32];
+            auto load_f = [&](float *dst, int b0) {
 #pragma unroll
-            for (int j = 0; j < 32; j++) dst[j] = __ldg(fcell + (size_t)min(b0 + j, p.ns - 1) * p.ld);
-        };
-        for (int it = 0, grp = 0; it < cnt; grp++) {
-            // b-tiles without stored tiles contribute nothing and are skipped
-            const int n = (int)(__ldg(p.tiles + l0 + it) >> 16);
-            while (it < cnt && (int)(__ldg(p.tiles + l0 + it) >> 16) == n) it++;
-            const int buf = grp & 1;
-            const uint32_t use = (uint32_t)(grp >> 1);
-            // the first chunk's f loads overlap the wait for the accumulator
-            if (live) load_f(fv, n * BN);
-            bool ok = true;
-            if (lane == 0) ok = mbar_wait(smem_u32(&accf_bar[buf]), use & 1u, p.err);
-            ok = __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
-            if (!ok) break;
-            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            const uint32_t taddr = tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(buf * BN);
-#pragma unroll
-            for (int c0 = 0; c0 < BN; c0 += 32) {
-                float v[32];
-                tmem_ld32(taddr + (uint32_t)c0, v);
-                // next chunk's loads are in flight during this chunk's FMAs
-                if (live && c0 + 32 < BN) load_f(fn, n * BN + c0 + 32);
-                if (live) {
-#pragma unroll
-                    for (int j = 0; j < 32; j++) sum = __fmaf_rn(v[j], fv[j], sum);
+                for (int q = 0; q < 32; q++) dst[q] = __ldg(fcell + (size_t)min(b0 + q, p.ns - 1) * p.ld);
+            };
+            for (int j = 0; j < cnt; grp++) {
+                // b-tiles without stored tiles contribute nothing and are skipped
+                const int n = (int)(__ldg(p.tiles + l0 + j) >> 16);
+                while (j < cnt && (int)(__ldg(p.tiles + l0 + j) >> 16) == n) j++;
+                const int buf = grp & 1;
+                const uint32_t use = (uint32_t)(grp >> 1);
+                // the first chunk's f loads overlap the wait for the accumulator
+                if (live) load_f(fv, n * BN);
+                bool ok = true;
+                if (lane == 0) ok = mbar_wait(smem_u32(&accf_bar[buf]), use & 1u, p.err);
+                ok = __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
+                if (!ok) {
+                    failed = true;
+                    break;
                 }
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                const uint32_t taddr = tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(buf * BN);
 #pragma unroll
-                for (int j = 0; j < 32; j++) fv[j] = fn[j];
+                for (int c0 = 0; c0 < BN; c0 += 32) {
+                    float v[32];
+                    tmem_ld32(taddr + (uint32_t)c0, v);
+                    // next chunk's loads are in flight during this chunk's FMAs
+                    if (live && c0 + 32 < BN) load_f(fn, n * BN + c0 + 32);
+                    if (live) {
+#pragma unroll
+                        for (int q = 0; q < 32; q++) sum = __fmaf_rn(v[q], fv[q], sum);
+                    }
+#pragma unroll
+                    for (int q = 0; q < 32; q++) fv[q] = fn[q];
+                }
+                asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+                __syncwarp();
+                if (lane == 0) mbar_arrive(smem_u32(&acce_bar[buf]));
             }
-            asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-            __syncwarp();
-            if (lane == 0) mbar_arrive(smem_u32(&acce_bar[buf]));
+            if (!failed && live) p.gain[(size_t)node * p.ld + cell] = sum;
         }
-        if (live) p.gain[(size_t)node * p.ld + cell] = sum;
     }
     __syncthreads();
+    if (CL > 1) cluster_sync();  // no remote write or arrival can reach this CTA after it leaves
     if (warp == 1) {
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * BN) : "memory");
@@ -392,6 +460,7 @@ struct gd_cmatrix {
     int mode = 0;  // GD_CMATRIX_BF16 or GD_CMATRIX_BF16X3
     int ns = 0, ns_k = 0;
     int tiles = 0;       // BN x BK tiles of one node's block upper triangle
+    int cluster = 1;     // CTAs per cluster sharing each G tile by multicast (1 or 2)
     int64_t slots = 0;   // stored (not all-zero) tiles over all nodes
     int *node_off = nullptr;    // [ns + 1] into list
     uint32_t *list = nullptr;   // stored tiles per node, n << 16 | k
@@ -533,6 +602,14 @@ extern "C" int gd_cmatrix_create(gd_ctx *ctx, int mode, gd_cmatrix **out)
     return GD_OK;
 }
 
+extern "C" int gd_cmatrix_set_cluster(gd_cmatrix *h, int ctas)
+{
+    if (!h) return gd::set_error(GD_ERR_INVALID_ARG, "NULL argument");
+    if (ctas != 1 && ctas != 2) return gd::set_error(GD_ERR_INVALID_ARG, "cluster size must be 1 or 2");
+    h->cluster = ctas;
+    return GD_OK;
+}
+
 extern "C" int gd_cmatrix_destroy(gd_cmatrix *h)
 {
     if (!h) return GD_OK;
@@ -571,7 +648,9 @@ extern "C" int gd_cmatrix_gain(gd_cmatrix *h, const float *f, int ncells, int ld
     const cuuint32_t fbox[2] = {BK, BM};
     const cuuint64_t gdims[3] = {(cuuint64_t)BK, (cuuint64_t)BN, (cuuint64_t)std::max<int64_t>(h->slots, 1)};
     const cuuint64_t gstr[2] = {(cuuint64_t)BK * 2, (cuuint64_t)BN * BK * 2};
-    const cuuint32_t gbox[3] = {BK, BN, 1};
+    // with a 2-CTA cluster each CTA loads (and multicasts) half of a G tile
+    const int cl = (h->cluster == 2 && ncells > BM) ? 2 : 1;
+    const cuuint32_t gbox[3] = {BK, (cuuint32_t)(BN / cl), 1};
     if ((rc = encode(enc, &tFh, h->fh, 2, fdims, fstr, fbox))) return rc;
     if ((rc = encode(enc, &tGh, h->gh, 3, gdims, gstr, gbox))) return rc;
     if (split) {
@@ -581,16 +660,31 @@ extern "C" int gd_cmatrix_gain(gd_cmatrix *h, const float *f, int ncells, int ld
         tFl = tFh;
         tGl = tGh;
     }
-    CmParams prm{h->ns, h->ns_k, ncells, ld, f, gain, h->err, h->node_off, h->list};
-    dim3 grid((ncells + BM - 1) / BM, h->ns);
+    // cell tiles padded to whole clusters: a tile past ncells reads zeros and stores nothing
+    const int m_tiles = ((ncells + BM - 1) / BM + cl - 1) / cl * cl;
+    CmParams prm{h->ns, h->ns_k, ncells, ld, f, gain, h->err, h->node_off, h->list, m_tiles};
+    // persistent grid: one CTA per SM (whole clusters), at most one per work unit
+    const int64_t units = (int64_t)h->ns * (m_tiles / cl);
+    const int sms = std::max(cl, h->ctx->c.sm_count / cl * cl);
+    dim3 grid((unsigned)std::min<int64_t>(sms, units * cl), 1);
     const size_t smem = (split ? 2 * 2 * (kTileA + kTileB) : 4 * (kTileA + kTileB)) + 1024;
-    if (split) {
-        GD_CUDA(cudaFuncSetAttribute(cmatrix_gain_kernel<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        cmatrix_gain_kernel<3><<<grid, kThreads, smem, st>>>(tFh, tFl, tGh, tGl, prm);
-    } else {
-        GD_CUDA(cudaFuncSetAttribute(cmatrix_gain_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        cmatrix_gain_kernel<1><<<grid, kThreads, smem, st>>>(tFh, tFl, tGh, tGl, prm);
-    }
+    void (*kern)(const CUtensorMap, const CUtensorMap, const CUtensorMap, const CUtensorMap, CmParams) =
+        split ? (cl == 2 ? cmatrix_gain_kernel<3, 2> : cmatrix_gain_kernel<3, 1>)
+              : (cl == 2 ? cmatrix_gain_kernel<1, 2> : cmatrix_gain_kernel<1, 1>);
+    GD_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = dim3(kThreads);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = (unsigned)cl;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    GD_CUDA(cudaLaunchKernelEx(&cfg, kern, tFh, tFl, tGh, tGl, prm));
     GD_CUDA(cudaGetLastError());
     // the kernel records a time-out instead of hanging; report it (inside a
     // stream capture the flag stays set for gd_cmatrix_check after replay)

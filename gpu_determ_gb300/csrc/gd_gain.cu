@@ -47,20 +47,25 @@ struct GainArgs {
     const uint32_t *D_members;
     const int *s_bounds;
     float *part;  // [chunk][n_pnt][cells_pad]
+    int cmap_smem;  // 1: box -> compact map copied to shared memory; 0: read through L1 (selects the instance)
 };
 
-template <int CB>
+template <int CB, bool CMAP_SMEM>
 __global__ void __launch_bounds__(kThreads, 1) gain_pair_kernel(GainArgs a)
 {
     constexpr int G = 32 / CB;  // item rows per warp
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ int row_next;
     const Dims &d = a.d;
-    // P_s[class index][CB] first, then the box -> compact map
+    // P_s[class index][CB] first, then (when it fits) the box -> compact map;
+    // otherwise the map is read from global memory through L1 (its lookups are
+    // uniform across the cells of a lane group)
     float *P = reinterpret_cast<float *>(smem);
-    int16_t *cmap = reinterpret_cast<int16_t *>(smem + (size_t)d.nclass * CB * sizeof(float));
+    int16_t *cmap_s = reinterpret_cast<int16_t *>(smem + (size_t)d.nclass * CB * sizeof(float));
+    const int16_t *cmap = CMAP_SMEM ? cmap_s : a.cmap;
 
-    for (int t = threadIdx.x; t < d.nxyz; t += blockDim.x) cmap[t] = a.cmap[t];
+    if (CMAP_SMEM)
+        for (int t = threadIdx.x; t < d.nxyz; t += blockDim.x) cmap_s[t] = a.cmap[t];
     for (int t = threadIdx.x; t < d.nclass * CB; t += blockDim.x) P[t] = 0.f;
 
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
@@ -227,9 +232,9 @@ __global__ void gain_reduce_kernel(const float *__restrict__ part, int nchunks, 
     }
 }
 
-size_t gain_smem_bytes(const Dims &d, int cb)
+size_t gain_smem_bytes(const Dims &d, int cb, bool cmap_smem)
 {
-    return (size_t)d.nclass * cb * sizeof(float) + (size_t)((d.nxyz * 2 + 15) & ~15);
+    return (size_t)d.nclass * cb * sizeof(float) + (cmap_smem ? (size_t)((d.nxyz * 2 + 15) & ~15) : 0);
 }
 
 // Number of s-chunks for nblk cell blocks: at least gain_waves CTAs per SM
@@ -261,14 +266,24 @@ int gain_plan_cells(Context &c)
 {
     int max_smem = 0;
     GD_CUDA(cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, c.device));
+    // widest cell block that fits: with the box -> compact map in shared memory
+    // first, then with the map read through L1
     int cb = 32;
-    while (cb > 4 && gain_smem_bytes(c.d, cb) > (size_t)max_smem) cb >>= 1;
-    if (gain_smem_bytes(c.d, cb) > (size_t)max_smem)
-        return set_error(GD_ERR_UNSUPPORTED, "velocity grid too large for the gain kernel's shared memory");
+    bool cmap_smem = true;
+    for (;;) {
+        if (gain_smem_bytes(c.d, cb, true) <= (size_t)max_smem) break;
+        if (gain_smem_bytes(c.d, cb, false) <= (size_t)max_smem) {
+            cmap_smem = false;
+            break;
+        }
+        if (cb == 4) return set_error(GD_ERR_UNSUPPORTED, "velocity grid too large for the gain kernel's shared memory");
+        cb >>= 1;
+    }
     if ((int64_t)c.d.nclass * cb * 4 >= ((int64_t)1 << 32))
         return set_error(GD_ERR_UNSUPPORTED, "pair-product array too large");
     c.gain_cb = cb;
-    c.gain_smem = gain_smem_bytes(c.d, cb);
+    c.gain_cmap_smem = cmap_smem;
+    c.gain_smem = gain_smem_bytes(c.d, cb, cmap_smem);
     return GD_OK;
 }
 
@@ -298,7 +313,7 @@ int run_gain(Context &c, const float *f, int ncells, int ld, float *gain, cudaSt
 {
     const Dims &d = c.d;
     const int cb = c.gain_cb;
-    const size_t smem = gain_smem_bytes(d, cb);
+    const size_t smem = c.gain_smem;
     const int nblk = (ncells + cb - 1) / cb;
     const int cells_pad = nblk * cb;
     // chunks of s: at least two CTAs per SM, whole waves preferred (one CTA
@@ -316,14 +331,20 @@ int run_gain(Context &c, const float *f, int ncells, int ld, float *gain, cudaSt
     GD_CUDA(cudaMemsetAsync(part, 0, part_bytes, st));
 
     GainArgs a{d, f, ld, ncells, cells_pad, c.d_cmap, c.d_grp_row_off, c.d_grp_rows, c.d_D_item_off,
-               c.d_D_items, c.d_D_members, d_bounds, part};
+               c.d_D_items, c.d_D_members, d_bounds, part, c.gain_cmap_smem ? 1 : 0};
     dim3 grid(nblk, nchunks);
     switch (cb) {
 #define GD_GAIN_CASE(CBV)                                                                       \
     case CBV:                                                                                   \
-        GD_CUDA(cudaFuncSetAttribute(gain_pair_kernel<CBV>,                                     \
-                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));  \
-        gain_pair_kernel<CBV><<<grid, kThreads, smem, st>>>(a);                                 \
+        if (a.cmap_smem) {                                                                      \
+            GD_CUDA(cudaFuncSetAttribute(gain_pair_kernel<CBV, true>,                           \
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)); \
+            gain_pair_kernel<CBV, true><<<grid, kThreads, smem, st>>>(a);                       \
+        } else {                                                                                \
+            GD_CUDA(cudaFuncSetAttribute(gain_pair_kernel<CBV, false>,                          \
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)); \
+            gain_pair_kernel<CBV, false><<<grid, kThreads, smem, st>>>(a);                      \
+        }                                                                                       \
         break;
         GD_GAIN_CASE(32)
         GD_GAIN_CASE(16)
@@ -382,14 +403,20 @@ int launch_gain_pair(Context &c, const float *f, int ncells, int ld, float *gain
     const int cells_pad = nblk * cb;
     GD_CUDA(cudaMemsetAsync(part, 0, (size_t)nchunks * d.n_pnt * cells_pad * sizeof(float), st));
     GainArgs a{d, f, ld, ncells, cells_pad, c.d_cmap, c.d_grp_row_off, c.d_grp_rows, c.d_D_item_off,
-               c.d_D_items, c.d_D_members, d_bounds, part};
+               c.d_D_items, c.d_D_members, d_bounds, part, c.gain_cmap_smem ? 1 : 0};
     dim3 grid(nblk, nchunks);
     switch (cb) {
 #define GD_GAIN_CASE(CBV)                                                                       \
     case CBV:                                                                                   \
-        GD_CUDA(cudaFuncSetAttribute(gain_pair_kernel<CBV>,                                     \
-                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));  \
-        gain_pair_kernel<CBV><<<grid, kThreads, smem, st>>>(a);                                 \
+        if (a.cmap_smem) {                                                                      \
+            GD_CUDA(cudaFuncSetAttribute(gain_pair_kernel<CBV, true>,                           \
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)); \
+            gain_pair_kernel<CBV, true><<<grid, kThreads, smem, st>>>(a);                       \
+        } else {                                                                                \
+            GD_CUDA(cudaFuncSetAttribute(gain_pair_kernel<CBV, false>,                          \
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)); \
+            gain_pair_kernel<CBV, false><<<grid, kThreads, smem, st>>>(a);                      \
+        }                                                                                       \
         break;
         GD_GAIN_CASE(32)
         GD_GAIN_CASE(16)

@@ -93,6 +93,7 @@ struct Context {
     int gain_path = GD_GAIN_PAIR;    // gain algorithm for gd_collision / gd_step
     gd_cmatrix *cmatrix = nullptr;   // collision matrices when gain_path is a GD_GAIN_CMATRIX_*
     int gain_cb = 32;                // cells per lane row of the gain kernel (fixed per grid)
+    bool gain_cmap_smem = true;      // its box -> compact map in shared memory (else through L1)
     size_t gain_smem = 0;            // its dynamic shared memory
     // scratch owned by the context (grown on demand)
     Scratch scratch;

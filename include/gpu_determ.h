@@ -180,6 +180,10 @@ enum { GD_CMATRIX_BF16 = 0, GD_CMATRIX_BF16X3 = 1 };
 int gd_cmatrix_create(gd_ctx *ctx, int mode, gd_cmatrix **out);
 int gd_cmatrix_gain(gd_cmatrix *cm, const float *f, int ncells, int ld, float *gain, gd_stream stream);
 int gd_cmatrix_destroy(gd_cmatrix *cm);
+/* CTAs per thread-block cluster of the gain kernel (1, the default, or 2):
+ * with 2, the two CTAs of a node's adjacent cell tiles each load half of
+ * every collision-matrix tile and multicast it to both. */
+int gd_cmatrix_set_cluster(gd_cmatrix *cm, int ctas);
 /* gd_cmatrix_gain synchronises the stream and reports a pipeline time-out of
  * its kernel, except inside a stream capture; after replaying a captured
  * graph, gd_cmatrix_check (synchronising) reports it instead. */
@@ -242,11 +246,13 @@ int gd_batch_info(const gd_batch *b, int *groups, int *streams, int *graph_nodes
  * (cand_ms = -1). */
 #define GD_AUTOTUNE_MAX 8
 typedef struct {
-    int path, waves;
+    int path, waves;  /* chosen gain path; pair kernel: minimum CTAs per SM */
     float best_ms;
     int n_candidates;
     int cand_path[GD_AUTOTUNE_MAX], cand_waves[GD_AUTOTUNE_MAX];
     float cand_ms[GD_AUTOTUNE_MAX];
+    int cluster;      /* collision matrices: CTAs per cluster (1 or 2) */
+    int cand_cluster[GD_AUTOTUNE_MAX];
 } gd_autotune_result;
 int gd_ctx_autotune(gd_ctx *ctx, const float *f, int ncells, int ld, int path_mask, double mem_budget,
                     gd_autotune_result *res, gd_stream stream);

@@ -83,7 +83,7 @@ def test_autotune_picks_a_measured_candidate(gdlib, cuda):
     mask = (1 << gdlib.GAIN_PAIR) | (1 << gdlib.GAIN_CMATRIX_BF16X3)
     r = ctx.autotune(f, cells, cells, path_mask=mask, mem_budget=8e9)
     ms = [c["ms"] for c in r["candidates"]]
-    assert len(ms) == 4 and all(m > 0 for m in ms)
+    assert len(ms) == 5 and all(m > 0 for m in ms)   # pair x 3 fills, BF16x3 matrices x 2 cluster sizes
     assert r["best_ms"] == pytest.approx(min(ms))
     gain = torch.empty_like(f)
     ctx.collision(f, cells, cells, None, gain)

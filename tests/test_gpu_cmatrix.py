@@ -97,3 +97,25 @@ def test_tensor_core_loss(cuda, gdlib, n, R, ncells, ld):
     assert abs(np.mean(rel)) < 2e-5
     if ld % 4:
         assert np.array_equal(got[:, :ncells], nu_pair.cpu().numpy()[:, :ncells])
+
+
+@pytest.mark.parametrize("ncells", [200, 300, 1000])
+def test_cluster_multicast_is_bitwise_equal(cuda, gdlib, ncells):
+    """Two-CTA clusters that multicast the collision-matrix tiles give the same
+    bits as one CTA per tile (same operands, same MMA order); an odd number of
+    cell tiles is padded to whole clusters."""
+    torch = cuda
+    spec = gdlib.GridSpec(12, R=4.8)
+    ctx = gdlib.Context(spec)
+    f = torch.from_numpy(inputs.mixtures(spec.fill(), ncells, seed=5)).cuda()
+    for mode in (gdlib.CMATRIX_BF16, gdlib.CMATRIX_BF16X3):
+        cm = gdlib.CollisionMatrix(ctx, mode)
+        outs = []
+        for ctas in (1, 2):
+            cm.set_cluster(ctas)
+            g = torch.full_like(f, -1.0)
+            cm.gain(f, ncells, ncells, g)
+            outs.append(g)
+        torch.cuda.synchronize()
+        assert torch.equal(outs[0], outs[1])
+        cm.close()
