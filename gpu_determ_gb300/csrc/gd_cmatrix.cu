@@ -53,7 +53,7 @@ struct CmParams {
     int *err;        // set to 1 when a wait times out
     const int *node_off;     // [ns + 1] each node's range of stored tiles
     const uint32_t *tiles;   // stored tiles, n << 16 | k, n-major then k within each node
-    int m_tiles;             // cell tiles, padded to whole clusters
+    int m_tiles;             // cell tiles, padded to whole clusters (the grid's x extent)
 };
 
 // G_i is symmetric in (a, b), so only its block upper triangle is stored and
@@ -123,34 +123,23 @@ __global__ void __launch_bounds__(kThreads, 1)
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = tmem_base_holder;
 
-    // work units (node, CL consecutive cell tiles): unit u is node u / m_groups;
-    // the CTAs (clusters) of the persistent grid take the units round-robin, and
-    // every counter below runs on across units, so one unit's pipeline fill and
-    // last epilogue overlap its neighbours
-    const int m_groups = p.m_tiles / CL;
-    const int units = p.ns * m_groups;
-    const int cid = (int)(blockIdx.x / CL), nclusters = (int)(gridDim.x / CL);
+    // one CTA per (cell tile, node); a cluster holds adjacent cell tiles of one node
+    const int m_tile = blockIdx.x, node = blockIdx.y;
+    const int l0 = __ldg(p.node_off + node), cnt = __ldg(p.node_off + node + 1) - l0;
 
     if (warp == 0) {
         // ---- TMA producer ----------------------------------------------------
         if (lane == 0) {
             int it = 0;
-            bool stop = false;
-            for (int u = cid; u < units && !stop; u += nclusters) {
-                const int node = u / m_groups, m_tile = (u % m_groups) * CL + (int)crank;
-                const int l0 = __ldg(p.node_off + node), cnt = __ldg(p.node_off + node + 1) - l0;
+            {
                 for (int j = 0; j < cnt; j++, it++) {
                     const int s = it % S;
                     const uint32_t ph = (uint32_t)(it / S) & 1u;
                     if (!mbar_wait(smem_u32(&empty_bar[s]), ph ^ 1u, p.err)) {
                         abort_flag = 1;
-                        stop = true;
                         break;
                     }
-                    if (*(volatile int *)&abort_flag) {
-                        stop = true;
-                        break;
-                    }
+                    if (*(volatile int *)&abort_flag) break;
                     const int k = (int)(__ldg(p.tiles + l0 + j) & 0xffffu);
                     unsigned char *st = base + (size_t)s * kStage;
                     const uint32_t fb = smem_u32(&full_bar[s]);
@@ -194,9 +183,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         if (lane == 0) {
             bool ok = true;
             int it = 0, grp = 0;  // stage counter; groups of tiles sharing one b-tile n
-            for (int u = cid; u < units && ok; u += nclusters) {
-                const int node = u / m_groups;
-                const int l0 = __ldg(p.node_off + node), cnt = __ldg(p.node_off + node + 1) - l0;
+            {
                 int j = 0;
                 while (ok && j < cnt) {
                     const uint32_t n = __ldg(p.tiles + l0 + j) >> 16;
@@ -249,12 +236,10 @@ __global__ void __launch_bounds__(kThreads, 1)
         const int row = quad * 32 + lane;
         int grp = 0;
         bool failed = false;
-        for (int u = cid; u < units && !failed; u += nclusters) {
-            const int node = u / m_groups, m_tile = (u % m_groups) * CL + (int)crank;
+        {
             const int cell = m_tile * BM + row;
             const bool live = cell < p.ncells;
             float sum = 0.f;
-            const int l0 = __ldg(p.node_off + node), cnt = __ldg(p.node_off + node + 1) - l0;
             // f[b][cell] for 32 consecutive b; rows b >= ns of G are zero, so T[b] = 0
             // there and clamping b keeps every load in bounds without a branch
             const float *fcell = p.f + (live ? cell : 0);
@@ -663,10 +648,10 @@ extern "C" int gd_cmatrix_gain(gd_cmatrix *h, const float *f, int ncells, int ld
     // cell tiles padded to whole clusters: a tile past ncells reads zeros and stores nothing
     const int m_tiles = ((ncells + BM - 1) / BM + cl - 1) / cl * cl;
     CmParams prm{h->ns, h->ns_k, ncells, ld, f, gain, h->err, h->node_off, h->list, m_tiles};
-    // persistent grid: one CTA per SM (whole clusters), at most one per work unit
-    const int64_t units = (int64_t)h->ns * (m_tiles / cl);
-    const int sms = std::max(cl, h->ctx->c.sm_count / cl * cl);
-    dim3 grid((unsigned)std::min<int64_t>(sms, units * cl), 1);
+    // one CTA per (cell tile, node), cell tiles fastest so that the CTAs in flight
+    // share a few nodes' matrix tiles in L2 (a persistent grid of one CTA per SM
+    // taking the tiles round-robin measured 3-4 % slower at 20^3 / 4096 cells)
+    dim3 grid((unsigned)m_tiles, (unsigned)h->ns);
     const size_t smem = (split ? 2 * 2 * (kTileA + kTileB) : 4 * (kTileA + kTileB)) + 1024;
     void (*kern)(const CUtensorMap, const CUtensorMap, const CUtensorMap, const CUtensorMap, CmParams) =
         split ? (cl == 2 ? cmatrix_gain_kernel<3, 2> : cmatrix_gain_kernel<3, 1>)
