@@ -208,7 +208,11 @@ extern "C" int gd_surrogate_gain(gd_surrogate *s, const float *f, int ncells, in
     if ((rc = gd_mlp_check(s->net, stream))) return rc;  // synchronises the stream
     if (s->est && (rc = gd_mlp_check(s->est, stream))) return rc;
     const int count = *s->h_count;
-    if (count > 0) {
+    if (count == ncells) {
+        // every cell falls back: the plain gain straight into place (the same
+        // launch as gathering all cells in order would make)
+        if ((rc = gd_collision(s->ctx, f, ncells, ld, nullptr, gain, stream))) return rc;
+    } else if (count > 0) {
         const int64_t tot = (int64_t)s->n * count;
         gather_cells_kernel<<<grid_for(tot), 256, 0, st>>>(f, ld, s->idx, count, s->n, s->fs, count);
         GD_CUDA(cudaGetLastError());

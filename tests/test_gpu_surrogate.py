@@ -93,3 +93,23 @@ def test_cell_rel_l2(gdlib, cuda):
     gdlib.cell_rel_l2(A, 7, B, 7, 50, 7, out)
     ref = np.linalg.norm(a - b, axis=0) / np.linalg.norm(b, axis=0)
     np.testing.assert_allclose(out.cpu().numpy(), ref, rtol=1e-12)
+
+
+def test_all_cells_fall_back(setup, cuda):
+    """An estimate above tolerance everywhere sends every cell to the plain
+    path, which then runs in place: the gain is bitwise the plain gain."""
+    gd, ctx, grid, f = setup
+    torch = cuda
+    n, N = f.shape
+    net = gd.Mlp(n, n, batch_cap=256, seed=4)
+    est = gd.Mlp(n, 1, batch_cap=256, flags=0, seed=0)
+    layers = [(np.zeros((o, i)), np.zeros(o)) for o, i in M.layer_shapes(n, 1)]
+    layers[4][1][0] = 5.0          # estimate log10(error) = 5 for every cell
+    est.set_params(M.pack(layers).astype(np.float32))
+    s = gd.Surrogate(ctx, net, est, 256)
+    nu, gain = torch.empty_like(f), torch.empty_like(f)
+    assert s.gain(f, N, N, 1e-3, nu, gain) == N
+    gain_p = torch.empty_like(f)
+    ctx.collision(f, N, N, None, gain_p)
+    torch.cuda.synchronize()
+    assert torch.equal(gain, gain_p)
