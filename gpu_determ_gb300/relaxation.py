@@ -3,6 +3,7 @@
     python -m gpu_determ_gb300.relaxation [--grid 20] [--radius 4.8] [--steps 100]
                                           [--courant 0.5 | --dt DT] [--cells 1]
                                           [--init two_beam|mixture] [--seed 0]
+                                          [--gain pair|bf16|bf16x3]
 
 Each step is gd_step (loss, gain, FP64 conservation projection, f <- f + dt Q) on
 every cell; before each step the FP64 moments of f are read back and reported as
@@ -23,7 +24,9 @@ import sys
 
 import numpy as np
 
-from . import DT_COURANT, DT_FIXED, Context, GridSpec, inputs
+from . import DT_COURANT, DT_FIXED, GAIN_CMATRIX_BF16, GAIN_CMATRIX_BF16X3, GAIN_PAIR, Context, GridSpec, inputs
+
+GAIN_PATHS = {"pair": GAIN_PAIR, "bf16": GAIN_CMATRIX_BF16, "bf16x3": GAIN_CMATRIX_BF16X3}
 
 
 def moments_to_state(m5: np.ndarray) -> dict:
@@ -37,7 +40,7 @@ def moments_to_state(m5: np.ndarray) -> dict:
 
 def run(grid: int = 20, radius: float = 4.8, steps: int = 100, dt: float | None = None,
         courant: float = 0.5, cells: int = 1, init: str = "two_beam", seed: int = 0, device: int = 0,
-        callback=None):
+        callback=None, gain: str = "pair"):
     """Relax `cells` homogeneous distributions for `steps` steps with the
     Courant step (or a fixed dt when given); returns the final f (numpy
     [n_pnt][cells]) and the per-step records."""
@@ -45,6 +48,7 @@ def run(grid: int = 20, radius: float = 4.8, steps: int = 100, dt: float | None 
 
     spec = GridSpec(grid, R=radius)
     ctx = Context(spec, device=device)
+    ctx.set_gain_path(GAIN_PATHS[gain])
     g = spec.fill()
     f0 = inputs.two_beam(g, cells) if init == "two_beam" else inputs.mixtures(g, cells, seed=seed)
     f = torch.from_numpy(np.ascontiguousarray(f0)).cuda(device)
@@ -80,8 +84,9 @@ def main(argv=None):
     p.add_argument("--cells", type=int, default=1)
     p.add_argument("--init", choices=["two_beam", "mixture"], default="two_beam")
     p.add_argument("--seed", type=int, default=0)
+    p.add_argument("--gain", choices=sorted(GAIN_PATHS), default="pair")
     a = p.parse_args(argv)
-    _, recs = run(a.grid, a.radius, a.steps, a.dt, a.courant, a.cells, a.init, a.seed)
+    _, recs = run(a.grid, a.radius, a.steps, a.dt, a.courant, a.cells, a.init, a.seed, gain=a.gain)
     for r in recs:
         print(json.dumps(r))
     return 0
