@@ -161,7 +161,8 @@ extern "C" int gd_surrogate_create(gd_ctx *ctx, gd_mlp *net, gd_mlp *est, int ma
     s->est = est;
     s->n = ci.n_pnt;
     s->cap = max_cells;
-    cudaGetDevice(&s->device);
+    s->device = ctx->c.device;
+    gd::DeviceGuard dg(s->device);
     const size_t blk = (size_t)s->n * max_cells * sizeof(float);
     if (cudaMalloc(&s->est_buf, (size_t)max_cells * sizeof(float)) != cudaSuccess ||
         cudaMalloc(&s->idx, (size_t)max_cells * sizeof(int)) != cudaSuccess ||

@@ -119,8 +119,11 @@ int gd_correction_basis(gd_ctx *ctx, float *basis, gd_stream stream);
 
 /* ---- collision operator ------------------------------------------------ */
 /* Loss frequency nu[i][c] = sum_j b(|i-j|) f[j][c] and gain I[i][c] over the
- * in-sphere nodes, FP32 (either output may be NULL).  Replaces the loss and
- * gain stages of evolve_colisions (collision_integral.h:11-17,
+ * in-sphere nodes (either output may be NULL), on the context's gain path:
+ * GD_GAIN_PAIR computes both in FP32 (SIMT kernels); the collision-matrix
+ * paths compute the gain on the tensor cores and, when ld is a multiple of
+ * 4, the loss as three BF16 GEMMs (see gd_ctx_set_gain_path).  Replaces the
+ * loss and gain stages of evolve_colisions (collision_integral.h:11-17,
  * collision_integral.cu:32-188, 587-648). */
 int gd_collision(gd_ctx *ctx, const float *f, int ncells, int ld, float *nu, float *gain,
                  gd_stream stream);
