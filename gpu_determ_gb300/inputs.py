@@ -107,6 +107,58 @@ def dirichlet_mixtures(grid: dict, ncells: int, seed: int = 0, kmax: int = 4, u_
     return out
 
 
+def cavity_field_params(ncells: int, amp: float = 0.8, T_amp: float = 0.3, seed: int = 0):
+    """Cell states of a 2-D lid-driven-style field on the unit square.
+
+    Cells sit on an m x m grid, m = ceil(sqrt(ncells)), at the centres
+    ((i + 1/2)/m, (j + 1/2)/m) in row order.  The flow is divergence free,
+    from the stream function psi = sum_k a_k sin(p_k pi x) sin(q_k pi y) over
+    the modes (p, q) in {1, 2}^2 with seeded amplitudes a_k ~ N(0, 1)
+    (a_(1,1) kept positive): u = d psi / dy, v = -d psi / dx, scaled so that
+    the largest |(u, v)| over the cells is amp (so u vanishes normal to the
+    walls, as in a cavity).  The temperature is
+    T = 1 + T_amp tau / max|tau| with tau = sum_k b_k cos(p_k pi x) cos(q_k pi y),
+    b_k ~ N(0, 1).  Density 1.  Returns u [ncells][3] (w = 0) and T [ncells]."""
+    rng = np.random.default_rng(seed)
+    m = int(np.ceil(np.sqrt(max(1, ncells))))
+    c = np.arange(ncells)
+    x = (c % m + 0.5) / m
+    y = (c // m + 0.5) / m
+    modes = [(1, 1), (1, 2), (2, 1), (2, 2)]
+    a = rng.normal(0.0, 1.0, len(modes))
+    a[0] = abs(a[0]) + 1.0
+    b = rng.normal(0.0, 1.0, len(modes))
+    u = np.zeros(ncells)
+    v = np.zeros(ncells)
+    tau = np.zeros(ncells)
+    for (p, q), ak, bk in zip(modes, a, b):
+        u += ak * q * np.pi * np.sin(p * np.pi * x) * np.cos(q * np.pi * y)
+        v -= ak * p * np.pi * np.cos(p * np.pi * x) * np.sin(q * np.pi * y)
+        tau += bk * np.cos(p * np.pi * x) * np.cos(q * np.pi * y)
+    speed = np.sqrt(u * u + v * v).max()
+    scale = amp / speed if speed > 0 else 0.0
+    vel = np.stack([u * scale, v * scale, np.zeros(ncells)], axis=1)
+    tmax = np.abs(tau).max()
+    T = 1.0 + (T_amp * tau / tmax if tmax > 0 else 0.0)
+    return vel, T
+
+
+def cavity_field(grid: dict, ncells: int, amp: float = 0.8, T_amp: float = 0.3, seed: int = 0,
+                 chunk: int = 1024) -> np.ndarray:
+    """One Maxwellian M(1, u_c, T_c) per cell of cavity_field_params, in FP64
+    on the host; float32 [n_pnt][ncells]."""
+    vel, T = cavity_field_params(ncells, amp, T_amp, seed)
+    xu, xv, xw = node_velocities(grid)
+    out = np.empty((len(xu), ncells), np.float32)
+    for c0 in range(0, ncells, chunk):
+        c1 = min(ncells, c0 + chunk)
+        uu, tt = vel[c0:c1], T[c0:c1]
+        c2 = ((xu[:, None] - uu[None, :, 0]) ** 2 + (xv[:, None] - uu[None, :, 1]) ** 2
+              + (xw[:, None] - uu[None, :, 2]) ** 2)
+        out[:, c0:c1] = (np.pi * tt[None, :]) ** -1.5 * np.exp(-c2 / tt[None, :])
+    return out
+
+
 def rankine_hugoniot(mach: float = 3.0, gamma: float = 5.0 / 3.0, n1: float = 1.0, T1: float = 1.0) -> dict:
     """Upstream/downstream states of a normal shock in the convention
     f ~ n (pi T)^{-3/2} exp(-|xi - u|^2 / T), where T = 2 k T_phys / m and the

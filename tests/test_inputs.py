@@ -55,3 +55,38 @@ def test_dirichlet_mixtures():
     assert T.min() >= 0.5 and T.max() <= 2.0
     # seeded: the same seed gives the same cells
     assert np.array_equal(f, inputs.dirichlet_mixtures(g, 200, seed=3))
+
+
+def test_cavity_field():
+    vel, T = inputs.cavity_field_params(4096, amp=0.8, T_amp=0.3, seed=2)
+    speed = np.sqrt((vel ** 2).sum(axis=1))
+    assert speed.max() == pytest.approx(0.8) and np.all(vel[:, 2] == 0.0)
+    assert T.min() >= 0.7 - 1e-12 and T.max() <= 1.3 + 1e-12
+    assert T.max() == pytest.approx(1.3) or T.min() == pytest.approx(0.7)
+    # divergence free: finite-difference divergence on the 64 x 64 cell grid is
+    # small next to the velocity gradients
+    m = 64
+    u = vel[:, 0].reshape(m, m)          # [row j (y)][col i (x)]
+    v = vel[:, 1].reshape(m, m)
+    h = 1.0 / m
+    div = (u[1:-1, 2:] - u[1:-1, :-2]) / (2 * h) + (v[2:, 1:-1] - v[:-2, 1:-1]) / (2 * h)
+    grad = np.abs((u[1:-1, 2:] - u[1:-1, :-2]) / (2 * h)).max()
+    assert np.abs(div).max() < 2e-2 * grad
+    # no flow through the walls: u ~ 0 at x = 0, 1 and v ~ 0 at y = 0, 1 (cell centres h/2 in)
+    assert np.abs(u[:, 0]).max() < 0.1 and np.abs(v[0, :]).max() < 0.1
+    # seeded
+    v2, T2 = inputs.cavity_field_params(4096, seed=2)
+    assert np.array_equal(vel, v2) and np.array_equal(T, T2)
+
+
+def test_cavity_field_moments():
+    spec = GridSpec(20, R=4.8)
+    g = spec.fill()
+    f = inputs.cavity_field(g, 64, seed=1)
+    vel, T = inputs.cavity_field_params(64, seed=1)
+    xu, xv, xw = inputs.node_velocities(g)
+    d3v = float(g["steps"][3])
+    n = f.sum(axis=0) * d3v
+    assert np.allclose(n, 1.0, rtol=2e-3)
+    assert np.allclose((f * xu[:, None]).sum(axis=0) * d3v / n, vel[:, 0], atol=2e-3)
+    assert np.allclose((f * xv[:, None]).sum(axis=0) * d3v / n, vel[:, 1], atol=2e-3)
