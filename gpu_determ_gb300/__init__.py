@@ -314,7 +314,7 @@ class CollisionMatrix:
         _check(lib().gd_cmatrix_gain(self._h, _ptr(f), int(ncells), int(ld), _ptr(gain), _stream(stream)))
 
     def set_cluster(self, ctas: int):
-        """1 or 2 CTAs per cluster (2: collision-matrix tiles multicast to both)."""
+        """CTAs per tensor-core MMA: 2 (default; CTA pair, M = 256 cells) or 1."""
         _check(lib().gd_cmatrix_set_cluster(self._h, int(ctas)))
 
     def close(self):

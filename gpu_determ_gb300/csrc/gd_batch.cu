@@ -208,7 +208,7 @@ extern "C" int gd_batch_info(const gd_batch *b, int *groups, int *streams, int *
 // cells and keeps the fastest.  Candidates: the FP32 pair kernel with 1, 2 or
 // 4 CTAs per SM as the minimum s-chunk fill (trading partial-sum traffic for
 // parallelism), and the tensor-core collision matrices in BF16x3 and BF16
-// mode, each with 1 or 2 CTAs per cluster (multicast of the matrix tiles),
+// mode, each with 1 or 2 CTAs per MMA (2: CTA-pair MMA, M = 256 cells),
 // when the caller's mask admits them and their stored triangle tiles
 // (bounded by every tile of the block upper triangle) fit the memory budget.  Each candidate: one untimed run, then the median of three
 // runs timed with CUDA events on the stream.

@@ -12,13 +12,15 @@
 // Contraction: for output node i and 128 cells c,
 //   D[c][b] = sum_a F[c][a] G_i[a][b]   (tcgen05.mma, BF16 x BF16 -> FP32 in TMEM)
 //   I[i][c] = sum_b D[c][b] f[b][c]      (epilogue, FP32)
-// One CTA per (128-cell tile, i).  Warp 0 issues TMA loads of F (cells x 64 a)
-// and G_i (256 b x 64 a) into a ring of shared-memory stages (128-byte
-// swizzle); warp 1 issues the MMAs (M = 128, N = 256, K = 16) into one of two
-// TMEM accumulators; warps 2..5 read the finished accumulator with tcgen05.ld
-// and fold it into the per-cell sums while the next one is being filled.
-// Every mbarrier wait is bounded: on time-out the CTA records an error and
-// stops issuing work instead of waiting forever.
+// One CTA per (128-cell tile, i), by default two CTAs per cluster running each
+// MMA as a CTA pair (M = 256 cells).  Warp 0 issues TMA loads of F (cells x
+// 64 a) and of G_i (256 b x 64 a, or this CTA's half of it) into a ring of
+// shared-memory stages (128-byte swizzle); warp 1 issues the MMAs (N = 256,
+// K = 16) into one of two TMEM accumulators, or relays its CTA's landed
+// stages to the pair's issuing CTA; warps 2..9 read the finished accumulator
+// with tcgen05.ld and fold it into the per-cell sums while the next one is
+// being filled.  Every mbarrier wait is bounded: on time-out the CTA records
+// an error and stops issuing work instead of waiting forever.
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
@@ -38,11 +40,22 @@ namespace {
 constexpr int BM = 128;  // cells per tile (MMA M, TMEM lanes)
 constexpr int BN = 256;  // b per accumulator tile (MMA N, TMEM columns)
 constexpr int BK = 64;   // a per stage (128 bytes of BF16: one swizzle row)
-constexpr int kThreads = 192;
+constexpr int kEpiWarps = 8;  // two per TMEM lane quadrant, 128 accumulator columns each
+constexpr int kThreads = 64 + 32 * kEpiWarps;
 constexpr uint32_t kTileA = BM * BK * 2;  // 16 KB
 constexpr uint32_t kTileB = BN * BK * 2;  // 32 KB
-constexpr uint32_t kIdesc = tc::umma_idesc_bf16(BM, BN);
 using namespace tc;
+
+// Pipeline stages and bytes per stage (one CTA's share) for NPASS passes and
+// CL CTAs per MMA; 192 KB of stages in every case.
+__host__ __device__ constexpr int cm_stages(int npass, int cl)
+{
+    return cl == 2 ? (npass == 1 ? 6 : 3) : (npass == 1 ? 4 : 2);
+}
+__host__ __device__ constexpr uint32_t cm_stage_bytes(int npass, int cl)
+{
+    return (npass == 1 ? 1u : 2u) * (kTileA + kTileB / (uint32_t)cl);
+}
 
 struct CmParams {
     int ns;       // in-sphere nodes
@@ -67,9 +80,12 @@ __host__ __device__ __forceinline__ int k_end(int n, int num_k)
 }
 
 // NPASS = 1: D = F_hi G_hi.  NPASS = 3: D = F_hi G_hi + F_hi G_lo + F_lo G_hi.
-// CL = 2: a cluster of two CTAs holding adjacent cell tiles of the same node;
-// each loads half of every G tile (BN / 2 rows) and multicasts it to both, so
-// the node's tiles cross L2 once per cluster instead of once per CTA.
+// CL = 2: a CTA pair (cluster of two) holding adjacent cell tiles of the same
+// node runs each tile as one pair MMA (tcgen05 cta_group::2, M = 256 cells):
+// each CTA loads its own F tile and half of the G tile (BN / 2 rows), the even
+// CTA issues the MMAs, and each CTA's tensor memory receives its own cells'
+// rows.  A CTA then brings 32 KB per tile into its shared memory instead of
+// 48 KB, and a G tile crosses L2 once per pair.
 template <int NPASS, int CL>
 __global__ void __launch_bounds__(kThreads, 1)
     cmatrix_gain_kernel(const __grid_constant__ CUtensorMap tmFh, const __grid_constant__ CUtensorMap tmFl,
@@ -77,8 +93,12 @@ __global__ void __launch_bounds__(kThreads, 1)
                         CmParams p)
 {
     constexpr int NPARTS = NPASS == 1 ? 1 : 2;
-    constexpr int S = NPASS == 1 ? 4 : 2;  // pipeline stages
-    constexpr uint32_t kStage = NPARTS * (kTileA + kTileB);
+    constexpr bool PAIR = CL == 2;
+    constexpr uint32_t kTileBc = kTileB / CL;  // this CTA's rows of a G tile
+    constexpr int S = cm_stages(NPASS, CL);  // pipeline stages
+    constexpr uint32_t kStage = cm_stage_bytes(NPASS, CL);
+    static_assert(kStage == NPARTS * (kTileA + kTileBc), "stage layout");
+    constexpr uint32_t kIdescT = umma_idesc_bf16(BM * CL, BN);
     extern __shared__ __align__(1024) unsigned char dsmem[];
     // 1024-byte aligned tile area
     unsigned char *base = reinterpret_cast<unsigned char *>(
@@ -86,91 +106,77 @@ __global__ void __launch_bounds__(kThreads, 1)
     __shared__ __align__(8) uint64_t full_bar[S], empty_bar[S], accf_bar[2], acce_bar[2];
     __shared__ uint32_t tmem_base_holder;
     __shared__ int abort_flag;
+    __shared__ int epi_failed;
+    __shared__ float half_sum[BM];
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
-    if (CL == 1) {
+    if (!PAIR) {
         if (threadIdx.x == 0) abort_flag = *(volatile int *)p.err;
         __syncthreads();
         if (abort_flag) return;  // an earlier CTA timed out: do no work
     } else {
-        // clustered CTAs never leave early: both must reach the cluster barriers
+        // paired CTAs never leave early: both must reach the cluster barriers
         if (threadIdx.x == 0) abort_flag = 0;
     }
-    const uint16_t cta_mask = (uint16_t)((1u << CL) - 1u);
-    const uint32_t crank = CL > 1 ? cluster_rank() : 0u;
+    if (threadIdx.x == 0) epi_failed = 0;
+    const uint32_t crank = PAIR ? cluster_rank() : 0u;
+    const bool leader = crank == 0;
     if (threadIdx.x == 0) {
         for (int s = 0; s < S; s++) {
-            mbar_init(smem_u32(&full_bar[s]), 1);
-            mbar_init(smem_u32(&empty_bar[s]), CL);  // released by the MMA of every CTA that reads it
+            // the even CTA's full barrier also takes the odd CTA's relay arrival
+            mbar_init(smem_u32(&full_bar[s]), (PAIR && leader) ? 2 : 1);
+            mbar_init(smem_u32(&empty_bar[s]), 1);  // the MMA commit
         }
         for (int b = 0; b < 2; b++) {
             mbar_init(smem_u32(&accf_bar[b]), 1);
-            mbar_init(smem_u32(&acce_bar[b]), 4);  // one arrival per epilogue warp
+            mbar_init(smem_u32(&acce_bar[b]), CL * kEpiWarps);  // every epilogue warp of the pair
         }
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     if (warp == 1) {
-        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
-                         smem_u32(&tmem_base_holder)),
-                     "r"(2 * BN)
-                     : "memory");
-        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+        tmem_alloc<CL>(smem_u32(&tmem_base_holder), 2 * BN);
         asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     }
     __syncthreads();
-    if (CL > 1) cluster_sync();  // the peer's barriers exist before any multicast or commit reaches them
+    if (PAIR) cluster_sync();  // the peer's barriers exist before any arrival or commit reaches them
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = tmem_base_holder;
 
-    // one CTA per (cell tile, node); a cluster holds adjacent cell tiles of one node
+    // one CTA per (cell tile, node); a pair holds adjacent cell tiles of one node
     const int m_tile = blockIdx.x, node = blockIdx.y;
     const int l0 = __ldg(p.node_off + node), cnt = __ldg(p.node_off + node + 1) - l0;
 
     if (warp == 0) {
-        // ---- TMA producer ----------------------------------------------------
+        // ---- TMA producer (both CTAs; each fills its own stages) ---------------
         if (lane == 0) {
             int it = 0;
-            {
-                for (int j = 0; j < cnt; j++, it++) {
-                    const int s = it % S;
-                    const uint32_t ph = (uint32_t)(it / S) & 1u;
-                    if (!mbar_wait(smem_u32(&empty_bar[s]), ph ^ 1u, p.err)) {
-                        abort_flag = 1;
-                        break;
-                    }
-                    if (*(volatile int *)&abort_flag) break;
-                    const int k = (int)(__ldg(p.tiles + l0 + j) & 0xffffu);
-                    unsigned char *st = base + (size_t)s * kStage;
-                    const uint32_t fb = smem_u32(&full_bar[s]);
-                    mbar_expect_tx(fb, kStage);
-                    tma_load_2d(smem_u32(st), &tmFh, k * BK, m_tile * BM, fb);
-                    // stored tile l0 + j ([slot][BN rows][BK]); with CL > 1 this CTA's
-                    // share of its rows, multicast into the same place in every CTA
-                    if (CL == 1) {
-                        tma_load_3d(smem_u32(st + kTileA), &tmGh, 0, 0, l0 + j, fb);
-                    } else {
-                        const uint32_t part = crank * (kTileB / CL);
-                        tma_load_3d_mc(smem_u32(st + kTileA) + part, &tmGh, 0, (int)crank * (BN / CL), l0 + j, fb,
-                                       cta_mask);
-                    }
-                    if (NPARTS == 2) {
-                        tma_load_2d(smem_u32(st + kTileA + kTileB), &tmFl, k * BK, m_tile * BM, fb);
-                        if (CL == 1) {
-                            tma_load_3d(smem_u32(st + 2 * kTileA + kTileB), &tmGl, 0, 0, l0 + j, fb);
-                        } else {
-                            const uint32_t part = crank * (kTileB / CL);
-                            tma_load_3d_mc(smem_u32(st + 2 * kTileA + kTileB) + part, &tmGl, 0,
-                                           (int)crank * (BN / CL), l0 + j, fb, cta_mask);
-                        }
-                    }
+            for (int j = 0; j < cnt; j++, it++) {
+                const int s = it % S;
+                const uint32_t ph = (uint32_t)(it / S) & 1u;
+                if (!mbar_wait(smem_u32(&empty_bar[s]), ph ^ 1u, p.err)) {
+                    abort_flag = 1;
+                    break;
+                }
+                if (*(volatile int *)&abort_flag) break;
+                const int k = (int)(__ldg(p.tiles + l0 + j) & 0xffffu);
+                unsigned char *st = base + (size_t)s * kStage;
+                const uint32_t fb = smem_u32(&full_bar[s]);
+                mbar_expect_tx(fb, kStage);
+                // F: this CTA's cells; G: stored tile l0 + j ([slot][BN rows][BK]),
+                // this CTA's BN / CL rows of it
+                tma_load_2d(smem_u32(st), &tmFh, k * BK, m_tile * BM, fb);
+                tma_load_3d(smem_u32(st + kTileA), &tmGh, 0, (int)crank * (BN / CL), l0 + j, fb);
+                if (NPARTS == 2) {
+                    tma_load_2d(smem_u32(st + kTileA + kTileBc), &tmFl, k * BK, m_tile * BM, fb);
+                    tma_load_3d(smem_u32(st + 2 * kTileA + kTileBc), &tmGl, 0, (int)crank * (BN / CL), l0 + j, fb);
                 }
             }
-            if (CL > 1) {
+            if (PAIR) {
                 // tail, bounded like every wait: the copies of the last stages have
-                // landed here, and every stage was released by the MMA of both CTAs
-                // (their commits have arrived here), before this CTA may leave the
-                // cluster; after a time-out the waits give up at once
+                // landed, and the pair MMAs that read them have completed (their
+                // commits have arrived here), before this CTA may leave the pair;
+                // after a time-out the waits give up at once
                 const int j0 = it > S ? it - S : 0;
                 for (int j = j0; j < it; j++)
                     if (!mbar_wait(smem_u32(&full_bar[j % S]), (uint32_t)(j / S) & 1u, p.err)) break;
@@ -178,118 +184,150 @@ __global__ void __launch_bounds__(kThreads, 1)
                     if (!mbar_wait(smem_u32(&empty_bar[j % S]), (uint32_t)(j / S) & 1u, p.err)) break;
             }
         }
+    } else if (warp == 1 && PAIR && !leader) {
+        // ---- relay (odd CTA): its stage s has landed -> arrive on the even CTA's
+        // full barrier, so the pair MMA reads both halves only when both are in
+        if (lane == 0) {
+            for (int it = 0; it < cnt; it++) {
+                const int s = it % S;
+                if (!mbar_wait(smem_u32(&full_bar[s]), (uint32_t)(it / S) & 1u, p.err)) break;
+                mbar_arrive_cluster(mapa_cluster(smem_u32(&full_bar[s]), 0));
+            }
+        }
     } else if (warp == 1) {
-        // ---- MMA issuer --------------------------------------------------------
+        // ---- MMA issuer (one CTA, or the even CTA of a pair) --------------------
         if (lane == 0) {
             bool ok = true;
             int it = 0, grp = 0;  // stage counter; groups of tiles sharing one b-tile n
-            {
-                int j = 0;
-                while (ok && j < cnt) {
-                    const uint32_t n = __ldg(p.tiles + l0 + j) >> 16;
-                    const int buf = grp & 1;
-                    const uint32_t use = (uint32_t)(grp >> 1);
-                    if (!mbar_wait(smem_u32(&acce_bar[buf]), (use & 1u) ^ 1u, p.err)) {
+            int j = 0;
+            while (ok && j < cnt) {
+                const uint32_t n = __ldg(p.tiles + l0 + j) >> 16;
+                const int buf = grp & 1;
+                const uint32_t use = (uint32_t)(grp >> 1);
+                if (!mbar_wait(smem_u32(&acce_bar[buf]), (use & 1u) ^ 1u, p.err)) {
+                    ok = false;
+                    break;
+                }
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                const uint32_t d_tmem = tmem + (uint32_t)(buf * BN);
+                bool first = true;
+                for (; j < cnt && (__ldg(p.tiles + l0 + j) >> 16) == n; j++, it++) {
+                    const int s = it % S;
+                    const uint32_t ph = (uint32_t)(it / S) & 1u;
+                    if (!mbar_wait(smem_u32(&full_bar[s]), ph, p.err)) {
                         ok = false;
                         break;
                     }
                     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-                    const uint32_t d_tmem = tmem + (uint32_t)(buf * BN);
-                    bool first = true;
-                    for (; j < cnt && (__ldg(p.tiles + l0 + j) >> 16) == n; j++, it++) {
-                        const int s = it % S;
-                        const uint32_t ph = (uint32_t)(it / S) & 1u;
-                        if (!mbar_wait(smem_u32(&full_bar[s]), ph, p.err)) {
-                            ok = false;
-                            break;
-                        }
-                        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-                        const uint32_t st = smem_u32(base + (size_t)s * kStage);
-                        const uint32_t aH = st, bH = st + kTileA;
-                        const uint32_t aL = st + kTileA + kTileB, bL = st + 2 * kTileA + kTileB;
+                    const uint32_t st = smem_u32(base + (size_t)s * kStage);
+                    const uint32_t aH = st, bH = st + kTileA;
+                    const uint32_t aL = st + kTileA + kTileBc, bL = st + 2 * kTileA + kTileBc;
 #pragma unroll
-                        for (int kk = 0; kk < BK / 16; kk++) {
-                            const uint32_t off = (uint32_t)kk * 32u;  // 16 BF16 along K
-                            const uint32_t acc = (!first || kk > 0) ? 1u : 0u;
-                            umma_bf16(d_tmem, umma_desc(aH + off), umma_desc(bH + off), kIdesc, acc);
+                    for (int kk = 0; kk < BK / 16; kk++) {
+                        const uint32_t off = (uint32_t)kk * 32u;  // 16 BF16 along K
+                        const uint32_t acc = (!first || kk > 0) ? 1u : 0u;
+                        if (PAIR) {
+                            umma_bf16_pair(d_tmem, umma_desc(aH + off), umma_desc(bH + off), kIdescT, acc);
                             if (NPASS == 3) {
-                                umma_bf16(d_tmem, umma_desc(aH + off), umma_desc(bL + off), kIdesc, 1u);
-                                umma_bf16(d_tmem, umma_desc(aL + off), umma_desc(bH + off), kIdesc, 1u);
+                                umma_bf16_pair(d_tmem, umma_desc(aH + off), umma_desc(bL + off), kIdescT, 1u);
+                                umma_bf16_pair(d_tmem, umma_desc(aL + off), umma_desc(bH + off), kIdescT, 1u);
+                            }
+                        } else {
+                            umma_bf16(d_tmem, umma_desc(aH + off), umma_desc(bH + off), kIdescT, acc);
+                            if (NPASS == 3) {
+                                umma_bf16(d_tmem, umma_desc(aH + off), umma_desc(bL + off), kIdescT, 1u);
+                                umma_bf16(d_tmem, umma_desc(aL + off), umma_desc(bH + off), kIdescT, 1u);
                             }
                         }
-                        if (CL == 1)
-                            umma_commit(smem_u32(&empty_bar[s]));
-                        else
-                            umma_commit_mc(smem_u32(&empty_bar[s]), cta_mask);
-                        first = false;
                     }
-                    if (!ok) break;
-                    umma_commit(smem_u32(&accf_bar[buf]));
-                    grp++;
+                    // the stage is free in both CTAs once these MMAs have read it
+                    if (PAIR)
+                        umma_commit_pair_mc(smem_u32(&empty_bar[s]), (uint16_t)3u);
+                    else
+                        umma_commit(smem_u32(&empty_bar[s]));
+                    first = false;
                 }
+                if (!ok) break;
+                if (PAIR)
+                    umma_commit_pair_mc(smem_u32(&accf_bar[buf]), (uint16_t)3u);
+                else
+                    umma_commit(smem_u32(&accf_bar[buf]));
+                grp++;
             }
             if (!ok) abort_flag = 1;
         }
-    } else {
-        // ---- epilogue: warps 2..5 own TMEM lane quadrants (warp % 4) -------------
+    } else if (warp >= 2) {
+        // ---- epilogue: warps 2..9; warp % 4 is the TMEM lane quadrant it may
+        // read, (warp - 2) / 4 the half of the accumulator columns it takes ---
         const int quad = warp & 3;
+        const int half = (warp - 2) >> 2;
         const int row = quad * 32 + lane;
         int grp = 0;
         bool failed = false;
-        {
-            const int cell = m_tile * BM + row;
-            const bool live = cell < p.ncells;
-            float sum = 0.f;
-            // f[b][cell] for 32 consecutive b; rows b >= ns of G are zero, so T[b] = 0
-            // there and clamping b keeps every load in bounds without a branch
-            const float *fcell = p.f + (live ? cell : 0);
-            float fv[32], fn[32];
-            auto load_f = [&](float *dst, int b0) {
+        const int cell = m_tile * BM + row;
+        const bool live = cell < p.ncells;
+        float sum = 0.f;
+        // f[b][cell] for this warp's 128 b of a group; rows b >= ns of G are
+        // zero, so T[b] = 0 there and clamping b keeps every load in bounds
+        // without a branch.  A group's values are requested as soon as the
+        // previous group is folded, so they arrive while its MMAs run.
+        const float *fcell = p.f + (live ? cell : 0);
+        float fv[BN / 2];
+        auto load_f = [&](int b0) {
 #pragma unroll
-                for (int q = 0; q < 32; q++) dst[q] = __ldg(fcell + (size_t)min(b0 + q, p.ns - 1) * p.ld);
-            };
-            for (int j = 0; j < cnt; grp++) {
-                // b-tiles without stored tiles contribute nothing and are skipped
-                const int n = (int)(__ldg(p.tiles + l0 + j) >> 16);
-                while (j < cnt && (int)(__ldg(p.tiles + l0 + j) >> 16) == n) j++;
-                const int buf = grp & 1;
-                const uint32_t use = (uint32_t)(grp >> 1);
-                // the first chunk's f loads overlap the wait for the accumulator
-                if (live) load_f(fv, n * BN);
-                bool ok = true;
-                if (lane == 0) ok = mbar_wait(smem_u32(&accf_bar[buf]), use & 1u, p.err);
-                ok = __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
-                if (!ok) {
-                    failed = true;
-                    break;
-                }
-                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-                const uint32_t taddr = tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(buf * BN);
-#pragma unroll
-                for (int c0 = 0; c0 < BN; c0 += 32) {
-                    float v[32];
-                    tmem_ld32(taddr + (uint32_t)c0, v);
-                    // next chunk's loads are in flight during this chunk's FMAs
-                    if (live && c0 + 32 < BN) load_f(fn, n * BN + c0 + 32);
-                    if (live) {
-#pragma unroll
-                        for (int q = 0; q < 32; q++) sum = __fmaf_rn(v[q], fv[q], sum);
-                    }
-#pragma unroll
-                    for (int q = 0; q < 32; q++) fv[q] = fn[q];
-                }
-                asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-                __syncwarp();
-                if (lane == 0) mbar_arrive(smem_u32(&acce_bar[buf]));
+            for (int q = 0; q < BN / 2; q++) fv[q] = __ldg(fcell + (size_t)min(b0 + q, p.ns - 1) * p.ld);
+        };
+        int j = 0;
+        int n = cnt > 0 ? (int)(__ldg(p.tiles + l0) >> 16) : 0;
+        if (live && cnt > 0) load_f(n * BN + half * (BN / 2));
+        for (; j < cnt; grp++) {
+            // b-tiles without stored tiles contribute nothing and are skipped
+            while (j < cnt && (int)(__ldg(p.tiles + l0 + j) >> 16) == n) j++;
+            const int n_next = j < cnt ? (int)(__ldg(p.tiles + l0 + j) >> 16) : -1;
+            const int buf = grp & 1;
+            const uint32_t use = (uint32_t)(grp >> 1);
+            bool ok = true;
+            if (lane == 0) ok = mbar_wait(smem_u32(&accf_bar[buf]), use & 1u, p.err);
+            ok = __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
+            if (!ok) {
+                failed = true;
+                break;
             }
-            if (!failed && live) p.gain[(size_t)node * p.ld + cell] = sum;
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const uint32_t taddr =
+                tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(buf * BN) + (uint32_t)(half * (BN / 2));
+#pragma unroll
+            for (int c0 = 0; c0 < BN / 2; c0 += 16) {
+                float v[16];
+                tmem_ld16(taddr + (uint32_t)c0, v);
+                if (live) {
+#pragma unroll
+                    for (int q = 0; q < 16; q++) sum = __fmaf_rn(v[q], fv[c0 + q], sum);
+                }
+            }
+            asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+            __syncwarp();
+            // report the drained accumulator to the MMA issuer's CTA
+            if (lane == 0) {
+                if (PAIR)
+                    mbar_arrive_cluster(mapa_cluster(smem_u32(&acce_bar[buf]), 0));
+                else
+                    mbar_arrive(smem_u32(&acce_bar[buf]));
+            }
+            if (live && n_next >= 0) load_f(n_next * BN + half * (BN / 2));
+            n = n_next;
         }
+        // the two column halves of a cell are added in a fixed order
+        if (failed) epi_failed = 1;
+        if (half == 1) half_sum[row] = sum;
+        asm volatile("bar.sync 1, %0;" ::"n"(32 * kEpiWarps) : "memory");
+        if (half == 0 && live && !epi_failed) p.gain[(size_t)node * p.ld + cell] = sum + half_sum[row];
     }
     __syncthreads();
-    if (CL > 1) cluster_sync();  // no remote write or arrival can reach this CTA after it leaves
+    if (PAIR) cluster_sync();  // no remote write or arrival can reach this CTA after it leaves
     if (warp == 1) {
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * BN) : "memory");
+        tmem_dealloc<CL>(tmem, 2 * BN);
     }
 }
 
@@ -445,7 +483,7 @@ struct gd_cmatrix {
     int mode = 0;  // GD_CMATRIX_BF16 or GD_CMATRIX_BF16X3
     int ns = 0, ns_k = 0;
     int tiles = 0;       // BN x BK tiles of one node's block upper triangle
-    int cluster = 1;     // CTAs per cluster sharing each G tile by multicast (1 or 2)
+    int cluster = 2;     // CTAs per MMA: 2 (CTA-pair MMA, M = 256 cells; the default) or 1
     int64_t slots = 0;   // stored (not all-zero) tiles over all nodes
     int *node_off = nullptr;    // [ns + 1] into list
     uint32_t *list = nullptr;   // stored tiles per node, n << 16 | k
@@ -633,7 +671,7 @@ extern "C" int gd_cmatrix_gain(gd_cmatrix *h, const float *f, int ncells, int ld
     const cuuint32_t fbox[2] = {BK, BM};
     const cuuint64_t gdims[3] = {(cuuint64_t)BK, (cuuint64_t)BN, (cuuint64_t)std::max<int64_t>(h->slots, 1)};
     const cuuint64_t gstr[2] = {(cuuint64_t)BK * 2, (cuuint64_t)BN * BK * 2};
-    // with a 2-CTA cluster each CTA loads (and multicasts) half of a G tile
+    // with a CTA pair each CTA loads half of a G tile
     const int cl = (h->cluster == 2 && ncells > BM) ? 2 : 1;
     const cuuint32_t gbox[3] = {BK, (cuuint32_t)(BN / cl), 1};
     if ((rc = encode(enc, &tFh, h->fh, 2, fdims, fstr, fbox))) return rc;
@@ -652,7 +690,8 @@ extern "C" int gd_cmatrix_gain(gd_cmatrix *h, const float *f, int ncells, int ld
     // share a few nodes' matrix tiles in L2 (a persistent grid of one CTA per SM
     // taking the tiles round-robin measured 3-4 % slower at 20^3 / 4096 cells)
     dim3 grid((unsigned)m_tiles, (unsigned)h->ns);
-    const size_t smem = (split ? 2 * 2 * (kTileA + kTileB) : 4 * (kTileA + kTileB)) + 1024;
+    const int npass = split ? 3 : 1;
+    const size_t smem = (size_t)cm_stages(npass, cl) * cm_stage_bytes(npass, cl) + 1024;
     void (*kern)(const CUtensorMap, const CUtensorMap, const CUtensorMap, const CUtensorMap, CmParams) =
         split ? (cl == 2 ? cmatrix_gain_kernel<3, 2> : cmatrix_gain_kernel<3, 1>)
               : (cl == 2 ? cmatrix_gain_kernel<1, 2> : cmatrix_gain_kernel<1, 1>);

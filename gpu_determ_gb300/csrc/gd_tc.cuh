@@ -74,33 +74,28 @@ __device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap *map
         : "memory");
 }
 
-__device__ __forceinline__ void tma_load_4d(uint32_t dst, const CUtensorMap *map, int c0, int c1, int c2, int c3,
-                                            uint32_t bar)
-{
-    asm volatile(
-        "cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], [%6];"
-        ::"r"(dst), "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(bar)
-        : "memory");
-}
-
-// Multicast variant: the box lands at the same shared-memory offset in every
-// CTA of the cluster named in cta_mask, each CTA's mbarrier at `bar` receiving
-// the complete_tx of the bytes written there.
-__device__ __forceinline__ void tma_load_3d_mc(uint32_t dst, const CUtensorMap *map, int c0, int c1, int c2,
-                                               uint32_t bar, uint16_t cta_mask)
-{
-    asm volatile(
-        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes.multicast::cluster"
-        " [%0], [%1, {%2, %3, %4}], [%5], %6;"
-        ::"r"(dst), "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(bar), "h"(cta_mask)
-        : "memory");
-}
-
 __device__ __forceinline__ uint32_t cluster_rank()
 {
     uint32_t r;
     asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
     return r;
+}
+
+// shared::cluster address of the location at shared::cta address `addr` in
+// CTA `rank` of this cluster.
+__device__ __forceinline__ uint32_t mapa_cluster(uint32_t addr, uint32_t rank)
+{
+    uint32_t r;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(addr), "r"(rank));
+    return r;
+}
+
+// Arrive on an mbarrier of any CTA of the cluster (default semantics, as for
+// a local arrive: no cluster-scope fence on the hot path; the tcgen05 fences
+// around the barrier order the tensor-core work on either side).
+__device__ __forceinline__ void mbar_arrive_cluster(uint32_t bar_cluster)
+{
+    asm volatile("mbarrier.arrive.shared::cluster.b64 _, [%0];" ::"r"(bar_cluster) : "memory");
 }
 
 // All threads of all CTAs of the cluster (release/acquire).
@@ -144,14 +139,70 @@ __device__ __forceinline__ void umma_commit(uint32_t bar)
                  : "memory");
 }
 
-// Arrive once on the mbarrier at `bar` in every CTA of cta_mask when the
-// issuing thread's earlier tcgen05 operations complete.
-__device__ __forceinline__ void umma_commit_mc(uint32_t bar, uint16_t cta_mask)
+// CTA-pair forms (cta_group::2).  A kernel uses one cta_group for all its
+// tcgen05 instructions.  The MMA is issued by one thread of the pair's even
+// CTA: M = 256 rows, A's rows 0..127 from the even CTA's shared memory and
+// 128..255 from the odd CTA's (same offset), B's N columns split in halves
+// the same way; each CTA's tensor memory receives its own 128 rows of D.
+__device__ __forceinline__ void umma_bf16_pair(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                               uint32_t accum)
 {
     asm volatile(
-        "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 [%0], %1;"
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::2.kind::f16 [%0], %1, %2, %3, p;\n\t}"
+        ::"r"(d_tmem), "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accum)
+        : "memory");
+}
+
+// Arrive once on the mbarrier at `bar` in every CTA of cta_mask when the
+// pair MMAs issued so far by this thread complete.
+__device__ __forceinline__ void umma_commit_pair_mc(uint32_t bar, uint16_t cta_mask)
+{
+    asm volatile(
+        "tcgen05.commit.cta_group::2.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 [%0], %1;"
         ::"r"(bar), "h"(cta_mask)
         : "memory");
+}
+
+// Tensor-memory allocation for CG = 1 (this CTA) or CG = 2 (one warp of each
+// CTA of the pair executes it collectively); whole warp, address to `holder`.
+template <int CG>
+__device__ __forceinline__ void tmem_alloc(uint32_t holder, uint32_t cols)
+{
+    if (CG == 1) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(holder), "r"(cols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    } else {
+        asm volatile("tcgen05.alloc.cta_group::2.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(holder), "r"(cols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::2.sync.aligned;" ::: "memory");
+    }
+}
+
+template <int CG>
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t cols)
+{
+    if (CG == 1)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(cols) : "memory");
+    else
+        asm volatile("tcgen05.dealloc.cta_group::2.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(cols) : "memory");
+}
+
+// 16 consecutive columns of this warp's 32 lanes (one lane per thread).
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float *v)
+{
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+        "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int j = 0; j < 16; j++) v[j] = __uint_as_float(r[j]);
 }
 
 __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float *v)

@@ -183,9 +183,10 @@ enum { GD_CMATRIX_BF16 = 0, GD_CMATRIX_BF16X3 = 1 };
 int gd_cmatrix_create(gd_ctx *ctx, int mode, gd_cmatrix **out);
 int gd_cmatrix_gain(gd_cmatrix *cm, const float *f, int ncells, int ld, float *gain, gd_stream stream);
 int gd_cmatrix_destroy(gd_cmatrix *cm);
-/* CTAs per thread-block cluster of the gain kernel (1, the default, or 2):
- * with 2, the two CTAs of a node's adjacent cell tiles each load half of
- * every collision-matrix tile and multicast it to both. */
+/* CTAs per tensor-core MMA of the gain kernel: 2 (the default) or 1.  With
+ * 2, the CTAs of a node's two adjacent 128-cell tiles form a cluster and run
+ * each MMA as a CTA pair (M = 256 cells): each loads its own cells and half
+ * of every collision-matrix tile.  Results are bitwise the same either way. */
 int gd_cmatrix_set_cluster(gd_cmatrix *cm, int ctas);
 /* gd_cmatrix_gain synchronises the stream and reports a pipeline time-out of
  * its kernel, except inside a stream capture; after replaying a captured

@@ -100,10 +100,11 @@ def test_tensor_core_loss(cuda, gdlib, n, R, ncells, ld):
 
 
 @pytest.mark.parametrize("ncells", [200, 300, 1000])
-def test_cluster_multicast_is_bitwise_equal(cuda, gdlib, ncells):
-    """Two-CTA clusters that multicast the collision-matrix tiles give the same
-    bits as one CTA per tile (same operands, same MMA order); an odd number of
-    cell tiles is padded to whole clusters."""
+def test_cta_pair_is_bitwise_equal(cuda, gdlib, ncells):
+    """CTA-pair MMAs (M = 256 cells over two CTAs, each loading half of every
+    collision-matrix tile) give the same bits as one CTA per 128-cell tile
+    (same operands, same MMA order, same epilogue); an odd number of cell
+    tiles is padded to whole pairs."""
     torch = cuda
     spec = gdlib.GridSpec(12, R=4.8)
     ctx = gdlib.Context(spec)
