@@ -46,15 +46,31 @@ constexpr uint32_t kTileA = BM * BK * 2;  // 16 KB
 constexpr uint32_t kTileB = BN * BK * 2;  // 32 KB
 using namespace tc;
 
-// Pipeline stages and bytes per stage (one CTA's share) for NPASS passes and
-// CL CTAs per MMA; 192 KB of stages in every case.
-__host__ __device__ constexpr int cm_stages(int npass, int cl)
+// Ring of shared-memory stages (192 KB) for NPASS passes and CL CTAs per
+// MMA.  A stage holds cm_tiles_per_stage consecutive stored tiles of one
+// b-tile group, each tile its F tile(s) and this CTA's rows of its G
+// tile(s).  One-pass CTA pairs put two tiles in a stage: their stream was
+// bound by the handshakes per stage (full/empty barriers, relay), not by the
+// bytes, and two tiles per stage (three stages) run at the tensor pipe's rate
+// where one tile (six stages) reached 86 % of it; one CTA per MMA keeps one
+// tile per stage (its 48 KB tiles would leave only two stages).
+__host__ __device__ constexpr int cm_tiles_per_stage(int npass, int cl) { return npass == 1 && cl == 2 ? 2 : 1; }
+__host__ __device__ constexpr uint32_t cm_tile_bytes(int npass, int cl)
 {
-    return cl == 2 ? (npass == 1 ? 6 : 3) : (npass == 1 ? 4 : 2);
+    return (npass == 1 ? 1u : 2u) * (kTileA + kTileB / (uint32_t)cl);
 }
 __host__ __device__ constexpr uint32_t cm_stage_bytes(int npass, int cl)
 {
-    return (npass == 1 ? 1u : 2u) * (kTileA + kTileB / (uint32_t)cl);
+    return (uint32_t)cm_tiles_per_stage(npass, cl) * cm_tile_bytes(npass, cl);
+}
+__host__ __device__ constexpr int cm_stages(int npass, int cl) { return (int)((192u << 10) / cm_stage_bytes(npass, cl)); }
+
+// Stored tiles in the stage that starts at list entry j of a node's cnt
+// tiles: two when allowed and entry j + 1 belongs to the same b-tile group.
+__device__ __forceinline__ int stage_len(const uint32_t *tiles, int j, int cnt, int tps)
+{
+    if (tps == 1 || j + 1 >= cnt) return 1;
+    return (__ldg(tiles + j) >> 16) == (__ldg(tiles + j + 1) >> 16) ? 2 : 1;
 }
 
 struct CmParams {
@@ -96,8 +112,10 @@ __global__ void __launch_bounds__(kThreads, 1)
     constexpr bool PAIR = CL == 2;
     constexpr uint32_t kTileBc = kTileB / CL;  // this CTA's rows of a G tile
     constexpr int S = cm_stages(NPASS, CL);  // pipeline stages
+    constexpr int TPS = cm_tiles_per_stage(NPASS, CL);
+    constexpr uint32_t kTileSlot = cm_tile_bytes(NPASS, CL);
     constexpr uint32_t kStage = cm_stage_bytes(NPASS, CL);
-    static_assert(kStage == NPARTS * (kTileA + kTileBc), "stage layout");
+    static_assert(kTileSlot == NPARTS * (kTileA + kTileBc) && S >= 2, "stage layout");
     constexpr uint32_t kIdescT = umma_idesc_bf16(BM * CL, BN);
     extern __shared__ __align__(1024) unsigned char dsmem[];
     // 1024-byte aligned tile area
@@ -150,8 +168,9 @@ __global__ void __launch_bounds__(kThreads, 1)
     if (warp == 0) {
         // ---- TMA producer (both CTAs; each fills its own stages) ---------------
         if (lane == 0) {
+            const uint32_t *tl = p.tiles + l0;
             int it = 0;
-            for (int j = 0; j < cnt; j++, it++) {
+            for (int j = 0; j < cnt; it++) {
                 const int s = it % S;
                 const uint32_t ph = (uint32_t)(it / S) & 1u;
                 if (!mbar_wait(smem_u32(&empty_bar[s]), ph ^ 1u, p.err)) {
@@ -159,18 +178,24 @@ __global__ void __launch_bounds__(kThreads, 1)
                     break;
                 }
                 if (*(volatile int *)&abort_flag) break;
-                const int k = (int)(__ldg(p.tiles + l0 + j) & 0xffffu);
+                const int len = stage_len(tl, j, cnt, TPS);
                 unsigned char *st = base + (size_t)s * kStage;
                 const uint32_t fb = smem_u32(&full_bar[s]);
-                mbar_expect_tx(fb, kStage);
-                // F: this CTA's cells; G: stored tile l0 + j ([slot][BN rows][BK]),
-                // this CTA's BN / CL rows of it
-                tma_load_2d(smem_u32(st), &tmFh, k * BK, m_tile * BM, fb);
-                tma_load_3d(smem_u32(st + kTileA), &tmGh, 0, (int)crank * (BN / CL), l0 + j, fb);
-                if (NPARTS == 2) {
-                    tma_load_2d(smem_u32(st + kTileA + kTileBc), &tmFl, k * BK, m_tile * BM, fb);
-                    tma_load_3d(smem_u32(st + 2 * kTileA + kTileBc), &tmGl, 0, (int)crank * (BN / CL), l0 + j, fb);
+                mbar_expect_tx(fb, (uint32_t)len * kTileSlot);
+                for (int t = 0; t < len; t++) {
+                    // F: this CTA's cells; G: stored tile l0 + j + t ([slot][BN rows][BK]),
+                    // this CTA's BN / CL rows of it
+                    const int k = (int)(__ldg(tl + j + t) & 0xffffu);
+                    unsigned char *ts = st + (size_t)t * kTileSlot;
+                    tma_load_2d(smem_u32(ts), &tmFh, k * BK, m_tile * BM, fb);
+                    tma_load_3d(smem_u32(ts + kTileA), &tmGh, 0, (int)crank * (BN / CL), l0 + j + t, fb);
+                    if (NPARTS == 2) {
+                        tma_load_2d(smem_u32(ts + kTileA + kTileBc), &tmFl, k * BK, m_tile * BM, fb);
+                        tma_load_3d(smem_u32(ts + 2 * kTileA + kTileBc), &tmGl, 0, (int)crank * (BN / CL),
+                                    l0 + j + t, fb);
+                    }
                 }
+                j += len;
             }
             if (PAIR) {
                 // tail, bounded like every wait: the copies of the last stages have
@@ -188,10 +213,12 @@ __global__ void __launch_bounds__(kThreads, 1)
         // ---- relay (odd CTA): its stage s has landed -> arrive on the even CTA's
         // full barrier, so the pair MMA reads both halves only when both are in
         if (lane == 0) {
-            for (int it = 0; it < cnt; it++) {
+            const uint32_t *tl = p.tiles + l0;
+            for (int j = 0, it = 0; j < cnt; it++) {
                 const int s = it % S;
                 if (!mbar_wait(smem_u32(&full_bar[s]), (uint32_t)(it / S) & 1u, p.err)) break;
                 mbar_arrive_cluster(mapa_cluster(smem_u32(&full_bar[s]), 0));
+                j += stage_len(tl, j, cnt, TPS);
             }
         }
     } else if (warp == 1) {
@@ -211,7 +238,7 @@ __global__ void __launch_bounds__(kThreads, 1)
                 asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
                 const uint32_t d_tmem = tmem + (uint32_t)(buf * BN);
                 bool first = true;
-                for (; j < cnt && (__ldg(p.tiles + l0 + j) >> 16) == n; j++, it++) {
+                while (j < cnt && (__ldg(p.tiles + l0 + j) >> 16) == n) {
                     const int s = it % S;
                     const uint32_t ph = (uint32_t)(it / S) & 1u;
                     if (!mbar_wait(smem_u32(&full_bar[s]), ph, p.err)) {
@@ -219,33 +246,38 @@ __global__ void __launch_bounds__(kThreads, 1)
                         break;
                     }
                     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-                    const uint32_t st = smem_u32(base + (size_t)s * kStage);
-                    const uint32_t aH = st, bH = st + kTileA;
-                    const uint32_t aL = st + kTileA + kTileBc, bL = st + 2 * kTileA + kTileBc;
+                    const int len = stage_len(p.tiles + l0, j, cnt, TPS);
+                    for (int t = 0; t < len; t++) {
+                        const uint32_t ts = smem_u32(base + (size_t)s * kStage + (size_t)t * kTileSlot);
+                        const uint32_t aH = ts, bH = ts + kTileA;
+                        const uint32_t aL = ts + kTileA + kTileBc, bL = ts + 2 * kTileA + kTileBc;
 #pragma unroll
-                    for (int kk = 0; kk < BK / 16; kk++) {
-                        const uint32_t off = (uint32_t)kk * 32u;  // 16 BF16 along K
-                        const uint32_t acc = (!first || kk > 0) ? 1u : 0u;
-                        if (PAIR) {
-                            umma_bf16_pair(d_tmem, umma_desc(aH + off), umma_desc(bH + off), kIdescT, acc);
-                            if (NPASS == 3) {
-                                umma_bf16_pair(d_tmem, umma_desc(aH + off), umma_desc(bL + off), kIdescT, 1u);
-                                umma_bf16_pair(d_tmem, umma_desc(aL + off), umma_desc(bH + off), kIdescT, 1u);
-                            }
-                        } else {
-                            umma_bf16(d_tmem, umma_desc(aH + off), umma_desc(bH + off), kIdescT, acc);
-                            if (NPASS == 3) {
-                                umma_bf16(d_tmem, umma_desc(aH + off), umma_desc(bL + off), kIdescT, 1u);
-                                umma_bf16(d_tmem, umma_desc(aL + off), umma_desc(bH + off), kIdescT, 1u);
+                        for (int kk = 0; kk < BK / 16; kk++) {
+                            const uint32_t off = (uint32_t)kk * 32u;  // 16 BF16 along K
+                            const uint32_t acc = (!first || kk > 0) ? 1u : 0u;
+                            if (PAIR) {
+                                umma_bf16_pair(d_tmem, umma_desc(aH + off), umma_desc(bH + off), kIdescT, acc);
+                                if (NPASS == 3) {
+                                    umma_bf16_pair(d_tmem, umma_desc(aH + off), umma_desc(bL + off), kIdescT, 1u);
+                                    umma_bf16_pair(d_tmem, umma_desc(aL + off), umma_desc(bH + off), kIdescT, 1u);
+                                }
+                            } else {
+                                umma_bf16(d_tmem, umma_desc(aH + off), umma_desc(bH + off), kIdescT, acc);
+                                if (NPASS == 3) {
+                                    umma_bf16(d_tmem, umma_desc(aH + off), umma_desc(bL + off), kIdescT, 1u);
+                                    umma_bf16(d_tmem, umma_desc(aL + off), umma_desc(bH + off), kIdescT, 1u);
+                                }
                             }
                         }
+                        first = false;
                     }
                     // the stage is free in both CTAs once these MMAs have read it
                     if (PAIR)
                         umma_commit_pair_mc(smem_u32(&empty_bar[s]), (uint16_t)3u);
                     else
                         umma_commit(smem_u32(&empty_bar[s]));
-                    first = false;
+                    j += len;
+                    it++;
                 }
                 if (!ok) break;
                 if (PAIR)
