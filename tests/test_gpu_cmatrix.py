@@ -120,3 +120,33 @@ def test_cta_pair_is_bitwise_equal(cuda, gdlib, ncells):
         torch.cuda.synchronize()
         assert torch.equal(outs[0], outs[1])
         cm.close()
+
+
+def test_headline_grid_against_pair_kernel(cuda, gdlib):
+    """20^3 (R = 4.8, 3648 nodes), the bench's lattice: the tensor-core gain
+    against the FP32 pair-product kernel (itself within 1e-5 of the FP64
+    oracle) on 300 seeded mixtures, with a leading dimension past the cells;
+    CTA pairs and one CTA per MMA give the same bits."""
+    torch = cuda
+    spec = gdlib.GridSpec(20, R=4.8)
+    ctx = gdlib.Context(spec)
+    nc, ld = 300, 304
+    ft = torch.zeros((ctx.n_pnt, ld), dtype=torch.float32, device="cuda")
+    ft[:, :nc] = torch.from_numpy(inputs.dirichlet_mixtures(spec.fill(), nc, seed=11)).cuda()
+    ref = torch.empty_like(ft)
+    ctx.collision(ft, nc, ld, None, ref)
+    ref = ref[:, :nc]
+    for mode, tol in ((gdlib.CMATRIX_BF16X3, 2e-5), (gdlib.CMATRIX_BF16, 1e-3)):
+        cm = gdlib.CollisionMatrix(ctx, mode)
+        outs = []
+        for ctas in (2, 1):
+            cm.set_cluster(ctas)
+            out = torch.full_like(ft, -1.0)
+            cm.gain(ft, nc, ld, out)
+            outs.append(out)
+        torch.cuda.synchronize()
+        assert torch.equal(outs[0], outs[1])
+        assert bool((outs[0][:, nc:] == -1.0).all())
+        rel = float((outs[0][:, :nc] - ref).norm() / ref.norm())
+        assert rel <= tol, (mode, rel)
+        cm.close()
