@@ -58,9 +58,10 @@ def parse():
     p.add_argument("--cpu-seconds", type=float, default=15.0,
                    help="target length of the bounded CPU-baseline sample")
     p.add_argument("--no-cpu-baseline", action="store_true")
-    p.add_argument("--gain", choices=["pair", "bf16", "bf16x3"], default="bf16",
-                   help="gain algorithm of the timed step (FP32 pair-product kernel or tensor-core collision matrices)")
-    p.add_argument("--alternatives", default="pair,bf16x3",
+    p.add_argument("--gain", choices=["pair", "pair_tc", "bf16", "bf16x3"], default="bf16",
+                   help="gain algorithm of the timed step (FP32 pair-product kernel, pair products with the "
+                        "contraction on the tensor cores, or tensor-core collision matrices)")
+    p.add_argument("--alternatives", default="pair,pair_tc,bf16x3",
                    help="comma list of other gain paths to time after the main run ('' for none)")
     p.add_argument("--no-surrogate", action="store_true", help="time the plain step only")
     p.add_argument("--settle", type=float, default=3.0, help="seconds of untimed plain steps before timing")
@@ -70,7 +71,7 @@ def parse():
     return p.parse_args()
 
 
-GAIN_PATHS = {"pair": 0, "bf16": 1, "bf16x3": 2}
+GAIN_PATHS = {"pair": 0, "bf16": 1, "bf16x3": 2, "pair_tc": 3}
 
 
 def workload(args, ncells):
@@ -289,11 +290,12 @@ def run_ours(args):
     peak, peak_kind = peaks()
     roof = gain_roofline(args.gain, ctx, f0, nc, stream, flush, peak, peak_kind, max(2, args.steps))
 
-    dtype = {"pair": "f32", "bf16": "bf16 (FP32 accumulate)", "bf16x3": "bf16x3 (FP32 accumulate)"}[args.gain]
+    dtype = {"pair": "f32", "pair_tc": "bf16x3 pair products and weights (FP32 accumulate)",
+             "bf16": "bf16 (FP32 accumulate)", "bf16x3": "bf16x3 (FP32 accumulate)"}[args.gain]
     # per plain step: pair path = loss, gain, chunk reduction, projection, max, dt,
     # relax (7); collision matrices = f conversion + 3 loss GEMMs, f conversion +
     # gain, projection, max, dt, relax (10)
-    plain_launches = 7 if args.gain == "pair" else 10
+    plain_launches = 7 if args.gain in ("pair", "pair_tc") else 10
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None,
@@ -438,11 +440,12 @@ def gain_roofline(name, ctx, f0, nc, stream, flush, peak, peak_kind, reps):
         a1.synchronize()
         g_ms.append(a0.elapsed_time(a1))
     g_avg = statistics.mean(g_ms) / 1000.0
-    if name == "pair":
+    if name in ("pair", "pair_tc"):
         inf = ctx.info
         flop = nc * (7 * inf["pair_products"] + 2 * inf["contraction_terms"] + inf["scatter_terms"])
-        kernel, work = "gain_pair_kernel (+ chunk reduction)", \
-            "7 FLOP per pair product + 2 per nonzero-weight term + 1 per scatter update"
+        kernel = "gain_pair_kernel (+ chunk reduction)" if name == "pair" else \
+            "pair_tc_kernel (tcgen05 contraction, + chunk reduction)"
+        work = "7 FLOP per pair product + 2 per nonzero-weight term + 1 per scatter update"
     else:
         # stored tiles: the nonzero 256 x 64 tiles of each G_i's block upper triangle
         tiles = ctx._info()["cmatrix_tiles"]
@@ -450,7 +453,7 @@ def gain_roofline(name, ctx, f0, nc, stream, flush, peak, peak_kind, reps):
         kernel, work = "cmatrix_gain_kernel (tcgen05)", \
             "MACs x 2 of the 128x256x64 tiles issued (nonzero tiles of the block upper triangle of each symmetric G_i; x3 for bf16x3)"
     traffic, traffic_src = None, None
-    if name != "pair":
+    if name not in ("pair", "pair_tc"):
         # DRAM bytes per launch: the collision matrices stream through once.  An
         # ncu capture of the same kernel (CTA pairs, one pass) on 14^3 / 4096
         # cells read and wrote 2.847 GB for 2.773 GB of stored matrix tiles

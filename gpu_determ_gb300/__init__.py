@@ -28,6 +28,7 @@ CMATRIX_BF16X3 = 1
 GAIN_PAIR = 0
 GAIN_CMATRIX_BF16 = 1
 GAIN_CMATRIX_BF16X3 = 2
+GAIN_PAIR_TC = 3
 MLP_SCALE_INPUT = 1
 MLP_SCALE_OUTPUT = 2
 MLP_LOSS_MSE = 4
@@ -244,7 +245,8 @@ class Context:
             pass
 
     def set_gain_path(self, path: int):
-        """GAIN_PAIR (FP32 pair-product kernel), GAIN_CMATRIX_BF16 or GAIN_CMATRIX_BF16X3."""
+        """GAIN_PAIR (FP32 pair-product kernel), GAIN_CMATRIX_BF16, GAIN_CMATRIX_BF16X3 or
+        GAIN_PAIR_TC (pair products with the weight contraction on the tensor cores)."""
         _check(lib().gd_ctx_set_gain_path(self._h, int(path)))
 
     # tables -----------------------------------------------------------------
@@ -278,7 +280,8 @@ class Context:
         r = _Autotune()
         _check(lib().gd_ctx_autotune(self._h, _ptr(f), int(ncells), int(ld), int(path_mask), float(mem_budget),
                                      C.byref(r), _stream(stream)))
-        names = {GAIN_PAIR: "pair", GAIN_CMATRIX_BF16: "cmatrix_bf16", GAIN_CMATRIX_BF16X3: "cmatrix_bf16x3"}
+        names = {GAIN_PAIR: "pair", GAIN_CMATRIX_BF16: "cmatrix_bf16", GAIN_CMATRIX_BF16X3: "cmatrix_bf16x3",
+                 GAIN_PAIR_TC: "pair_tc"}
         cands = [{"path": names[r.cand_path[k]], "waves": r.cand_waves[k], "cluster": r.cand_cluster[k],
                   "ms": r.cand_ms[k]} for k in range(r.n_candidates)]
         return {"path": names[r.path], "waves": r.waves, "cluster": r.cluster, "best_ms": r.best_ms,

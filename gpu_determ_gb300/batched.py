@@ -21,7 +21,7 @@ import sys
 
 import numpy as np
 
-from . import DT_COURANT, GAIN_CMATRIX_BF16X3, GAIN_PAIR, Batch, Context, GridSpec, inputs
+from . import DT_COURANT, GAIN_CMATRIX_BF16X3, GAIN_PAIR, GAIN_PAIR_TC, Batch, Context, GridSpec, inputs
 
 
 def build(cells: int = 4096, grids=(12, 16, 20, 24), radius: float = 4.8, mach: float = 3.0,
@@ -41,7 +41,8 @@ def build(cells: int = 4096, grids=(12, 16, 20, 24), radius: float = 4.8, mach: 
         nc = len(mine)
         tune = None
         if autotune:
-            tune = ctx.autotune(f, nc, nc, path_mask=(1 << GAIN_PAIR) | (1 << GAIN_CMATRIX_BF16X3),
+            tune = ctx.autotune(f, nc, nc,
+                                path_mask=(1 << GAIN_PAIR) | (1 << GAIN_PAIR_TC) | (1 << GAIN_CMATRIX_BF16X3),
                                 mem_budget=mem_budget)
         m5 = torch.zeros((nc, 5), dtype=torch.float64, device=dev)
         t = torch.zeros(1, dtype=torch.float32, device=dev)

@@ -207,11 +207,13 @@ extern "C" int gd_batch_info(const gd_batch *b, int *groups, int *streams, int *
 // Autotuner: times the gain launch candidates of one context on the caller's
 // cells and keeps the fastest.  Candidates: the FP32 pair kernel with 1, 2 or
 // 4 CTAs per SM as the minimum s-chunk fill (trading partial-sum traffic for
-// parallelism), and the tensor-core collision matrices in BF16x3 and BF16
-// mode, each with 1 or 2 CTAs per MMA (2: CTA-pair MMA, M = 256 cells),
-// when the caller's mask admits them and their stored triangle tiles
-// (bounded by every tile of the block upper triangle) fit the memory budget.  Each candidate: one untimed run, then the median of three
-// runs timed with CUDA events on the stream.
+// parallelism), the pair formulation with its contraction on the tensor cores
+// (when its per-class-box weight table fits the memory budget), and the
+// tensor-core collision matrices in BF16x3 and BF16 mode, each with 1 or 2
+// CTAs per MMA (2: CTA-pair MMA, M = 256 cells), when the caller's mask admits
+// them and their stored triangle tiles (bounded by every tile of the block
+// upper triangle) fit the memory budget.  Each candidate: one untimed run,
+// then the median of three runs timed with CUDA events on the stream.
 
 extern "C" int gd_ctx_autotune(gd_ctx *ctx, const float *f, int ncells, int ld, int path_mask, double mem_budget,
                                gd_autotune_result *res, gd_stream stream)
@@ -219,7 +221,7 @@ extern "C" int gd_ctx_autotune(gd_ctx *ctx, const float *f, int ncells, int ld, 
     using namespace gd;
     if (!ctx || !f || !res) return set_error(GD_ERR_INVALID_ARG, "NULL argument");
     if (ncells < 1 || ld < ncells) return set_error(GD_ERR_INVALID_ARG, "need 1 <= ncells <= ld");
-    if (!(path_mask & 7)) return set_error(GD_ERR_INVALID_ARG, "path_mask admits no gain path");
+    if (!(path_mask & 15)) return set_error(GD_ERR_INVALID_ARG, "path_mask admits no gain path");
     Context &c = ctx->c;
     gd::DeviceGuard ds(c.device);
     cudaStream_t st = (cudaStream_t)stream;
@@ -230,6 +232,8 @@ extern "C" int gd_ctx_autotune(gd_ctx *ctx, const float *f, int ncells, int ld, 
     std::vector<Cand> cands;
     if (path_mask & (1 << GD_GAIN_PAIR))
         for (int w : {1, 2, 4}) cands.push_back({GD_GAIN_PAIR, w, 1});
+    if ((path_mask & (1 << GD_GAIN_PAIR_TC)) && pair_tc_bytes(c) <= mem_budget)
+        cands.push_back({GD_GAIN_PAIR_TC, 0, 1});
     if ((path_mask & (1 << GD_GAIN_CMATRIX_BF16X3)) && cmatrix_bytes_bound(c, GD_CMATRIX_BF16X3) <= mem_budget)
         for (int cl : {1, 2}) cands.push_back({GD_GAIN_CMATRIX_BF16X3, 0, cl});
     if ((path_mask & (1 << GD_GAIN_CMATRIX_BF16)) && cmatrix_bytes_bound(c, GD_CMATRIX_BF16) <= mem_budget)

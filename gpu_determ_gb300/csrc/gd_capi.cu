@@ -238,6 +238,7 @@ static void destroy_context(Context &c)
 {
     gd_cmatrix_destroy(c.cmatrix);
     c.cmatrix = nullptr;
+    pair_tc_free(c);
     cudaFree(c.d_cmap);
     cudaFree(c.d_nodes);
     cudaFree(c.d_b);
@@ -430,15 +431,20 @@ int gd_ctx_destroy(gd_ctx *ctx)
 int gd_ctx_set_gain_path(gd_ctx *ctx, int path)
 {
     if (!ctx) return set_error(GD_ERR_INVALID_ARG, "context is NULL");
-    if (path != GD_GAIN_PAIR && path != GD_GAIN_CMATRIX_BF16 && path != GD_GAIN_CMATRIX_BF16X3)
+    if (path != GD_GAIN_PAIR && path != GD_GAIN_CMATRIX_BF16 && path != GD_GAIN_CMATRIX_BF16X3 &&
+        path != GD_GAIN_PAIR_TC)
         return set_error(GD_ERR_INVALID_ARG, "unknown gain path");
     gd::Context &c = ctx->c;
     if (path == c.gain_path) return GD_OK;
     gd::DeviceGuard g(c.device);
     gd_cmatrix_destroy(c.cmatrix);
     c.cmatrix = nullptr;
+    gd::pair_tc_free(c);
     c.gain_path = GD_GAIN_PAIR;
-    if (path != GD_GAIN_PAIR) {
+    if (path == GD_GAIN_PAIR_TC) {
+        int rc = gd::pair_tc_build(c);
+        if (rc) return rc;
+    } else if (path != GD_GAIN_PAIR) {
         const int mode = path == GD_GAIN_CMATRIX_BF16 ? GD_CMATRIX_BF16 : GD_CMATRIX_BF16X3;
         int rc = gd_cmatrix_create(ctx, mode, &c.cmatrix);
         if (rc) return rc;
@@ -571,6 +577,10 @@ int gd_ctx_check(gd_ctx *ctx, gd_stream stream)
     GD_CUDA(cudaStreamSynchronize(st));
     if (c.cmatrix) {
         const int rc = gd_cmatrix_check(c.cmatrix, stream);
+        if (rc) return rc;
+    }
+    if (c.pair_tc) {
+        const int rc = gd::pair_tc_check(c, st);
         if (rc) return rc;
     }
     if (!h[0]) return GD_OK;

@@ -803,6 +803,22 @@ double cmatrix_bytes_bound(const Context &c, int mode)
     return (double)tiles * ns * BN * BK * 2.0 * (mode == GD_CMATRIX_BF16X3 ? 2.0 : 1.0);
 }
 
+int encode_bf16_sw128(CUtensorMap *m, void *ptr, int rank, const uint64_t *dims, const uint64_t *strides,
+                      const uint32_t *box)
+{
+    EncodeTiled fn;
+    int rc = get_encoder(&fn);
+    if (rc) return rc;
+    cuuint64_t dd[5], ss[4];
+    cuuint32_t bb[5];
+    for (int i = 0; i < rank; i++) {
+        dd[i] = dims[i];
+        bb[i] = box[i];
+        if (i + 1 < rank) ss[i] = strides[i];
+    }
+    return encode(fn, m, ptr, rank, dd, ss, bb);
+}
+
 int run_loss_path(Context &c, const float *f, int ncells, int ld, float *nu, cudaStream_t st)
 {
     if (c.gain_path != GD_GAIN_PAIR && c.cmatrix) {
@@ -814,6 +830,7 @@ int run_loss_path(Context &c, const float *f, int ncells, int ld, float *nu, cud
 
 int run_gain_path(Context &c, const float *f, int ncells, int ld, float *gain, cudaStream_t st)
 {
+    if (c.gain_path == GD_GAIN_PAIR_TC && c.pair_tc) return run_pair_tc(c, f, ncells, ld, gain, st);
     if (c.gain_path == GD_GAIN_PAIR || !c.cmatrix) return run_gain(c, f, ncells, ld, gain, st);
     return gd_cmatrix_gain(c.cmatrix, f, ncells, ld, gain, st);
 }

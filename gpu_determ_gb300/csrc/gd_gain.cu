@@ -363,6 +363,17 @@ int run_gain(Context &c, const float *f, int ncells, int ld, float *gain, cudaSt
     return GD_OK;
 }
 
+int reduce_gain_partials(Context &c, const float *part, int nchunks, int cells_pad, int ncells, int ld,
+                         float *gain, cudaStream_t st)
+{
+    const int64_t outs = (int64_t)c.d.n_pnt * ncells;
+    const int rblocks = (int)std::min<int64_t>((outs + 255) / 256, (int64_t)c.sm_count * 16);
+    gain_reduce_kernel<<<std::max(rblocks, 1), 256, 0, st>>>(part, nchunks, c.d.n_pnt, cells_pad, ncells, ld,
+                                                              gain);
+    GD_CUDA(cudaGetLastError());
+    return GD_OK;
+}
+
 // ---------------------------------------------------------------------------
 // Launch pieces for callers that bring their own partial-sum buffer (the
 // allocation-free entry point in gd_noalloc.cu).  run_gain above does not

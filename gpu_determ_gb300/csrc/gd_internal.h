@@ -1,6 +1,7 @@
 // gd_internal.h -- shared declarations of the GB300 collision-integral library.
 #pragma once
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -11,6 +12,8 @@
 #include "gpu_determ.h"
 
 namespace gd {
+
+struct PairTc;
 
 // Lattice sizes derived from a grid spec.  The "class box" of a parity
 // class is the set of offsets v with 0 <= v_a < n_a and v_a of one parity per
@@ -92,6 +95,7 @@ struct Context {
     int64_t pair_products = 0, contraction_terms = 0, scatter_terms = 0;
     int gain_path = GD_GAIN_PAIR;    // gain algorithm for gd_collision / gd_step
     gd_cmatrix *cmatrix = nullptr;   // collision matrices when gain_path is a GD_GAIN_CMATRIX_*
+    PairTc *pair_tc = nullptr;       // per-D weight table when gain_path is GD_GAIN_PAIR_TC
     int gain_cb = 32;                // cells per lane row of the gain kernel (fixed per grid)
     bool gain_cmap_smem = true;      // its box -> compact map in shared memory (else through L1)
     size_t gain_smem = 0;            // its dynamic shared memory
@@ -174,6 +178,26 @@ int gain_launch_shape(Context &c, int ncells, int *cb, size_t *smem, int *nblk, 
 void gain_chunk_bounds(const Context &c, int nchunks, int *bounds);
 int launch_gain_pair(Context &c, const float *f, int ncells, int ld, float *gain, float *part,
                      int nchunks, const int *d_bounds, int cb, size_t smem, cudaStream_t st);
+
+// device copy of the work-balanced s-chunk boundaries for nchunks chunks
+// (built once per count, gd_gain.cu)
+int gain_bounds_device(Context &c, int nchunks, const int **out);
+// gain[node][c] = sum over chunks of part[chunk][node][c], in chunk order
+int reduce_gain_partials(Context &c, const float *part, int nchunks, int cells_pad, int ncells, int ld,
+                         float *gain, cudaStream_t st);
+
+// pair-product gain with the contraction on the tensor cores (gd_pair_tc.cu)
+int pair_tc_build(Context &c);
+void pair_tc_free(Context &c);
+double pair_tc_bytes(const Context &c);
+int run_pair_tc(Context &c, const float *f, int ncells, int ld, float *gain, cudaStream_t st);
+// reports (and clears) a pipeline time-out of the pair tensor-core kernel
+int pair_tc_check(Context &c, cudaStream_t st);
+
+// BF16 tiled tensor map with 128-byte swizzle for the TMA loads of the
+// tensor-core kernels (gd_cmatrix.cu)
+int encode_bf16_sw128(CUtensorMap *m, void *ptr, int rank, const uint64_t *dims, const uint64_t *strides,
+                      const uint32_t *box);
 
 // scratch -------------------------------------------------------------------
 int ensure_scratch(Context &c, size_t bytes);

@@ -1,0 +1,610 @@
+// gd_pair_tc.cu -- gain in the pair-product formulation with its contraction
+// on the tensor cores (sm_103a).
+//
+// The FP32 gain kernel (gd_gain.cu) walks the pair sums s = i + i1: for every
+// s it forms the pair products P_s[n] on the class box B(D(s)), contracts them
+// with the weight row of every row group present in B(D(s)),
+//     C_s[m] = sum_{n in B(D)} W_D[m][n] P_s[n],
+// and adds C_s[m] to the outputs (s +- g)/2 of each member g of group m
+// (collision_integral.cu:75-188 summed in pair-product form).  Here the
+// contraction is one GEMM per (s, 128 cells) on the tensor cores:
+//     C^T [128 cells x M_D] = P_s^T [128 cells x K_D] . W_D^T [K_D x M_D],
+// W_D holding D's group rows restricted to B(D) (K_D = |B(D)| class offsets in
+// the order (x2 * ey + y2) * ez + z2, M_D groups in the order of D's work
+// items), stored once per D in chunks of 64 offsets.  P and W are split into
+// BF16 hi + lo and P_hi W_hi + P_hi W_lo + P_lo W_hi accumulates in FP32
+// (relative error ~1e-6 against the FP32 kernel).  Boxes with more than 256
+// groups run as several passes of at most 256 groups, each forming P again.
+//
+// One CTA per (128-cell tile, chunk of s), warp-specialized:
+//   warps 10..17 pair products of one 64-offset chunk for the 128 cells (thread
+//                = cell, eight gathers of f per product, the FP32 products of
+//                the FP32 kernel), split into BF16 hi/lo and written to shared
+//                memory in the MMA's 128-byte-swizzled K-major layout; two
+//                groups of four warps fill the two stages alternately;
+//   warp 0       TMA loads of the chunk's weight rows (hi, lo), 16 rows a box;
+//   warp 1       tcgen05.mma (M = 128 cells, N = groups padded to 16, K = 16)
+//                into one of two TMEM accumulators per (s, pass);
+//   warps 2..9   read C^T from TMEM (thread = cell; two warps per lane quadrant
+//                taking alternate blocks of 16 groups) and add each group's sum
+//                to the CTA's partial outputs at its members' targets (s +- g)/2.
+// Within one s every target receives one update and the epilogue takes the
+// units in s order, so every partial sum is formed in a fixed order; the
+// chunk partials are added in chunk order.  Results are bitwise reproducible.
+// Every mbarrier wait is bounded (a time-out sets the error flag).
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "gd_internal.h"
+#include "gd_tc.cuh"
+
+namespace gd {
+namespace {
+
+using namespace tc;
+
+constexpr int PT_BM = 128;               // cells per CTA (MMA M, TMEM lanes)
+constexpr int PT_KC = 64;                // class offsets per chunk (one 128-byte swizzle row of BF16)
+constexpr int PT_NMAX = 256;             // groups per pass (MMA N, TMEM columns per accumulator)
+constexpr uint32_t kPTile = PT_BM * PT_KC * 2;     // 16 KB: P part of one chunk
+constexpr uint32_t kWTile = PT_NMAX * PT_KC * 2;   // 32 KB: W part of one chunk (up to 256 rows)
+constexpr uint32_t kPtStage = 2 * kPTile + 2 * kWTile;  // P hi, P lo, W hi, W lo
+constexpr int kPtStages = 2;
+constexpr int kEpiWarps = 8;             // two per TMEM lane quadrant
+constexpr int kProdWarps = 8;            // two groups of four
+constexpr int kPtThreads = 32 * (2 + kEpiWarps + kProdWarps);
+
+struct PtArgs {
+    Dims d;
+    const float *f;
+    int ld, ncells, cells_pad;
+    const int16_t *cmap;
+    const int *D_item_off;
+    const int4 *D_items;
+    const uint32_t *D_members;
+    const int *wrow;        // [nxyz] first weight row of each D
+    const int *s_bounds;    // [chunks + 1]
+    float *part;            // [chunk][n_pnt][cells_pad]
+    int *err;
+};
+
+// One (s, pass) of the walk: its class box, groups and weight rows.
+struct Unit {
+    int sx, sy, sz, px, py, pz;
+    int ex, ey, ez, K, nch;    // class box extents, offsets, 64-offset chunks
+    int it0, mcnt, npad;       // first work item of this pass, groups, groups padded to 16
+    int mpad;                  // all of D's groups padded to 16 (rows per chunk in the table)
+    int wrow;                  // first table row of D
+    int npass;
+};
+
+__device__ __forceinline__ void unit_of(const PtArgs &a, int sl, int q, Unit &u)
+{
+    const Dims &d = a.d;
+    u.sz = sl % d.sz;
+    u.sy = (sl / d.sz) % d.sy;
+    u.sx = sl / (d.sz * d.sy);
+    const int Dx = min(u.sx, 2 * d.nx - 2 - u.sx), Dy = min(u.sy, 2 * d.ny - 2 - u.sy),
+              Dz = min(u.sz, 2 * d.nz - 2 - u.sz);
+    u.ex = (Dx >> 1) + 1;
+    u.ey = (Dy >> 1) + 1;
+    u.ez = (Dz >> 1) + 1;
+    u.px = u.sx & 1;
+    u.py = u.sy & 1;
+    u.pz = u.sz & 1;
+    u.K = u.ex * u.ey * u.ez;
+    u.nch = (u.K + PT_KC - 1) / PT_KC;
+    const int Did = (Dx * d.ny + Dy) * d.nz + Dz;
+    const int i0 = __ldg(a.D_item_off + Did), m = __ldg(a.D_item_off + Did + 1) - i0;
+    u.npass = (m + PT_NMAX - 1) / PT_NMAX;
+    u.it0 = i0 + q * PT_NMAX;
+    u.mcnt = min(PT_NMAX, m - q * PT_NMAX);
+    u.npad = (u.mcnt + 15) & ~15;
+    u.mpad = (m + 15) & ~15;
+    u.wrow = __ldg(a.wrow + Did);
+}
+
+__device__ __forceinline__ int npass_of(const PtArgs &a, int sl)
+{
+    const Dims &d = a.d;
+    const int sz = sl % d.sz, sy = (sl / d.sz) % d.sy, sx = sl / (d.sz * d.sy);
+    const int Dx = min(sx, 2 * d.nx - 2 - sx), Dy = min(sy, 2 * d.ny - 2 - sy), Dz = min(sz, 2 * d.nz - 2 - sz);
+    const int Did = (Dx * d.ny + Dy) * d.nz + Dz;
+    const int m = __ldg(a.D_item_off + Did + 1) - __ldg(a.D_item_off + Did);
+    return (m + PT_NMAX - 1) / PT_NMAX;
+}
+
+// Two BF16 values in one word, the first at the lower address.
+__device__ __forceinline__ uint32_t pack_bf16(float first, float second)
+{
+    const uint32_t a = (uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(first));
+    const uint32_t b = (uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(second));
+    return a | (b << 16);
+}
+
+template <bool CMAP_SMEM>
+__global__ void __launch_bounds__(kPtThreads, 1)
+    pair_tc_kernel(const __grid_constant__ CUtensorMap tmWh, const __grid_constant__ CUtensorMap tmWl, PtArgs a)
+{
+    extern __shared__ __align__(1024) unsigned char dsmem[];
+    unsigned char *base = reinterpret_cast<unsigned char *>(
+        (reinterpret_cast<uintptr_t>(dsmem) + 1023) & ~static_cast<uintptr_t>(1023));
+    int16_t *cmap_s = reinterpret_cast<int16_t *>(base + kPtStages * kPtStage);
+    __shared__ __align__(8) uint64_t full_bar[kPtStages], empty_bar[kPtStages], accf_bar[2], acce_bar[2];
+    __shared__ uint32_t tmem_base_holder;
+    __shared__ int epi_fail;
+
+    const Dims &d = a.d;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (threadIdx.x == 0) {
+        epi_fail = 0;
+        for (int s = 0; s < kPtStages; s++) {
+            mbar_init(smem_u32(&full_bar[s]), 4 + 1);  // four producer warps + the TMA arrival
+            mbar_init(smem_u32(&empty_bar[s]), 1);      // the MMA commit
+        }
+        for (int b = 0; b < 2; b++) {
+            mbar_init(smem_u32(&accf_bar[b]), 1);
+            mbar_init(smem_u32(&acce_bar[b]), kEpiWarps);  // the epilogue warps
+        }
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (CMAP_SMEM)
+        for (int t = threadIdx.x; t < d.nxyz; t += blockDim.x) cmap_s[t] = a.cmap[t];
+    if (warp == 1) {
+        tmem_alloc<1>(smem_u32(&tmem_base_holder), 2 * PT_NMAX);
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    }
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = tmem_base_holder;
+    const int16_t *cmap = CMAP_SMEM ? cmap_s : a.cmap;
+
+    const int m_tile = blockIdx.x, chunk = blockIdx.y;
+    const int s_begin = __ldg(a.s_bounds + chunk), s_end = __ldg(a.s_bounds + chunk + 1);
+
+    if (warp == 0) {
+        // ---- TMA: weight rows of every chunk --------------------------------------
+        if (lane == 0) {
+            int ck = 0;
+            bool ok = true;
+            for (int sl = s_begin; ok && sl < s_end; sl++) {
+                const int np = npass_of(a, sl);
+                for (int q = 0; ok && q < np; q++) {
+                    Unit u;
+                    unit_of(a, sl, q, u);
+                    for (int ch = 0; ch < u.nch; ch++, ck++) {
+                        const int st = ck & 1;
+                        if (!mbar_wait(smem_u32(&empty_bar[st]), ((uint32_t)(ck >> 1) & 1u) ^ 1u, a.err)) {
+                            ok = false;
+                            break;
+                        }
+                        unsigned char *sb = base + (size_t)st * kPtStage;
+                        const uint32_t fb = smem_u32(&full_bar[st]);
+                        mbar_expect_tx(fb, 2u * (uint32_t)u.npad * (PT_KC * 2));
+                        const int row0 = u.wrow + ch * u.mpad + q * PT_NMAX;
+                        for (int r = 0; r < u.npad; r += 16) {
+                            tma_load_2d(smem_u32(sb + 2 * kPTile + r * (PT_KC * 2)), &tmWh, 0, row0 + r, fb);
+                            tma_load_2d(smem_u32(sb + 2 * kPTile + kWTile + r * (PT_KC * 2)), &tmWl, 0, row0 + r,
+                                        fb);
+                        }
+                    }
+                }
+            }
+        }
+    } else if (warp == 1) {
+        // ---- MMA ---------------------------------------------------------------------
+        if (lane == 0) {
+            int ck = 0, uc = 0;
+            bool ok = true;
+            for (int sl = s_begin; ok && sl < s_end; sl++) {
+                const int np = npass_of(a, sl);
+                for (int q = 0; ok && q < np; q++, uc++) {
+                    Unit u;
+                    unit_of(a, sl, q, u);
+                    const int buf = uc & 1;
+                    if (!mbar_wait(smem_u32(&acce_bar[buf]), ((uint32_t)(uc >> 1) & 1u) ^ 1u, a.err)) {
+                        ok = false;
+                        break;
+                    }
+                    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                    const uint32_t d_tmem = tmem + (uint32_t)(buf * PT_NMAX);
+                    const uint32_t idesc = umma_idesc_bf16(PT_BM, u.npad);
+                    for (int ch = 0; ch < u.nch; ch++, ck++) {
+                        const int st = ck & 1;
+                        if (!mbar_wait(smem_u32(&full_bar[st]), (uint32_t)(ck >> 1) & 1u, a.err)) {
+                            ok = false;
+                            break;
+                        }
+                        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                        const uint32_t sb = smem_u32(base + (size_t)st * kPtStage);
+                        const uint32_t pH = sb, pL = sb + kPTile, wH = sb + 2 * kPTile, wL = sb + 2 * kPTile + kWTile;
+#pragma unroll
+                        for (int kk = 0; kk < PT_KC / 16; kk++) {
+                            const uint32_t off = (uint32_t)kk * 32u;
+                            const uint32_t acc = (ch > 0 || kk > 0) ? 1u : 0u;
+                            umma_bf16(d_tmem, umma_desc(pH + off), umma_desc(wH + off), idesc, acc);
+                            umma_bf16(d_tmem, umma_desc(pH + off), umma_desc(wL + off), idesc, 1u);
+                            umma_bf16(d_tmem, umma_desc(pL + off), umma_desc(wH + off), idesc, 1u);
+                        }
+                        umma_commit(smem_u32(&empty_bar[st]));
+                    }
+                    if (!ok) break;
+                    umma_commit(smem_u32(&accf_bar[buf]));
+                }
+            }
+        }
+    } else if (warp < 2 + kEpiWarps) {
+        // ---- epilogue: thread = cell = TMEM lane (warp % 4 is the lane quadrant it
+        // may read); the two warps of a quadrant take alternate 16-group blocks ----
+        const int quad = warp & 3;
+        const int half = (warp - 2) >> 2;
+        const int row = quad * 32 + lane;
+        const int cell = m_tile * PT_BM + row;
+        const bool live = cell < a.ncells;
+        float *part = a.part + (size_t)chunk * d.n_pnt * a.cells_pad + cell;
+        int uc = 0;
+        bool ok = true;
+        for (int sl = s_begin; ok && sl < s_end; sl++) {
+            const int np = npass_of(a, sl);
+            for (int q = 0; ok && q < np; q++, uc++) {
+                Unit u;
+                unit_of(a, sl, q, u);
+                const int buf = uc & 1;
+                if (lane == 0 && !mbar_wait(smem_u32(&accf_bar[buf]), (uint32_t)(uc >> 1) & 1u, a.err)) epi_fail = 1;
+                // both warps of a cell finish one unit before either starts the
+                // next (their targets may coincide across units); the decision to
+                // stop is taken after the barrier, by all of them alike
+                asm volatile("bar.sync 1, %0;" ::"n"(32 * kEpiWarps) : "memory");
+                if (*(volatile int *)&epi_fail) {
+                    ok = false;
+                    break;
+                }
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                const uint32_t taddr = tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(buf * PT_NMAX);
+                for (int m0 = half * 16; m0 < u.mcnt; m0 += 32) {
+                    float v[16];
+                    tmem_ld16(taddr + (uint32_t)m0, v);
+                    if (!live) continue;
+                    const int mend = min(16, u.mcnt - m0);
+                    for (int t = 0; t < mend; t++) {
+                        const int4 item = __ldg(a.D_items + u.it0 + m0 + t);
+                        const float acc = v[t];
+                        // explicit load/add/store: global float reductions flush
+                        // subnormal values to zero, and corner-node contributions
+                        // are subnormal.  Within one s the targets of all members
+                        // are distinct, so two members go at a time.
+                        for (int mm = item.y; mm < item.z; mm += 2) {
+                            const bool two = mm + 1 < item.z;
+                            int tgt[16];
+                            float old[16];
+#pragma unroll
+                            for (int h2 = 0; h2 < 2; h2++) {
+                                const uint32_t pk = __ldg(a.D_members + (h2 && two ? mm + 1 : mm));
+                                const int gx = 2 * (int)(pk & 31) + u.px, gy = 2 * (int)((pk >> 6) & 31) + u.py,
+                                          gz = 2 * (int)((pk >> 12) & 31) + u.pz;
+                                const int X0 = ((u.sx - gx) >> 1) * d.nyz, X1 = X0 + gx * d.nyz;
+                                const int Y0 = ((u.sy - gy) >> 1) * d.nz, Y1 = Y0 + gy * d.nz;
+                                const int Z0 = (u.sz - gz) >> 1, Z1 = Z0 + gz;
+#pragma unroll
+                                for (int sg = 0; sg < 8; sg++) {
+                                    const bool hx = sg & 1, hy = (sg >> 1) & 1, hz = (sg >> 2) & 1;
+                                    const bool dup = (hx && gx == 0) || (hy && gy == 0) || (hz && gz == 0) ||
+                                                     (h2 && !two);
+                                    const int tg = dup ? -1 : cmap[(hx ? X1 : X0) + (hy ? Y1 : Y0) + (hz ? Z1 : Z0)];
+                                    tgt[h2 * 8 + sg] = tg;
+                                    old[h2 * 8 + sg] = tg >= 0 ? part[(size_t)tg * a.cells_pad] : 0.f;
+                                }
+                            }
+#pragma unroll
+                            for (int e = 0; e < 16; e++)
+                                if (tgt[e] >= 0) part[(size_t)tgt[e] * a.cells_pad] = old[e] + acc;
+                        }
+                    }
+                }
+                asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+                __syncwarp();
+                if (lane == 0) mbar_arrive(smem_u32(&acce_bar[buf]));
+            }
+        }
+    } else {
+        // ---- pair products ------------------------------------------------------------
+        const int pw = warp - 2 - kEpiWarps;
+        const int grp = pw >> 2;             // fills the stages of chunks ck with ck % 2 == grp
+        const int row = (pw & 3) * 32 + lane;  // cell row of the P tile
+        const int cell = m_tile * PT_BM + row;
+        const bool live = cell < a.ncells;
+        const float *fcol = a.f + (live ? cell : 0);
+        const uint32_t swz = (uint32_t)(row & 7);
+        const uint32_t rowoff = (uint32_t)(row >> 3) * 1024u + (uint32_t)(row & 7) * 128u;
+        int ck = 0;
+        bool ok = true;
+        for (int sl = s_begin; ok && sl < s_end; sl++) {
+            const int np = npass_of(a, sl);
+            for (int q = 0; ok && q < np; q++) {
+                Unit u;
+                unit_of(a, sl, q, u);
+                for (int ch = 0; ch < u.nch; ch++, ck++) {
+                    const int st = ck & 1;
+                    if (st != grp) continue;
+                    bool w = true;
+                    if (lane == 0) w = mbar_wait(smem_u32(&empty_bar[st]), ((uint32_t)(ck >> 1) & 1u) ^ 1u, a.err);
+                    if (__shfl_sync(0xffffffffu, w ? 1 : 0, 0) == 0) {
+                        ok = false;
+                        break;
+                    }
+                    unsigned char *pH = base + (size_t)st * kPtStage + rowoff;
+                    unsigned char *pL = pH + kPTile;
+                    // class offset k = ch * 64 + t decoded as (x2, y2, z2) with z2
+                    // fastest; along a z-run only lz and l1z move, by +-1
+                    int k = ch * PT_KC;
+                    int z2 = k % u.ez, y2 = (k / u.ez) % u.ey, x2 = k / (u.ez * u.ey);
+                    int A = 0, B = 0, Cc = 0, Dd = 0;
+                    auto set_run = [&]() {
+                        const int nxv = 2 * x2 + u.px, nyv = 2 * y2 + u.py;
+                        const int X0 = ((u.sx + nxv) >> 1) * d.nyz, X1 = ((u.sx - nxv) >> 1) * d.nyz;
+                        const int Y0 = ((u.sy + nyv) >> 1) * d.nz, Y1 = ((u.sy - nyv) >> 1) * d.nz;
+                        A = X0 + Y0;
+                        B = X1 + Y1;
+                        Cc = X0 + Y1;
+                        Dd = X1 + Y0;
+                    };
+                    if (k < u.K) set_run();
+                    const int zc0 = (u.sz + u.pz) >> 1, zc1 = (u.sz - u.pz) >> 1;
+#pragma unroll 1
+                    for (int j = 0; j < PT_KC / 8; j++) {
+                        float pv[8];
+#pragma unroll
+                        for (int t = 0; t < 8; t++) {
+                            float p = 0.f;
+                            if (k < u.K) {
+                                const int lz = zc0 + z2, l1z = zc1 - z2;
+                                const int k0 = cmap[A + lz], k1 = cmap[B + l1z], k2 = cmap[Cc + l1z], k3 = cmap[Dd + lz];
+                                const int k4 = cmap[A + l1z], k5 = cmap[B + lz], k6 = cmap[Cc + lz], k7 = cmap[Dd + l1z];
+#define GD_F(kk) (((kk) >= 0 && live) ? __ldg(fcol + (size_t)(kk) * a.ld) : 0.f)
+                                const float f0 = GD_F(k0), f1 = GD_F(k1), f2 = GD_F(k2), f3 = GD_F(k3);
+                                const float f4 = GD_F(k4), f5 = GD_F(k5), f6 = GD_F(k6), f7 = GD_F(k7);
+#undef GD_F
+                                p = __fmaf_rn(f0, f1, f2 * f3) + __fmaf_rn(f4, f5, f6 * f7);
+                            }
+                            pv[t] = p;
+                            k++;
+                            if (++z2 == u.ez) {
+                                z2 = 0;
+                                if (++y2 == u.ey) {
+                                    y2 = 0;
+                                    x2++;
+                                }
+                                if (k < u.K) set_run();
+                            }
+                        }
+                        uint4 hv, lv;
+                        float hf[8], lf[8];
+#pragma unroll
+                        for (int t = 0; t < 8; t++) {
+                            hf[t] = __bfloat162float(__float2bfloat16_rn(pv[t]));
+                            lf[t] = pv[t] - hf[t];
+                        }
+                        hv.x = pack_bf16(hf[0], hf[1]);
+                        hv.y = pack_bf16(hf[2], hf[3]);
+                        hv.z = pack_bf16(hf[4], hf[5]);
+                        hv.w = pack_bf16(hf[6], hf[7]);
+                        lv.x = pack_bf16(lf[0], lf[1]);
+                        lv.y = pack_bf16(lf[2], lf[3]);
+                        lv.z = pack_bf16(lf[4], lf[5]);
+                        lv.w = pack_bf16(lf[6], lf[7]);
+                        // 16-byte chunk j of this row, 128-byte swizzle
+                        const uint32_t co = (((uint32_t)j ^ swz) & 7u) * 16u;
+                        *reinterpret_cast<uint4 *>(pH + co) = hv;
+                        *reinterpret_cast<uint4 *>(pL + co) = lv;
+                    }
+                    // generic-proxy writes, read next by the tensor cores
+                    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                    __syncwarp();
+                    if (lane == 0) mbar_arrive(smem_u32(&full_bar[st]));
+                }
+            }
+        }
+    }
+    __syncthreads();
+    if (warp == 1) {
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        tmem_dealloc<1>(tmem, 2 * PT_NMAX);
+    }
+}
+
+}  // namespace
+
+// Weight table of the tensor-core pair path: for every D (box-indexed like g),
+// its groups' rows restricted to B(D), in chunks of 64 class offsets: rows
+// wrow[D] + ch * mpad(D) + m hold group m's weights at offsets ch * 64 .. +63
+// (BF16 hi and lo, zero past K_D and for the padding groups).
+struct PairTc {
+    __nv_bfloat16 *wh = nullptr, *wl = nullptr;
+    int *wrow = nullptr;
+    int *err = nullptr;  // set by the kernel when a pipeline wait times out
+    int64_t rows = 0;
+    int max_items = 0;
+};
+
+namespace {
+
+int64_t table_rows(const Dims &d, const std::vector<int> &item_off, std::vector<int> *wrow)
+{
+    int64_t rows = 0;
+    if (wrow) wrow->assign(d.nxyz, 0);
+    for (int Dx = 0; Dx < d.nx; Dx++)
+        for (int Dy = 0; Dy < d.ny; Dy++)
+            for (int Dz = 0; Dz < d.nz; Dz++) {
+                const int Did = (Dx * d.ny + Dy) * d.nz + Dz;
+                const int64_t K = (int64_t)((Dx >> 1) + 1) * ((Dy >> 1) + 1) * ((Dz >> 1) + 1);
+                const int m = item_off[Did + 1] - item_off[Did];
+                if (wrow) (*wrow)[Did] = (int)rows;
+                rows += (K + PT_KC - 1) / PT_KC * (int64_t)((m + 15) & ~15);
+            }
+    return rows;
+}
+
+int download_item_offsets(const Context &c, std::vector<int> &item_off)
+{
+    item_off.resize(c.d.nxyz + 1);
+    GD_CUDA(cudaMemcpy(item_off.data(), c.d_D_item_off, sizeof(int) * (c.d.nxyz + 1), cudaMemcpyDeviceToHost));
+    return GD_OK;
+}
+
+}  // namespace
+
+double pair_tc_bytes(const Context &c)
+{
+    std::vector<int> item_off;
+    if (download_item_offsets(c, item_off)) return 1e300;
+    return (double)table_rows(c.d, item_off, nullptr) * PT_KC * 2.0 * 2.0;
+}
+
+void pair_tc_free(Context &c)
+{
+    if (!c.pair_tc) return;
+    cudaFree(c.pair_tc->wh);
+    cudaFree(c.pair_tc->wl);
+    cudaFree(c.pair_tc->wrow);
+    cudaFree(c.pair_tc->err);
+    delete c.pair_tc;
+    c.pair_tc = nullptr;
+}
+
+int pair_tc_build(Context &c)
+{
+    if (c.pair_tc) return GD_OK;
+    const Dims &d = c.d;
+    std::vector<int> item_off, wrow;
+    int rc = download_item_offsets(c, item_off);
+    if (rc) return rc;
+    const int64_t n_items = item_off[d.nxyz];
+    std::vector<int4> items(n_items + 1);
+    GD_CUDA(cudaMemcpy(items.data(), c.d_D_items, sizeof(int4) * n_items, cudaMemcpyDeviceToHost));
+    const int64_t rows = table_rows(d, item_off, &wrow);
+    if (rows >= ((int64_t)1 << 31)) return set_error(GD_ERR_UNSUPPORTED, "pair weight table too large");
+    const size_t bytes = (size_t)rows * PT_KC * sizeof(__nv_bfloat16);
+    const size_t lim = memory_limit();
+    if (lim && 2 * bytes > lim) return set_error(GD_ERR_OUT_OF_MEMORY, "pair weight table exceeds the memory limit");
+    // dense rows of every group in the class-box layout (x2 * hy + y2) * hz + z2
+    const uint32_t unit = (uint32_t)c.gain_cb * 4u;
+    std::vector<__nv_bfloat16> h(2 * (size_t)rows * PT_KC, __float2bfloat16_rn(0.f));
+    __nv_bfloat16 *hh = h.data(), *hl = h.data() + (size_t)rows * PT_KC;
+    int max_items = 0;
+    for (int Dx = 0; Dx < d.nx; Dx++)
+        for (int Dy = 0; Dy < d.ny; Dy++)
+            for (int Dz = 0; Dz < d.nz; Dz++) {
+                const int Did = (Dx * d.ny + Dy) * d.nz + Dz;
+                const int ex = (Dx >> 1) + 1, ey = (Dy >> 1) + 1, ez = (Dz >> 1) + 1;
+                const int i0 = item_off[Did], m = item_off[Did + 1] - i0, mpad = (m + 15) & ~15;
+                max_items = std::max(max_items, m);
+                for (int t = 0; t < m; t++) {
+                    const int gidx = items[i0 + t].x;
+                    for (int e = c.h_grp_row_off[gidx]; e < c.h_grp_row_off[gidx + 1]; e++) {
+                        const WEntry we = c.h_grp_rows[e];
+                        if (we.w == 0.0f) continue;  // row padding
+                        const int nc = (int)(we.off / unit);
+                        const int z2 = nc % d.hz, y2 = (nc / d.hz) % d.hy, x2 = nc / (d.hz * d.hy);
+                        if (x2 >= ex || y2 >= ey || z2 >= ez) continue;  // P is zero outside B(D)
+                        const int k = (x2 * ey + y2) * ez + z2;
+                        const size_t at = ((size_t)wrow[Did] + (size_t)(k / PT_KC) * mpad + t) * PT_KC + k % PT_KC;
+                        const __nv_bfloat16 hi = __float2bfloat16_rn(we.w);
+                        hh[at] = hi;
+                        hl[at] = __float2bfloat16_rn(we.w - __bfloat162float(hi));
+                    }
+                }
+            }
+    PairTc *pt = new PairTc;
+    pt->rows = rows;
+    pt->max_items = max_items;
+    cudaError_t e1 = cudaMalloc(&pt->wh, bytes), e2 = cudaMalloc(&pt->wl, bytes),
+                e3 = cudaMalloc(&pt->wrow, sizeof(int) * d.nxyz), e4 = cudaMalloc(&pt->err, sizeof(int));
+    if (e1 != cudaSuccess || e2 != cudaSuccess || e3 != cudaSuccess || e4 != cudaSuccess) {
+        cudaFree(pt->wh);
+        cudaFree(pt->wl);
+        cudaFree(pt->wrow);
+        cudaFree(pt->err);
+        delete pt;
+        cudaGetLastError();
+        return set_error(GD_ERR_OUT_OF_MEMORY, "pair weight table allocation");
+    }
+    c.pair_tc = pt;
+    GD_CUDA(cudaMemcpy(pt->wh, hh, bytes, cudaMemcpyHostToDevice));
+    GD_CUDA(cudaMemcpy(pt->wl, hl, bytes, cudaMemcpyHostToDevice));
+    GD_CUDA(cudaMemcpy(pt->wrow, wrow.data(), sizeof(int) * d.nxyz, cudaMemcpyHostToDevice));
+    GD_CUDA(cudaMemset(pt->err, 0, sizeof(int)));
+    return GD_OK;
+}
+
+int pair_tc_check(Context &c, cudaStream_t st)
+{
+    if (!c.pair_tc) return GD_OK;
+    int flag = 0;
+    GD_CUDA(cudaMemcpyAsync(&flag, c.pair_tc->err, sizeof(int), cudaMemcpyDeviceToHost, st));
+    GD_CUDA(cudaStreamSynchronize(st));
+    if (flag) {
+        GD_CUDA(cudaMemset(c.pair_tc->err, 0, sizeof(int)));
+        return set_error(GD_ERR_CUDA, "pair tensor-core gain kernel: a pipeline wait timed out");
+    }
+    return GD_OK;
+}
+
+int run_pair_tc(Context &c, const float *f, int ncells, int ld, float *gain, cudaStream_t st)
+{
+    if (!c.pair_tc) return set_error(GD_ERR_INVALID_ARG, "pair weight table not built");
+    const Dims &d = c.d;
+    const PairTc &pt = *c.pair_tc;
+    const int tiles = (ncells + PT_BM - 1) / PT_BM;
+    const int cells_pad = tiles * PT_BM;
+    // chunks of s: about four waves of one CTA per SM, within the partial buffer
+    const int sms = std::max(1, c.sm_count);
+    int nchunks = (int)std::min<int64_t>(std::max(1, (4 * sms + tiles - 1) / tiles), d.ns);
+    while (nchunks > 1 && (size_t)nchunks * d.n_pnt * cells_pad * sizeof(float) > ((size_t)16 << 30)) nchunks--;
+    const int *d_bounds = nullptr;
+    int rc = gain_bounds_device(c, nchunks, &d_bounds);
+    if (rc) return rc;
+    const size_t part_bytes = (size_t)nchunks * d.n_pnt * cells_pad * sizeof(float);
+    if ((rc = ensure_scratch(c, part_bytes))) return rc;
+    float *part = static_cast<float *>(c.scratch.ptr);
+    GD_CUDA(cudaMemsetAsync(part, 0, part_bytes, st));
+
+    CUtensorMap tWh, tWl;
+    const uint64_t dims[2] = {(uint64_t)PT_KC, (uint64_t)std::max<int64_t>(pt.rows, 16)};
+    const uint64_t strides[1] = {(uint64_t)PT_KC * 2};
+    const uint32_t box[2] = {PT_KC, 16};
+    if ((rc = encode_bf16_sw128(&tWh, pt.wh, 2, dims, strides, box))) return rc;
+    if ((rc = encode_bf16_sw128(&tWl, pt.wl, 2, dims, strides, box))) return rc;
+
+    int max_smem = 0;
+    GD_CUDA(cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, c.device));
+    const size_t cmap_bytes = ((size_t)d.nxyz * 2 + 15) & ~(size_t)15;
+    size_t smem = (size_t)kPtStages * kPtStage + 1024;
+    const bool cmap_smem = smem + cmap_bytes + 512 <= (size_t)max_smem;
+    if (cmap_smem) smem += cmap_bytes;
+    if (smem > (size_t)max_smem) return set_error(GD_ERR_UNSUPPORTED, "pair tensor-core kernel: shared memory");
+    PtArgs a{d, f, ld, ncells, cells_pad, c.d_cmap, c.d_D_item_off, c.d_D_items, c.d_D_members, pt.wrow,
+             d_bounds, part, pt.err};
+    dim3 grid((unsigned)tiles, (unsigned)nchunks);
+    if (cmap_smem) {
+        GD_CUDA(cudaFuncSetAttribute(pair_tc_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        pair_tc_kernel<true><<<grid, kPtThreads, smem, st>>>(tWh, tWl, a);
+    } else {
+        GD_CUDA(cudaFuncSetAttribute(pair_tc_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        pair_tc_kernel<false><<<grid, kPtThreads, smem, st>>>(tWh, tWl, a);
+    }
+    GD_CUDA(cudaGetLastError());
+    if ((rc = reduce_gain_partials(c, part, nchunks, cells_pad, ncells, ld, gain, st))) return rc;
+    // the kernel records a time-out instead of hanging; report it (inside a
+    // stream capture the flag stays set for gd_ctx_check after replay)
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    GD_CUDA(cudaStreamIsCapturing(st, &cap));
+    if (cap != cudaStreamCaptureStatusNone) return GD_OK;
+    return pair_tc_check(c, st);
+}
+
+}  // namespace gd

@@ -194,8 +194,12 @@ int gd_cmatrix_set_cluster(gd_cmatrix *cm, int ctas);
 int gd_cmatrix_check(gd_cmatrix *cm, gd_stream stream);
 /* Gain algorithm used by gd_collision and gd_step for this context:
  * GD_GAIN_PAIR (default, FP32 pair-product kernel), GD_GAIN_CMATRIX_BF16 or
- * GD_GAIN_CMATRIX_BF16X3 (builds the context's collision matrices). */
-enum { GD_GAIN_PAIR = 0, GD_GAIN_CMATRIX_BF16 = 1, GD_GAIN_CMATRIX_BF16X3 = 2 };
+ * GD_GAIN_CMATRIX_BF16X3 (builds the context's collision matrices), or
+ * GD_GAIN_PAIR_TC (the pair-product formulation with its weight contraction on
+ * the tensor cores, pair products and weights split into BF16 hi + lo; builds
+ * a per-class-box weight table of a few GB at 24^3 instead of n^3 matrices,
+ * so it serves the grids whose collision matrices do not fit). */
+enum { GD_GAIN_PAIR = 0, GD_GAIN_CMATRIX_BF16 = 1, GD_GAIN_CMATRIX_BF16X3 = 2, GD_GAIN_PAIR_TC = 3 };
 int gd_ctx_set_gain_path(gd_ctx *ctx, int path);
 
 /* Layout conversion between the full box [nx*ny*nz][ld_box] of the reference
@@ -245,7 +249,8 @@ int gd_batch_info(const gd_batch *b, int *groups, int *streams, int *graph_nodes
  * s-chunk split).  path_mask: bits (1 << GD_GAIN_*) that may be chosen; the
  * collision-matrix paths only when their stored tiles (at most every 256 x 64
  * tile of each G_i's block upper triangle, 2 bytes per entry in BF16, 4 in
- * BF16X3) fit mem_budget bytes.  Allocates a gain buffer for
+ * BF16X3) fit mem_budget bytes, GD_GAIN_PAIR_TC only when its weight table
+ * does.  Allocates a gain buffer for
  * the duration of the call.  Candidates that run out of memory are skipped
  * (cand_ms = -1). */
 #define GD_AUTOTUNE_MAX 8
