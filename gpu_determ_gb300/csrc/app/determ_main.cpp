@@ -11,7 +11,7 @@
 // Option keys beyond the reference's nx, ny, nz, npx: vmin, vmax, R, steps,
 // dt_mode (courant|fixed), courant, dt, out_step, init (reference|two_beam|
 // mixture), seed, results, checkpoint, resume, rows (literal|cells),
-// correction (per_cell|none), gain (pair|bf16|bf16x3).
+// correction (per_cell|none), gain (pair|pair_tc|bf16|bf16x3).
 // rows = literal writes the reference's row set (it reads the [node][cell]
 // arrays with a flat node index, so row "index" is node*npx + cell over the
 // first nx*ny*nz entries); rows = cells writes one row per (node, cell).
@@ -114,7 +114,9 @@ int main(int argc, char **argv)
     init_correction_array(&correction_array, vgrid.device(), opts);
     init_matrices(vgrid.device(), &b, &a, opts);
     if (ro.gain != "pair") {
-        const int path = ro.gain == "bf16" ? GD_GAIN_CMATRIX_BF16 : GD_GAIN_CMATRIX_BF16X3;
+        const int path = ro.gain == "bf16"      ? GD_GAIN_CMATRIX_BF16
+                         : ro.gain == "pair_tc" ? GD_GAIN_PAIR_TC
+                                                : GD_GAIN_CMATRIX_BF16X3;
         if (gd_ctx_set_gain_path(vgrid.device().context(), path) != GD_OK) {
             std::cerr << "gain path " << ro.gain << ": " << gd_last_error() << std::endl;
             return 5;

@@ -183,8 +183,8 @@ void load_run_options(RunOptions &ro, const std::string &fname)
         else if (key == "rows") ro.literal_rows = (value != "cells");
         else if (key == "correction") ro.correction = (value != "none");
         else if (key == "gain") {
-            if (value != "pair" && value != "bf16" && value != "bf16x3")
-                throw std::runtime_error("gain must be pair, bf16 or bf16x3, not '" + value + "'");
+            if (value != "pair" && value != "pair_tc" && value != "bf16" && value != "bf16x3")
+                throw std::runtime_error("gain must be pair, pair_tc, bf16 or bf16x3, not '" + value + "'");
             ro.gain = value;
         }
     });

@@ -58,7 +58,8 @@ struct RunOptions {
     std::string resume;       // key "resume": checkpoint file to start from
     bool literal_rows = true; // key "rows": literal (reference row order) | cells
     bool correction = true;   // key "correction": per_cell | none
-    std::string gain = "pair";  // key "gain": pair (FP32 kernel) | bf16 | bf16x3 (collision matrices)
+    std::string gain = "pair";  // key "gain": pair (FP32 kernel) | pair_tc (its contraction on tensor cores) |
+                                // bf16 | bf16x3 (collision matrices)
 };
 void load_run_options(RunOptions &, const std::string &);
 

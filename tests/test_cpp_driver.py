@@ -77,21 +77,23 @@ def test_checkpoint_resume_is_exact(cuda, gdlib, tmp_path):
 
 
 def test_driver_tensor_core_gain(cuda, gdlib, tmp_path):
-    """`gain = bf16x3` in the options file runs the same driver on the
-    collision matrices: results.out within 1e-4 (relative to each column's
-    largest value) of the FP32 pair kernel's; an unknown gain is refused."""
+    """`gain = bf16x3` (collision matrices) or `gain = pair_tc` (pair products
+    with the contraction on the tensor cores) in the options file runs the
+    same driver: results.out within 1e-4 (relative to each column's largest
+    value) of the FP32 pair kernel's; an unknown gain is refused."""
     base = "nx = 8\nny = 8\nnz = 8\nnpx = 64\ninit = mixture\nseed = 2\nrows = cells\nsteps = 2\n"
     cols = []
-    for gain in ("pair", "bf16x3"):
+    for gain in ("pair", "bf16x3", "pair_tc"):
         d = tmp_path / gain
         d.mkdir()
         r = run_driver(gdlib, d, base + f"gain = {gain}\n")
         assert r.returncode == 0, r.stdout + r.stderr
         cols.append(np.array([[float(v) for v in l.split()[4:9]] for l in open(d / "results.out")]))
-    a, b = cols
-    assert a.shape == b.shape and a.shape[0] > 0
-    for k in range(4):  # F, DC, IC, CI
-        assert np.max(np.abs(a[:, k] - b[:, k])) <= 1e-4 * np.max(np.abs(a[:, k]))
+    a = cols[0]
+    for b in cols[1:]:
+        assert a.shape == b.shape and a.shape[0] > 0
+        for k in range(4):  # F, DC, IC, CI
+            assert np.max(np.abs(a[:, k] - b[:, k])) <= 1e-4 * np.max(np.abs(a[:, k]))
     bad = tmp_path / "bad"
     bad.mkdir()
     r = run_driver(gdlib, bad, base + "gain = fp8\n")
