@@ -806,7 +806,7 @@ double cmatrix_bytes_bound(const Context &c, int mode)
 int encode_bf16_sw128(CUtensorMap *m, void *ptr, int rank, const uint64_t *dims, const uint64_t *strides,
                       const uint32_t *box)
 {
-    EncodeTiled fn;
+    EncodeTiled fn = nullptr;
     int rc = get_encoder(&fn);
     if (rc) return rc;
     cuuint64_t dd[5], ss[4];

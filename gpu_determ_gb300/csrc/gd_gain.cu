@@ -89,7 +89,6 @@ __global__ void __launch_bounds__(kThreads, 1) gain_pair_kernel(GainArgs a)
                   Dz = min(sz, 2 * d.nz - 2 - sz);
         const int ex = (Dx >> 1) + 1, ey = (Dy >> 1) + 1, ez = (Dz >> 1) + 1;
         const int px = sx & 1, py = sy & 1, pz = sz & 1;
-        const int nB = ex * ey * ez;
 
         // 1. pair products P_s[n] on B(D(s)); zeros where only the previous
         //    s's box had values, so P_s is zero outside B(D(s)) and the rows
@@ -113,7 +112,7 @@ __global__ void __launch_bounds__(kThreads, 1) gain_pair_kernel(GainArgs a)
             // two pair products per iteration: 16 independent loads in flight
             for (int c2 = 0; c2 < ez; c2 += 2) {
                 const bool two = c2 + 1 < ez;
-                const int nz0 = 2 * c2 + pz, nz1 = nz0 + 2;
+                const int nz0 = 2 * c2 + pz;
                 const int lz0 = (sz + nz0) >> 1, l1z0 = (sz - nz0) >> 1;
                 const int lz1 = two ? lz0 + 1 : lz0, l1z1 = two ? l1z0 - 1 : l1z0;
                 const int k0 = cmap[A + lz0], k1 = cmap[B + l1z0], k2 = cmap[Cc + l1z0], k3 = cmap[Dd + lz0];
@@ -382,7 +381,6 @@ int reduce_gain_partials(Context &c, const float *part, int nchunks, int cells_p
 int gain_launch_shape(Context &c, int ncells, int *cb_out, size_t *smem_out, int *nblk_out,
                       int *chunks_out)
 {
-    const Dims &d = c.d;
     const int cb = c.gain_cb;
     const int nblk = (ncells + cb - 1) / cb;
     const int nchunks = gain_chunk_count(c, nblk);
