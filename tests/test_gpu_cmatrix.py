@@ -150,3 +150,40 @@ def test_headline_grid_against_pair_kernel(cuda, gdlib):
         rel = float((outs[0][:, :nc] - ref).norm() / ref.norm())
         assert rel <= tol, (mode, rel)
         cm.close()
+
+
+def test_c2_batch_against_fp64_oracle(cuda, gdlib):
+    """Config C2 (16^3, R = 4.8): seeded mixtures of 1-3 Maxwellians with
+    n ~ lognormal(0, 0.3), u ~ N(0, 0.7^2) per axis, T ~ U[0.6, 1.8]; the gain
+    and the FP64-projected Q of every gain path against the FP64 oracle.
+    GD_C2_CELLS sets the batch (the config's 1024; 256 by default so the
+    oracle's CPU time stays short)."""
+    import os
+    torch = cuda
+    nc = int(os.environ.get("GD_C2_CELLS", "256"))
+    spec = gdlib.GridSpec(16, R=4.8)
+    ctx = gdlib.Context(spec)
+    f = inputs.mixtures(spec.fill(), nc, seed=2024)
+    o = Oracle(16, R=4.8)
+    nu_ref = o.loss_f64(o.to_box(f))
+    i_ref = o.gain_f64(o.to_box(f))
+    _, q_ref, _, _ = o.project(f, nu_ref, i_ref)
+    ft = torch.from_numpy(f).cuda()
+    tols = {gdlib.GAIN_PAIR: (1e-5, 1e-4), gdlib.GAIN_PAIR_TC: (2e-5, 2e-4),
+            gdlib.GAIN_CMATRIX_BF16X3: (2e-5, 2e-4), gdlib.GAIN_CMATRIX_BF16: (5e-3, 5e-3)}
+    report = {}
+    for path, (tol_i, tol_q) in tols.items():
+        ctx.set_gain_path(path)
+        nu, gain = torch.empty_like(ft), torch.empty_like(ft)
+        q = torch.zeros(ft.shape, dtype=torch.float64, device="cuda")
+        ctx.collision(ft, nc, nc, nu, gain)
+        ctx.project(ft, nu, gain, nc, nc, q=q)
+        ctx.check()
+        g = gain.cpu().numpy().astype(np.float64)
+        qq = q.cpu().numpy()
+        rel_i = np.linalg.norm(g - i_ref) / np.linalg.norm(i_ref)
+        rel_q = np.linalg.norm(qq - q_ref) / np.linalg.norm(q_ref)
+        cell_q = np.linalg.norm(qq - q_ref, axis=0) / np.linalg.norm(q_ref, axis=0)
+        report[path] = (rel_i, rel_q, float(np.median(cell_q)), float(np.quantile(cell_q, 0.99)))
+        assert rel_i <= tol_i and rel_q <= tol_q, (path, report[path])
+    print("C2 16^3,", nc, "cells: path -> (gain rel-L2, Q rel-L2, Q per-cell median, p99) vs FP64:", report)

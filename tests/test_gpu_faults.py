@@ -61,6 +61,9 @@ def test_memory_limit(gdlib, cuda):
         with pytest.raises(gdlib.GDError) as e:
             gdlib.Mlp(ctx.n_pnt, ctx.n_pnt, batch_cap=256)
         assert e.value.code == 3
+        with pytest.raises(gdlib.GDError) as e:
+            ctx.set_gain_path(gdlib.GAIN_PAIR_TC)      # its per-box weight table
+        assert e.value.code == 3
         # the context keeps working on the pair kernel
         q = _q(ctx, f, 64, torch)
         ctx.check()
@@ -68,4 +71,6 @@ def test_memory_limit(gdlib, cuda):
     finally:
         gdlib.set_memory_limit(0)
     ctx.set_gain_path(gdlib.GAIN_CMATRIX_BF16)
+    ctx.check()
+    ctx.set_gain_path(gdlib.GAIN_PAIR_TC)
     ctx.check()
