@@ -309,11 +309,11 @@ def run_ours(args):
     if model is None:
         line["gpu_launches"] = plain_launches * args.steps
     else:
-        # loss 4 (f conversion + 3 GEMMs), network 8, nu f 1, error network 8,
-        # selection 1, projection 1, relaxation 3; plain gain 2 (f conversion +
-        # matrices) when any cell falls back, plus gather 1 and scatter 1 when
-        # only some do
-        line["gpu_launches"] = sum(26 + (0 if k == 0 else 2 if k == nc else 4) for k in fb_timed)
+        # loss 4 (f conversion + 3 GEMMs), error network 8, selection 1,
+        # projection 1, relaxation 3; then either the plain gain 2 (f conversion
+        # + matrices) in place when every cell falls back, or the network 8 and
+        # nu f 1, plus gather 1, plain gain 2 and scatter 1 when some cells do
+        line["gpu_launches"] = sum(17 + (2 if k == nc else 9 + (4 if k > 0 else 0)) for k in fb_timed)
         rep = surrogate_report(args, gd, ctx, model, f0, nc, stream, fit_s, fb_timed, plain_value)
         rep["speedup_vs_plain"] = value / plain_value
         line["accuracy"] = next(c for c in rep["tolerance_curve"] if c["tol"] == args.tol)

@@ -1,12 +1,14 @@
 // gd_surrogate.cu -- collision gain from the learned surrogate with the plain
 // method as fallback.
 //
-// Per call: the loss frequency nu is computed exactly (loss kernel); the
-// network predicts Q for every cell, giving the gain I = Q + nu f; an error
+// Per call: the loss frequency nu is computed exactly (loss kernel); an error
 // network predicts log10 of each cell's relative L2 error; cells whose
 // estimate exceeds log10(tol) (or is not finite) are compacted in ascending
-// order, their f gathered into a dense block, their gain recomputed by the
-// context's plain gain path and scattered back.  The caller then applies the
+// order.  When every cell falls back, the context's plain gain runs in place
+// and the network is not evaluated.  Otherwise the network predicts Q for
+// every cell, giving the gain I = Q + nu f, and the fallback cells' f is
+// gathered into a dense block, their gain recomputed by the context's plain
+// gain path and scattered back.  The caller then applies the
 // FP64 conservation projection (gd_project) as for the plain method, so every
 // cell's Q conserves mass, momentum and energy whichever path produced it.
 #include <cuda_runtime.h>
@@ -198,28 +200,33 @@ extern "C" int gd_surrogate_gain(gd_surrogate *s, const float *f, int ncells, in
         if (n_fallback) *n_fallback = ncells;
         return GD_OK;
     }
+    // the exact loss, then the error estimate decides which cells take the
+    // plain gain; the network runs only when some cell keeps its output
     if ((rc = gd_collision(s->ctx, f, ncells, ld, nu, nullptr, stream))) return rc;
-    if ((rc = gd_mlp_forward(s->net, f, ld, ncells, gain, ld, stream))) return rc;
-    add_loss_kernel<<<grid_for((int64_t)s->n * ncells), 256, 0, st>>>(gain, nu, f, s->n, ncells, ld);
-    GD_CUDA(cudaGetLastError());
     if (s->est && (rc = gd_mlp_forward(s->est, f, ld, ncells, s->est_buf, ncells, stream))) return rc;
     select_kernel<<<1, 1024, 0, st>>>(s->est ? s->est_buf : nullptr, ncells, std::log10(tol), 0, s->idx, s->d_count);
     GD_CUDA(cudaGetLastError());
     GD_CUDA(cudaMemcpyAsync(s->h_count, s->d_count, sizeof(int), cudaMemcpyDeviceToHost, st));
-    if ((rc = gd_mlp_check(s->net, stream))) return rc;  // synchronises the stream
+    GD_CUDA(cudaStreamSynchronize(st));
     if (s->est && (rc = gd_mlp_check(s->est, stream))) return rc;
     const int count = *s->h_count;
     if (count == ncells) {
         // every cell falls back: the plain gain straight into place (the same
         // launch as gathering all cells in order would make)
         if ((rc = gd_collision(s->ctx, f, ncells, ld, nullptr, gain, stream))) return rc;
-    } else if (count > 0) {
-        const int64_t tot = (int64_t)s->n * count;
-        gather_cells_kernel<<<grid_for(tot), 256, 0, st>>>(f, ld, s->idx, count, s->n, s->fs, count);
+    } else {
+        if ((rc = gd_mlp_forward(s->net, f, ld, ncells, gain, ld, stream))) return rc;
+        add_loss_kernel<<<grid_for((int64_t)s->n * ncells), 256, 0, st>>>(gain, nu, f, s->n, ncells, ld);
         GD_CUDA(cudaGetLastError());
-        if ((rc = gd_collision(s->ctx, s->fs, count, count, nullptr, s->gs, stream))) return rc;
-        scatter_cells_kernel<<<grid_for(tot), 256, 0, st>>>(s->gs, count, s->idx, count, s->n, gain, ld);
-        GD_CUDA(cudaGetLastError());
+        if (count > 0) {
+            const int64_t tot = (int64_t)s->n * count;
+            gather_cells_kernel<<<grid_for(tot), 256, 0, st>>>(f, ld, s->idx, count, s->n, s->fs, count);
+            GD_CUDA(cudaGetLastError());
+            if ((rc = gd_collision(s->ctx, s->fs, count, count, nullptr, s->gs, stream))) return rc;
+            scatter_cells_kernel<<<grid_for(tot), 256, 0, st>>>(s->gs, count, s->idx, count, s->n, gain, ld);
+            GD_CUDA(cudaGetLastError());
+        }
+        if ((rc = gd_mlp_check(s->net, stream))) return rc;  // synchronises the stream
     }
     if (est_out) {
         if (s->est)
