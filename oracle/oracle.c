@@ -1,8 +1,8 @@
 /*
  * oracle.c -- CPU restatement of the gpu_determ collision-integral path.
  *
- * TEST INFRASTRUCTURE ONLY: the checker for the CUDA kernels and the timed
- * OpenMP host baseline.  Nothing in the product links it.
+ * TEST INFRASTRUCTURE ONLY: the oracle the CUDA kernels are tested against, and
+ * the timed OpenMP host baseline.  Nothing in the product links it.
  *
  * Built with -ffp-contract=off so that float and double expressions round
  * exactly as written (the reference's host code is compiled that way on

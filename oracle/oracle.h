@@ -1,7 +1,7 @@
 /*
  * oracle.h -- CPU restatement of the gpu_determ collision-integral path.
  *
- * TEST INFRASTRUCTURE ONLY.  This library is the checker for the CUDA path in
+ * TEST INFRASTRUCTURE ONLY.  This library is the oracle for the CUDA path in
  * gpu_determ_gb300/csrc: tests, the smoke check and the CPU-baseline leg of
  * bench.py load it; the product never links or calls it.
  *

@@ -1,7 +1,8 @@
 """numpy/ctypes view of the oracle library (test infrastructure only).
 
 Imported by tests/, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
-bench.py, as the checker.  The product path never imports this module.
+bench.py, as the oracle results are compared with.  The product path never
+imports this module.
 """
 from __future__ import annotations
 
