@@ -17,7 +17,7 @@
 // groups run as several passes of at most 256 groups, each forming P again.
 //
 // One CTA per (128-cell tile, chunk of s), warp-specialized:
-//   warps 10..17 pair products of one 64-offset chunk for the 128 cells (thread
+//   warps 14..21 pair products of one 64-offset chunk for the 128 cells (thread
 //                = cell, eight gathers of f per product, the FP32 products of
 //                the FP32 kernel), split into BF16 hi/lo and written to shared
 //                memory in the MMA's 128-byte-swizzled K-major layout; two
@@ -25,9 +25,10 @@
 //   warp 0       TMA loads of the chunk's weight rows (hi, lo), 16 rows a box;
 //   warp 1       tcgen05.mma (M = 128 cells, N = groups padded to 16, K = 16)
 //                into one of two TMEM accumulators per (s, pass);
-//   warps 2..9   read C^T from TMEM (thread = cell; two warps per lane quadrant
-//                taking alternate blocks of 16 groups) and add each group's sum
-//                to the CTA's partial outputs at its members' targets (s +- g)/2.
+//   warps 2..13  read C^T from TMEM (thread = cell; three warps per lane
+//                quadrant taking every third block of 16 groups) and add each
+//                group's sum, by fire-and-forget reductions, to the CTA's
+//                partial outputs at its members' targets (s +- g)/2.
 // Within one s every target receives one update and the epilogue takes the
 // units in s order, so every partial sum is formed in a fixed order; the
 // chunk partials are added in chunk order.  Results are bitwise reproducible.
@@ -55,7 +56,7 @@ constexpr uint32_t kPTile = PT_BM * PT_KC * 2;     // 16 KB: P part of one chunk
 constexpr uint32_t kWTile = PT_NMAX * PT_KC * 2;   // 32 KB: W part of one chunk (up to 256 rows)
 constexpr uint32_t kPtStage = 2 * kPTile + 2 * kWTile;  // P hi, P lo, W hi, W lo
 constexpr int kPtStages = 2;
-constexpr int kEpiWarps = 8;             // two per TMEM lane quadrant
+constexpr int kEpiWarps = 12;            // three per TMEM lane quadrant
 constexpr int kProdWarps = 8;            // two groups of four
 constexpr int kPtThreads = 32 * (2 + kEpiWarps + kProdWarps);
 
@@ -240,9 +241,9 @@ __global__ void __launch_bounds__(kPtThreads, 1)
         }
     } else if (warp < 2 + kEpiWarps) {
         // ---- epilogue: thread = cell = TMEM lane (warp % 4 is the lane quadrant it
-        // may read); the two warps of a quadrant take alternate 16-group blocks ----
+        // may read); the quadrant's warps take every third 16-group block -------
         const int quad = warp & 3;
-        const int half = (warp - 2) >> 2;
+        const int third = (warp - 2) >> 2;  // which of the quadrant's warps
         const int row = quad * 32 + lane;
         const int cell = m_tile * PT_BM + row;
         const bool live = cell < a.ncells;
@@ -256,9 +257,9 @@ __global__ void __launch_bounds__(kPtThreads, 1)
                 unit_of(a, sl, q, u);
                 const int buf = uc & 1;
                 if (lane == 0 && !mbar_wait(smem_u32(&accf_bar[buf]), (uint32_t)(uc >> 1) & 1u, a.err)) epi_fail = 1;
-                // both warps of a cell finish one unit before either starts the
-                // next (their targets may coincide across units); the decision to
-                // stop is taken after the barrier, by all of them alike
+                // all warps of a cell finish one unit before any starts the next
+                // (their targets may coincide across units); the decision to stop
+                // is taken after the barrier, by all of them alike
                 asm volatile("bar.sync 1, %0;" ::"n"(32 * kEpiWarps) : "memory");
                 if (*(volatile int *)&epi_fail) {
                     ok = false;
@@ -266,7 +267,7 @@ __global__ void __launch_bounds__(kPtThreads, 1)
                 }
                 asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
                 const uint32_t taddr = tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(buf * PT_NMAX);
-                for (int m0 = half * 16; m0 < u.mcnt; m0 += 32) {
+                for (int m0 = third * 16; m0 < u.mcnt; m0 += 16 * (kEpiWarps / 4)) {
                     float v[16];
                     tmem_ld16(taddr + (uint32_t)m0, v);
                     if (!live) continue;
@@ -274,35 +275,29 @@ __global__ void __launch_bounds__(kPtThreads, 1)
                     for (int t = 0; t < mend; t++) {
                         const int4 item = __ldg(a.D_items + u.it0 + m0 + t);
                         const float acc = v[t];
-                        // explicit load/add/store: global float reductions flush
-                        // subnormal values to zero, and corner-node contributions
-                        // are subnormal.  Within one s the targets of all members
-                        // are distinct, so two members go at a time.
-                        for (int mm = item.y; mm < item.z; mm += 2) {
-                            const bool two = mm + 1 < item.z;
-                            int tgt[16];
-                            float old[16];
+                        // fire-and-forget reductions: within one s every target
+                        // receives one update, and the units of one cell are
+                        // ordered by the epilogue barrier, so each partial sum
+                        // still accumulates in s order (bitwise reproducible);
+                        // like the tensor-core products, the reduction flushes
+                        // subnormal contributions to zero
+                        for (int mm = item.y; mm < item.z; mm++) {
+                            const uint32_t pk = __ldg(a.D_members + mm);
+                            const int gx = 2 * (int)(pk & 31) + u.px, gy = 2 * (int)((pk >> 6) & 31) + u.py,
+                                      gz = 2 * (int)((pk >> 12) & 31) + u.pz;
+                            const int X0 = ((u.sx - gx) >> 1) * d.nyz, X1 = X0 + gx * d.nyz;
+                            const int Y0 = ((u.sy - gy) >> 1) * d.nz, Y1 = Y0 + gy * d.nz;
+                            const int Z0 = (u.sz - gz) >> 1, Z1 = Z0 + gz;
 #pragma unroll
-                            for (int h2 = 0; h2 < 2; h2++) {
-                                const uint32_t pk = __ldg(a.D_members + (h2 && two ? mm + 1 : mm));
-                                const int gx = 2 * (int)(pk & 31) + u.px, gy = 2 * (int)((pk >> 6) & 31) + u.py,
-                                          gz = 2 * (int)((pk >> 12) & 31) + u.pz;
-                                const int X0 = ((u.sx - gx) >> 1) * d.nyz, X1 = X0 + gx * d.nyz;
-                                const int Y0 = ((u.sy - gy) >> 1) * d.nz, Y1 = Y0 + gy * d.nz;
-                                const int Z0 = (u.sz - gz) >> 1, Z1 = Z0 + gz;
-#pragma unroll
-                                for (int sg = 0; sg < 8; sg++) {
-                                    const bool hx = sg & 1, hy = (sg >> 1) & 1, hz = (sg >> 2) & 1;
-                                    const bool dup = (hx && gx == 0) || (hy && gy == 0) || (hz && gz == 0) ||
-                                                     (h2 && !two);
-                                    const int tg = dup ? -1 : cmap[(hx ? X1 : X0) + (hy ? Y1 : Y0) + (hz ? Z1 : Z0)];
-                                    tgt[h2 * 8 + sg] = tg;
-                                    old[h2 * 8 + sg] = tg >= 0 ? part[(size_t)tg * a.cells_pad] : 0.f;
-                                }
+                            for (int sg = 0; sg < 8; sg++) {
+                                const bool hx = sg & 1, hy = (sg >> 1) & 1, hz = (sg >> 2) & 1;
+                                const bool dup = (hx && gx == 0) || (hy && gy == 0) || (hz && gz == 0);
+                                const int tg = dup ? -1 : cmap[(hx ? X1 : X0) + (hy ? Y1 : Y0) + (hz ? Z1 : Z0)];
+                                if (tg >= 0)
+                                    asm volatile("red.relaxed.gpu.global.add.f32 [%0], %1;" ::"l"(part + (size_t)tg * a.cells_pad),
+                                                 "f"(acc)
+                                                 : "memory");
                             }
-#pragma unroll
-                            for (int e = 0; e < 16; e++)
-                                if (tgt[e] >= 0) part[(size_t)tgt[e] * a.cells_pad] = old[e] + acc;
                         }
                     }
                 }
