@@ -2,7 +2,7 @@
 
     python -m gpu_determ_gb300.large [--grid 32] [--radius 5.5] [--cells 16384] [--steps 200]
                                      [--pairs 65536] [--train-steps 4000] [--tol 1e-3]
-                                     [--check-every 1] [--seed 0]
+                                     [--gain pair_tc] [--check-gain pair] [--check-every 1] [--seed 0]
 
 Cells carry one Maxwellian each from a 2-D lid-driven-style field
 (inputs.cavity_field: divergence-free sinusoidal flow, |u| <= 0.8,
@@ -11,9 +11,13 @@ with FP32 accumulation) is trained first on mixtures of 1-4 Maxwellians
 labelled by the plain method of the same context (surrogate.fit).  Each step
 is: loss nu, surrogate gain with plain fallback above the tolerance
 (gd_surrogate_gain), FP64 conservation projection, Courant relaxation
-(dt = courant / max nu' as relax_f).  On check steps the plain FP32 gain of the
-same f (the context's plain path, its FP32 pair kernel at this size) gives the
-step's relative L2 error of Q and the conservation error of the projected Q.
+(dt = courant / max nu' as relax_f).  The plain method (training labels,
+fallback, plain-step timing) is the --gain path: at 32^3 the collision matrices
+do not fit, and the pair products with the contraction on the tensor cores
+(pair_tc) run twice as fast as the FP32 pair kernel (pair) at ~6e-7 from it.
+On check steps the --check-gain path (by default the plain FP32 kernel, on a
+second context) gives the plain Q of the same f, hence the step's relative L2
+error of Q, and the conservation error of the projected Q is measured.
 
 Reported: per checked step the fallback fraction, batch and per-cell relative
 L2 of Q, conservation error; totals: surrogate-step cells*steps/s (CUDA
@@ -28,18 +32,27 @@ import math
 import sys
 import time
 
-from . import DT_COURANT, Context, GridSpec, cell_rel_l2, inputs
+from . import DT_COURANT, GAIN_PAIR, GAIN_PAIR_TC, Context, GridSpec, cell_rel_l2, inputs
+
+GAINS = {"pair": GAIN_PAIR, "pair_tc": GAIN_PAIR_TC}
 
 
 def run(grid: int = 32, radius: float = 5.5, cells: int = 16384, steps: int = 200, pairs: int = 65536,
         train_steps: int = 4000, tol: float = 1e-3, check_every: int = 1, courant: float = 0.5, seed: int = 0,
         est_pairs: int = 16384, est_steps: int = 1500, calib_pairs: int = 4096, plain_steps: int = 2,
-        device: int = 0, log=None) -> dict:
+        gain: str = "pair_tc", check_gain: str = "pair", device: int = 0, log=None) -> dict:
     import torch
     from . import surrogate as S
     dev = torch.device("cuda", device)
+    plain_name, check_name = gain, check_gain
     spec = GridSpec(grid, R=radius)
     ctx = Context(spec, device=device)
+    ctx.set_gain_path(GAINS[gain])
+    if check_gain == gain:
+        check_ctx = ctx
+    else:
+        check_ctx = Context(spec, device=device)
+        check_ctx.set_gain_path(GAINS[check_gain])
     g = spec.fill()
     n = ctx.n_pnt
     stream = torch.cuda.current_stream(dev)
@@ -75,8 +88,8 @@ def run(grid: int = 32, radius: float = 5.5, cells: int = 16384, steps: int = 20
         if check:
             e1.record(stream)
             # plain Q of the same f, before the relaxation changes it
-            ctx.collision(f, cells, cells, nu_p, gain_p, stream=stream)
-            ctx.project(f, nu_p, gain_p, cells, cells, q=q_p, stream=stream)
+            check_ctx.collision(f, cells, cells, nu_p, gain_p, stream=stream)
+            check_ctx.project(f, nu_p, gain_p, cells, cells, q=q_p, stream=stream)
             cell_rel_l2(q, cells, q_p, cells, n, cells, err, stream=stream)
             rec = {"step": k, "fallback_fraction": nfb / cells,
                    "batch_rel_l2": float((q - q_p).norm() / q_p.norm()),
@@ -122,7 +135,7 @@ def run(grid: int = 32, radius: float = 5.5, cells: int = 16384, steps: int = 20
     value = cells * steps / (ms_total * 1e-3)
     plain_value = cells / (plain_ms * 1e-3)
     return {"grid": grid, "radius": radius, "n_pnt": n, "cells": cells, "steps": steps, "tol": tol,
-            "plain_gain": "FP32 pair kernel", "fit": model.report, "fit_s": round(fit_s, 1),
+            "plain_gain": plain_name, "check_gain": check_name, "fit": model.report, "fit_s": round(fit_s, 1),
             "surrogate_step": {"cell_steps_per_s": value, "ms_per_step": ms_total / steps,
                                "fallback_fraction": fallbacks / (cells * steps)},
             "plain_step": {"cell_steps_per_s": plain_value, "ms_per_step": plain_ms, "steps": plain_steps},
@@ -144,12 +157,15 @@ def main(argv=None):
     p.add_argument("--tol", type=float, default=1e-3)
     p.add_argument("--check-every", type=int, default=1)
     p.add_argument("--plain-steps", type=int, default=2)
+    p.add_argument("--gain", choices=sorted(GAINS), default="pair_tc",
+                   help="plain method: labels, fallback and the timed plain step")
+    p.add_argument("--check-gain", choices=sorted(GAINS), default="pair", help="plain method of the per-step checks")
     p.add_argument("--seed", type=int, default=0)
     a = p.parse_args(argv)
     log = lambda s: print(s, file=sys.stderr, flush=True)
     res = run(a.grid, a.radius, a.cells, a.steps, a.pairs, a.train_steps, a.tol, a.check_every, seed=a.seed,
               est_pairs=a.est_pairs, est_steps=a.est_steps, calib_pairs=a.calib_pairs,
-              plain_steps=a.plain_steps, log=log)
+              plain_steps=a.plain_steps, gain=a.gain, check_gain=a.check_gain, log=log)
     print(json.dumps(res))
     return 0 if math.isfinite(res["surrogate_step"]["cell_steps_per_s"]) else 1
 

@@ -21,8 +21,8 @@ def test_batched_runner_small(cuda, gdlib):
 
 def test_large_runner_small(cuda, gdlib):
     """The 32^3 runner's code path on a 12^3 lattice: surrogate trained on a
-    few thousand pairs, cavity-field cells, per-step checks against the plain
-    gain, with fallback above the tolerance."""
+    few thousand pairs, cavity-field cells, the tensor-core pair path as the
+    plain method and fallback, per-step checks against the FP32 pair kernel."""
     from gpu_determ_gb300 import large
     res = large.run(grid=12, radius=4.8, cells=256, steps=3, pairs=2048, train_steps=300, tol=1e-3,
                     est_pairs=1024, est_steps=200, calib_pairs=1024, plain_steps=1)
@@ -33,7 +33,10 @@ def test_large_runner_small(cuda, gdlib):
         assert 0.0 <= rec["fallback_fraction"] <= 1.0
         assert rec["conservation_max"] < 1e-11
         if rec["fallback_fraction"] == 1.0:
-            assert rec["batch_rel_l2"] == 0.0
+            # the fallback is the tensor-core pair path: its gain is ~1e-6 from the
+            # FP32 kernel's, and Q = I - nu f of these near-Maxwellian cells is
+            # small next to I, which magnifies that difference ~30-fold
+            assert rec["batch_rel_l2"] < 1e-4
     assert res["surrogate_step"]["cell_steps_per_s"] > 0 and res["plain_step"]["cell_steps_per_s"] > 0
     assert max(res["moment_drift"].values()) < 1e-5
     assert np.isfinite(res["time"]) and res["time"] > 0
