@@ -210,8 +210,9 @@ int gd_box_to_compact(gd_ctx *ctx, const float *box, int ncells, int ld_box, flo
 int gd_compact_to_box(gd_ctx *ctx, const float *compact, int ncells, int ld, float *box, int ld_box,
                       gd_stream stream);
 
-/* Gain I[i][c] exactly as gd_collision computes it, but with no device
- * allocation of any kind during the call.  No counterpart in the reference:
+/* Gain I[i][c] exactly as gd_collision computes it on the FP32 pair kernel
+ * (GD_GAIN_PAIR, whichever gain path the context has selected), but with no
+ * device allocation of any kind during the call.  No counterpart in the reference:
  * it exists for callers that cannot let a library call cudaMalloc (a custom
  * allocator or memory pool owns the device, a latency-critical loop must not
  * hit cudaMalloc's implicit synchronisation, or allocation is forbidden after
