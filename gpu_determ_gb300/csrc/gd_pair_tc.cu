@@ -486,37 +486,8 @@ int pair_tc_build(Context &c)
     const size_t bytes = (size_t)rows * PT_KC * sizeof(__nv_bfloat16);
     const size_t lim = memory_limit();
     if (lim && 2 * bytes > lim) return set_error(GD_ERR_OUT_OF_MEMORY, "pair weight table exceeds the memory limit");
-    // dense rows of every group in the class-box layout (x2 * hy + y2) * hz + z2
-    const uint32_t unit = (uint32_t)c.gain_cb * 4u;
-    std::vector<__nv_bfloat16> h(2 * (size_t)rows * PT_KC, __float2bfloat16_rn(0.f));
-    __nv_bfloat16 *hh = h.data(), *hl = h.data() + (size_t)rows * PT_KC;
-    int max_items = 0;
-    for (int Dx = 0; Dx < d.nx; Dx++)
-        for (int Dy = 0; Dy < d.ny; Dy++)
-            for (int Dz = 0; Dz < d.nz; Dz++) {
-                const int Did = (Dx * d.ny + Dy) * d.nz + Dz;
-                const int ex = (Dx >> 1) + 1, ey = (Dy >> 1) + 1, ez = (Dz >> 1) + 1;
-                const int i0 = item_off[Did], m = item_off[Did + 1] - i0, mpad = (m + 15) & ~15;
-                max_items = std::max(max_items, m);
-                for (int t = 0; t < m; t++) {
-                    const int gidx = items[i0 + t].x;
-                    for (int e = c.h_grp_row_off[gidx]; e < c.h_grp_row_off[gidx + 1]; e++) {
-                        const WEntry we = c.h_grp_rows[e];
-                        if (we.w == 0.0f) continue;  // row padding
-                        const int nc = (int)(we.off / unit);
-                        const int z2 = nc % d.hz, y2 = (nc / d.hz) % d.hy, x2 = nc / (d.hz * d.hy);
-                        if (x2 >= ex || y2 >= ey || z2 >= ez) continue;  // P is zero outside B(D)
-                        const int k = (x2 * ey + y2) * ez + z2;
-                        const size_t at = ((size_t)wrow[Did] + (size_t)(k / PT_KC) * mpad + t) * PT_KC + k % PT_KC;
-                        const __nv_bfloat16 hi = __float2bfloat16_rn(we.w);
-                        hh[at] = hi;
-                        hl[at] = __float2bfloat16_rn(we.w - __bfloat162float(hi));
-                    }
-                }
-            }
     PairTc *pt = new PairTc;
     pt->rows = rows;
-    pt->max_items = max_items;
     cudaError_t e1 = cudaMalloc(&pt->wh, bytes), e2 = cudaMalloc(&pt->wl, bytes),
                 e3 = cudaMalloc(&pt->wrow, sizeof(int) * d.nxyz), e4 = cudaMalloc(&pt->err, sizeof(int));
     if (e1 != cudaSuccess || e2 != cudaSuccess || e3 != cudaSuccess || e4 != cudaSuccess) {
@@ -528,11 +499,73 @@ int pair_tc_build(Context &c)
         cudaGetLastError();
         return set_error(GD_ERR_OUT_OF_MEMORY, "pair weight table allocation");
     }
-    c.pair_tc = pt;
-    GD_CUDA(cudaMemcpy(pt->wh, hh, bytes, cudaMemcpyHostToDevice));
-    GD_CUDA(cudaMemcpy(pt->wl, hl, bytes, cudaMemcpyHostToDevice));
-    GD_CUDA(cudaMemcpy(pt->wrow, wrow.data(), sizeof(int) * d.nxyz, cudaMemcpyHostToDevice));
-    GD_CUDA(cudaMemset(pt->err, 0, sizeof(int)));
+    c.pair_tc = pt;  // a failure below frees it again
+    if (cudaMemcpy(pt->wrow, wrow.data(), sizeof(int) * d.nxyz, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemset(pt->err, 0, sizeof(int)) != cudaSuccess) {
+        pair_tc_free(c);
+        return set_error(GD_ERR_CUDA, "pair weight table upload");
+    }
+
+    // dense rows of every group in the class-box layout (x2 * hy + y2) * hz + z2,
+    // built D by D into a host slab of at most ~128 MB per part and uploaded
+    // slab by slab (D's rows are contiguous and in D order)
+    const uint32_t unit = (uint32_t)c.gain_cb * 4u;
+    const int64_t slab_cap = std::max<int64_t>((int64_t)1 << 20, 1);
+    std::vector<__nv_bfloat16> sh, sl;
+    int64_t slab0 = 0, slab_rows = 0;
+    auto flush = [&]() -> int {
+        if (slab_rows == 0) return GD_OK;
+        const size_t nb = (size_t)slab_rows * PT_KC * sizeof(__nv_bfloat16);
+        GD_CUDA(cudaMemcpy(pt->wh + (size_t)slab0 * PT_KC, sh.data(), nb, cudaMemcpyHostToDevice));
+        GD_CUDA(cudaMemcpy(pt->wl + (size_t)slab0 * PT_KC, sl.data(), nb, cudaMemcpyHostToDevice));
+        slab0 += slab_rows;
+        slab_rows = 0;
+        return GD_OK;
+    };
+    int max_items = 0;
+    for (int Dx = 0; Dx < d.nx; Dx++)
+        for (int Dy = 0; Dy < d.ny; Dy++)
+            for (int Dz = 0; Dz < d.nz; Dz++) {
+                const int Did = (Dx * d.ny + Dy) * d.nz + Dz;
+                const int ex = (Dx >> 1) + 1, ey = (Dy >> 1) + 1, ez = (Dz >> 1) + 1;
+                const int i0 = item_off[Did], m = item_off[Did + 1] - i0, mpad = (m + 15) & ~15;
+                const int64_t K = (int64_t)ex * ey * ez, rows_d = (K + PT_KC - 1) / PT_KC * mpad;
+                max_items = std::max(max_items, m);
+                if (slab_rows > 0 && slab_rows + rows_d > slab_cap && (rc = flush())) {
+                    pair_tc_free(c);
+                    return rc;
+                }
+                const size_t need = (size_t)(slab_rows + rows_d) * PT_KC;
+                if (sh.size() < need) {
+                    sh.resize(need);
+                    sl.resize(need);
+                }
+                const size_t base = (size_t)slab_rows * PT_KC;
+                std::fill(sh.begin() + base, sh.begin() + need, __float2bfloat16_rn(0.f));
+                std::fill(sl.begin() + base, sl.begin() + need, __float2bfloat16_rn(0.f));
+                for (int t = 0; t < m; t++) {
+                    const int gidx = items[i0 + t].x;
+                    for (int e = c.h_grp_row_off[gidx]; e < c.h_grp_row_off[gidx + 1]; e++) {
+                        const WEntry we = c.h_grp_rows[e];
+                        if (we.w == 0.0f) continue;  // row padding
+                        const int nc = (int)(we.off / unit);
+                        const int z2 = nc % d.hz, y2 = (nc / d.hz) % d.hy, x2 = nc / (d.hz * d.hy);
+                        if (x2 >= ex || y2 >= ey || z2 >= ez) continue;  // P is zero outside B(D)
+                        const int k = (x2 * ey + y2) * ez + z2;
+                        const size_t at = base + ((size_t)(k / PT_KC) * mpad + t) * PT_KC + k % PT_KC;
+                        const __nv_bfloat16 hi = __float2bfloat16_rn(we.w);
+                        sh[at] = hi;
+                        sl[at] = __float2bfloat16_rn(we.w - __bfloat162float(hi));
+                    }
+                }
+                slab_rows += rows_d;
+            }
+    if (!(rc = flush()) && slab0 != rows) rc = set_error(GD_ERR_CUDA, "pair weight table: row count mismatch");
+    if (rc) {
+        pair_tc_free(c);
+        return rc;
+    }
+    pt->max_items = max_items;
     return GD_OK;
 }
 
