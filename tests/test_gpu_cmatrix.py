@@ -99,7 +99,7 @@ def test_tensor_core_loss(cuda, gdlib, n, R, ncells, ld):
         assert np.array_equal(got[:, :ncells], nu_pair.cpu().numpy()[:, :ncells])
 
 
-@pytest.mark.parametrize("ncells", [200, 300, 1000])
+@pytest.mark.parametrize("ncells", [129, 200, 300, 1000])
 def test_cta_pair_is_bitwise_equal(cuda, gdlib, ncells):
     """CTA-pair MMAs (M = 256 cells over two CTAs, each loading half of every
     collision-matrix tile) give the same bits as one CTA per 128-cell tile

@@ -95,3 +95,21 @@ def test_autotune_includes_pair_tc(cuda, gdlib):
     assert paths.count("pair") == 3 and paths.count("pair_tc") == 1
     assert all(c["ms"] > 0 for c in r["candidates"])
     assert r["best_ms"] == pytest.approx(min(c["ms"] for c in r["candidates"]))
+
+
+@pytest.mark.parametrize("nc,ld", [(1, 1), (129, 136)])
+def test_pair_tc_edge_cell_counts(cuda, gdlib, nc, ld):
+    """One cell, and one cell past a 128-cell tile (a nearly empty second
+    tile), with a leading dimension past the cells: the FP32 kernel's gain to
+    2e-5 and untouched padding columns."""
+    torch = cuda
+    spec = gdlib.GridSpec(8, R=16.5)
+    ctx = gdlib.Context(spec)
+    ft = torch.zeros((ctx.n_pnt, ld), dtype=torch.float32, device="cuda")
+    ft[:, :nc] = torch.from_numpy(inputs.mixtures(spec.fill(), nc, seed=nc)).cuda()
+    ref = _gain(gdlib, ctx, gdlib.GAIN_PAIR, ft, nc, ld, torch)
+    out = _gain(gdlib, ctx, gdlib.GAIN_PAIR_TC, ft, nc, ld, torch)
+    assert bool((out[:, nc:] == -1.0).all())
+    rel = float((out[:, :nc] - ref[:, :nc]).norm() / ref[:, :nc].norm())
+    assert rel <= 2e-5, rel
+    ctx.check()
