@@ -186,7 +186,8 @@ int gd_cmatrix_destroy(gd_cmatrix *cm);
 /* CTAs per tensor-core MMA of the gain kernel: 2 (the default) or 1.  With
  * 2, the CTAs of a node's two adjacent 128-cell tiles form a cluster and run
  * each MMA as a CTA pair (M = 256 cells): each loads its own cells and half
- * of every collision-matrix tile.  Results are bitwise the same either way. */
+ * of every collision-matrix tile; a call with at most 128 cells runs one CTA
+ * per MMA.  Results are bitwise the same either way. */
 int gd_cmatrix_set_cluster(gd_cmatrix *cm, int ctas);
 /* gd_cmatrix_gain synchronises the stream and reports a pipeline time-out of
  * its kernel, except inside a stream capture; after replaying a captured
