@@ -463,9 +463,17 @@ def gain_roofline(name, ctx, f0, nc, stream, flush, peak, peak_kind, reps):
         traffic = 1.027 * g_bytes
         traffic_src = "ncu dram__bytes_read+write of a 14^3/4096-cell launch, scaled by collision-matrix bytes"
     ach = flop / g_avg / 1e12
-    return {"bound": "tensor", "kernel": kernel, "achieved": ach, "peak": peak, "unit": "TFLOP/s",
-            "frac": ach / peak, "peak_source": f"{peak_kind} bf16 dense (MEASURED_PEAKS.json)", "work": work,
-            "flop_per_launch": flop, "traffic": traffic, "traffic_source": traffic_src, "launch_ms": g_avg * 1000.0}
+    out = {"bound": "tensor", "kernel": kernel, "achieved": ach, "peak": peak, "unit": "TFLOP/s",
+           "frac": ach / peak, "peak_source": f"{peak_kind} bf16 dense (MEASURED_PEAKS.json)", "work": work,
+           "flop_per_launch": flop, "traffic": traffic, "traffic_source": traffic_src, "launch_ms": g_avg * 1000.0}
+    if name not in ("pair", "pair_tc"):
+        # the dense bilinear form's count, 2 n^3 + 2 n^2 FLOP per cell: what the
+        # launch computes without exploiting the symmetry of G_i and its zero tiles
+        n = ctx.n_pnt
+        dense = nc * (2.0 * n ** 3 + 2.0 * n ** 2) * (3 if name == "bf16x3" else 1)
+        out["dense_equivalent"] = {"flop_per_launch": dense, "tflops": dense / g_avg / 1e12,
+                                   "issued_fraction": flop / dense}
+    return out
 
 
 def one_step_q(gd, ctx, f0, nc):
