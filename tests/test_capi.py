@@ -101,3 +101,17 @@ def test_missing_library_fails_loudly(gdlib, monkeypatch):
     monkeypatch.setattr(gd, "_lib", None)
     with pytest.raises(ImportError):
         gd.lib()
+
+
+def test_python_constants_match_header(gdlib):
+    """The binding's enum constants equal the header's (gain paths, matrix
+    modes, network flags)."""
+    src = open(os.path.join(HEADER, "gpu_determ.h")).read()
+    vals = {m.group(1): int(m.group(2)) for m in re.finditer(r"\b(GD_[A-Z0-9_]+)\s*=\s*(\d+)", src)}
+    for name, py in (("GD_GAIN_PAIR", "GAIN_PAIR"), ("GD_GAIN_CMATRIX_BF16", "GAIN_CMATRIX_BF16"),
+                     ("GD_GAIN_CMATRIX_BF16X3", "GAIN_CMATRIX_BF16X3"), ("GD_GAIN_PAIR_TC", "GAIN_PAIR_TC"),
+                     ("GD_CMATRIX_BF16", "CMATRIX_BF16"), ("GD_CMATRIX_BF16X3", "CMATRIX_BF16X3"),
+                     ("GD_MLP_SCALE_INPUT", "MLP_SCALE_INPUT"), ("GD_MLP_SCALE_OUTPUT", "MLP_SCALE_OUTPUT"),
+                     ("GD_MLP_LOSS_MSE", "MLP_LOSS_MSE"), ("GD_MLP_LOSS_BATCH", "MLP_LOSS_BATCH")):
+        assert name in vals, name
+        assert getattr(gdlib, py) == vals[name], (name, vals[name], getattr(gdlib, py))
