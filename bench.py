@@ -58,6 +58,8 @@ def parse():
     p.add_argument("--cpu-seconds", type=float, default=15.0,
                    help="target length of the bounded CPU-baseline sample")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--ref-cells", type=int, default=128,
+                   help="reference arm: whole cells of the workload evaluated per step on the host")
     p.add_argument("--gain", choices=["pair", "pair_tc", "bf16", "bf16x3"], default="bf16",
                    help="gain algorithm of the timed step (FP32 pair-product kernel, pair products with the "
                         "contraction on the tensor cores, or tensor-core collision matrices)")
@@ -135,51 +137,75 @@ class Clocks:
                 "reasons": reasons, "samples": len(rows)}
 
 
-def cpu_baseline(args, seconds):
-    """The oracle's FP32 OpenMP host path (loss + gain + FP64 projection) on a
-    bounded sample of cells of the same workload."""
-    from gpu_determ_gb300 import GridSpec, inputs
+def host_oracle(args):
+    """The oracle for the bench grid and its grid lists (built by the oracle
+    itself, so a host-only run never loads the GPU library)."""
     from oracle.pyoracle import Oracle
     o = Oracle(args.grid, R=args.radius)
-    grid = GridSpec(args.grid, R=args.radius).fill()
-    threads = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    return o, {"u": o.u, "v": o.v, "w": o.w, "ui": o.ui, "vi": o.vi, "wi": o.wi}
 
-    def run(nc):
-        f = inputs.mixtures(grid, nc, seed=args.seed + 1)
-        fb = o.to_box(f)
-        t0 = time.perf_counter()
-        nu = o.loss_f32(fb)
-        gain = o.gain_f32(fb)
-        o.project(f, nu, gain)
-        return time.perf_counter() - t0
 
-    run(1)  # thread pool and page warm-up
-    nc, t = 2, run(2)
+def host_step(o, f):
+    """One collision evaluation of the oracle's FP32 OpenMP host path (loss +
+    gain + FP64 projection) on compact [n_pnt][cells]; returns seconds."""
+    fb = o.to_box(f)
+    t0 = time.perf_counter()
+    nu = o.loss_f32(fb)
+    gain = o.gain_f32(fb)
+    o.project(f, nu, gain)
+    return time.perf_counter() - t0
+
+
+def host_threads():
+    return int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+
+
+def workload_cells(args, grid, ncells):
+    """The first ncells cells of the bench workload (its seed and its full
+    batch of args.cells draws, so the sample is a prefix of the timed cells)."""
+    from gpu_determ_gb300 import inputs
+    f = inputs.dirichlet_mixtures(grid, max(args.cells, ncells), seed=args.seed + 17)
+    return np.ascontiguousarray(f[:, :ncells])
+
+
+def cpu_baseline(args, seconds):
+    """The oracle's FP32 OpenMP host path on a bounded sample of whole cells
+    of the workload, grown until one evaluation takes about `seconds`."""
+    o, grid = host_oracle(args)
+    f_all = workload_cells(args, grid, 2048)
+    host_step(o, f_all[:, :1])  # thread pool and page warm-up
+    nc, t = 2, host_step(o, f_all[:, :2])
     while t < 0.6 * seconds and nc < 2048:  # grow the sample to the target length
         nc = min(2048, max(nc * 2, int(nc * seconds / max(t, 1e-3))))
-        t = run(nc)
-    return {"value": nc / t, "unit": UNIT, "cores": threads, "kind": "port",
+        t = host_step(o, f_all[:, :nc])
+    return {"value": nc / t, "unit": UNIT, "cores": host_threads(), "kind": "port",
             "sample": f"{nc} cell(s) x 1 step, all {o.n_pnt} nodes, {t:.1f} s"}
 
 
 def run_reference(args):
+    """The reference arm: the oracle's host path (the reference has no CPU
+    implementation of its own) timed on all host cores, each step one
+    collision evaluation of the same --ref-cells whole cells of the workload,
+    whatever --steps is; rank 0 only."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    vals = []
-    info = None
-    # each sample warms its thread pool and pages up with a one-cell run first,
-    # so the host path needs no separate warm-up steps
-    for _ in range(max(1, args.steps)):
-        info = cpu_baseline(args, args.cpu_seconds / max(1, args.steps) * 2)
-        vals.append(info["value"])
-    v = statistics.median(vals)
-    info["value"] = v
-    # ms_per_step: one step of the bench's workload (args.cells cells) at this rate
+    o, grid = host_oracle(args)
+    nc = max(1, args.ref_cells)
+    f = workload_cells(args, grid, nc)
+    for _ in range(max(args.warmup, 1)):
+        host_step(o, f[:, :2])  # warm-up of the thread pool and pages, on two cells
+    times = [host_step(o, f) for _ in range(max(1, args.steps))]
+    total = sum(times)
+    v = nc * len(times) / total
+    info = {"value": v, "unit": UNIT, "cores": host_threads(), "kind": "port",
+            "sample": f"{nc} cell(s) of the workload per step x {len(times)} steps, all {o.n_pnt} nodes, "
+                      f"{total:.1f} s"}
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * args.cells / v,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * total / len(times),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic", "config": dict(workload(args, 1), gain="oracle FP32 OpenMP host path"),
+            "data": "synthetic", "config": dict(workload(args, args.cells), gain="oracle FP32 OpenMP host path",
+                                                sample_cells=nc),
             "cpu_baseline": info,
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)

@@ -13,7 +13,7 @@ from __future__ import annotations
 import ctypes as C
 import os
 
-__all__ = ["GDError", "GridSpec", "Context", "CollisionMatrix", "Mlp", "Surrogate", "Batch", "cell_rel_l2", "lib", "library_path", "load_options",
+__all__ = ["GDError", "GridSpec", "Context", "CollisionMatrix", "Mlp", "Surrogate", "Batch", "cell_rel_l2", "fma_peak", "lib", "library_path", "load_options",
            "DT_COURANT", "DT_FIXED", "CMATRIX_BF16", "CMATRIX_BF16X3",
            "MLP_SCALE_INPUT", "MLP_SCALE_OUTPUT", "MLP_LOSS_MSE", "MLP_LOSS_BATCH"]
 
@@ -60,6 +60,11 @@ class _Info(C.Structure):
                 ("nonzero_weights", C.c_int64), ("table_a_elems", C.c_int64),
                 ("pair_products", C.c_int64), ("contraction_terms", C.c_int64),
                 ("scatter_terms", C.c_int64), ("cmatrix_tiles", C.c_int64)]
+
+
+class _PairSizes(C.Structure):
+    _fields_ = [("n_groups", C.c_int), ("nclass", C.c_int), ("n_entries", C.c_int64), ("n_items", C.c_int64),
+                ("n_members", C.c_int64)]
 
 
 class _MlpInfo(C.Structure):
@@ -111,6 +116,7 @@ def lib():
     L.gd_cmatrix_gain.argtypes = [vp, vp, i, i, vp, vp]
     L.gd_cmatrix_destroy.argtypes = [vp]
     L.gd_cmatrix_set_cluster.argtypes = [vp, i]
+    L.gd_cmatrix_set_chain.argtypes = [vp, i]
     L.gd_ctx_set_gain_path.argtypes = [vp, i]
     L.gd_box_to_compact.argtypes = [vp, vp, i, i, vp, i, vp]
     L.gd_compact_to_box.argtypes = [vp, vp, i, i, vp, i, vp]
@@ -137,16 +143,22 @@ def lib():
     L.gd_batch_check.argtypes = [vp]
     L.gd_batch_info.argtypes = [vp, P(i), P(i), P(i), P(C.c_int64)]
     L.gd_ctx_autotune.argtypes = [vp, vp, i, i, i, C.c_double, P(_Autotune), vp]
+    L.gd_fma_peak.argtypes = [i, i, P(C.c_double)]
+    L.gd_mlp_inject_timeout.argtypes = [vp, i]
+    L.gd_pair_tables.argtypes = [vp, P(_PairSizes), vp, vp, vp, vp, vp, vp]
+    L.gd_pair_tc_table.argtypes = [vp, P(C.c_int64), vp, vp, vp]
+    L.gd_ctx_inject_timeout.argtypes = [vp, i]
     for name in ("gd_grid_count", "gd_grid_fill", "gd_ctx_create", "gd_ctx_destroy", "gd_ctx_info",
                  "gd_export_tables", "gd_correction_basis", "gd_collision", "gd_project",
                  "gd_relax", "gd_step", "gd_moments", "gd_ctx_check", "gd_set_memory_limit", "gd_gain_noalloc",
                  "gd_box_to_compact", "gd_compact_to_box", "gd_load_options", "gd_cmatrix_create",
-                 "gd_cmatrix_gain", "gd_cmatrix_destroy", "gd_cmatrix_set_cluster", "gd_ctx_set_gain_path",
+                 "gd_cmatrix_gain", "gd_cmatrix_destroy", "gd_cmatrix_set_cluster", "gd_cmatrix_set_chain", "gd_ctx_set_gain_path",
                  "gd_mlp_create", "gd_mlp_destroy", "gd_mlp_set_io_scale", "gd_mlp_info", "gd_mlp_forward", "gd_mlp_train_step",
                  "gd_mlp_loss", "gd_mlp_check", "gd_mlp_get_params", "gd_mlp_set_params", "gd_mlp_get_grads",
                  "gd_surrogate_create", "gd_surrogate_destroy", "gd_surrogate_gain", "gd_cell_rel_l2",
                  "gd_cmatrix_check", "gd_batch_create", "gd_batch_destroy", "gd_batch_add", "gd_batch_step",
-                 "gd_batch_check", "gd_batch_info", "gd_ctx_autotune"):
+                 "gd_batch_check", "gd_batch_info", "gd_ctx_autotune", "gd_fma_peak",
+                 "gd_mlp_inject_timeout", "gd_ctx_inject_timeout", "gd_pair_tables", "gd_pair_tc_table"):
         getattr(L, name).restype = i
     _lib = L
     return L
@@ -302,6 +314,41 @@ class Context:
     def moments(self, f, ncells, ld, m5, stream=None):
         _check(lib().gd_moments(self._h, _ptr(f), int(ncells), int(ld), _ptr(m5), _stream(stream)))
 
+    def pair_tables(self) -> dict:
+        """The pair-product tables the gain kernels read (gd_pair_tables), as
+        numpy arrays."""
+        import numpy as np
+        sz = _PairSizes()
+        _check(lib().gd_pair_tables(self._h, C.byref(sz), None, None, None, None, None, None))
+        nxyz = self.spec.nx * self.spec.ny * self.spec.nz
+        out = {"grp_row_off": np.zeros(sz.n_groups + 1, np.int32),
+               "entry_class": np.zeros(sz.n_entries, np.int32), "entry_w": np.zeros(sz.n_entries, np.float32),
+               "item_off": np.zeros(nxyz + 1, np.int32), "items": np.zeros((sz.n_items, 3), np.int32),
+               "members": np.zeros(sz.n_members, np.uint32)}
+        _check(lib().gd_pair_tables(self._h, C.byref(sz), *(out[k].ctypes.data for k in
+                                                            ("grp_row_off", "entry_class", "entry_w", "item_off",
+                                                             "items", "members"))))
+        out["nclass"] = sz.nclass
+        return out
+
+    def pair_tc_table(self) -> dict:
+        """The per-D weight table of the pair path on tensor cores (raw BF16
+        bits of the hi and lo parts, [rows][64]) and each D's first row."""
+        import numpy as np
+        rows = C.c_int64(0)
+        _check(lib().gd_pair_tc_table(self._h, C.byref(rows), None, None, None))
+        nxyz = self.spec.nx * self.spec.ny * self.spec.nz
+        out = {"wrow": np.zeros(nxyz, np.int32), "wh": np.zeros((rows.value, 64), np.uint16),
+               "wl": np.zeros((rows.value, 64), np.uint16)}
+        _check(lib().gd_pair_tc_table(self._h, C.byref(rows), out["wrow"].ctypes.data, out["wh"].ctypes.data,
+                                      out["wl"].ctypes.data))
+        return out
+
+    def inject_timeout(self, polls: int):
+        """Failure-detection test hook: the next tensor-core loss GEMM's bounded
+        wait runs out after `polls` polls; check() then reports it."""
+        _check(lib().gd_ctx_inject_timeout(self._h, int(polls)))
+
 
 class CollisionMatrix:
     """Dense collision matrices G_i of a context on the device and the
@@ -319,6 +366,10 @@ class CollisionMatrix:
     def set_cluster(self, ctas: int):
         """CTAs per tensor-core MMA: 2 (default; CTA pair, M = 256 cells) or 1."""
         _check(lib().gd_cmatrix_set_cluster(self._h, int(ctas)))
+
+    def set_chain(self, tiles: int):
+        """Most stored tiles per tensor-memory accumulation (even; 0 = unlimited)."""
+        _check(lib().gd_cmatrix_set_chain(self._h, int(tiles)))
 
     def close(self):
         if self._h:
@@ -370,6 +421,11 @@ class Mlp:
 
     def check(self, stream=None):
         _check(lib().gd_mlp_check(self._h, _stream(stream)))
+
+    def inject_timeout(self, polls: int):
+        """Failure-detection test hook: the next forward pass's first GEMM has
+        its bounded wait run out after `polls` polls; check() then reports it."""
+        _check(lib().gd_mlp_inject_timeout(self._h, int(polls)))
 
     def get_params(self):
         import numpy as np
@@ -428,6 +484,14 @@ class Surrogate:
             self.close()
         except Exception:
             pass
+
+
+def fma_peak(device: int = 0, precision: int = 32) -> float:
+    """Measured FP32 (precision 32) or FP64 (64) FMA throughput of the device
+    in FLOP/s: the roofline denominator of the SIMT kernels."""
+    v = C.c_double(0.0)
+    _check(lib().gd_fma_peak(int(device), int(precision), C.byref(v)))
+    return v.value
 
 
 def cell_rel_l2(a, lda, b, ldb, n, ncells, out, stream=None):

@@ -180,12 +180,14 @@ extern "C" int gd_batch_check(gd_batch *b)
     if (!b) return set_error(GD_ERR_INVALID_ARG, "NULL argument");
     gd::DeviceGuard ds(b->device);
     GD_CUDA(cudaStreamSynchronize(b->main));
-    for (gd_ctx *c : b->slot_ctx)
-        if (c->c.cmatrix) {
-            int rc = gd_cmatrix_check(c->c.cmatrix, nullptr);
-            if (rc) return rc;
-        }
-    return GD_OK;
+    // every context's records (projection status, tensor-core time-outs),
+    // each read and cleared by gd_ctx_check
+    int first = GD_OK;
+    for (gd_ctx *c : b->slot_ctx) {
+        const int rc = gd_ctx_check(c, nullptr);
+        if (rc && first == GD_OK) first = rc;
+    }
+    return first;
 }
 
 extern "C" int gd_batch_info(const gd_batch *b, int *groups, int *streams, int *graph_nodes, int64_t *steps)

@@ -474,6 +474,42 @@ int gd_ctx_info(const gd_ctx *ctx, gd_info *out)
     return GD_OK;
 }
 
+int gd_pair_tables(gd_ctx *ctx, gd_pair_table_sizes *sizes, int *grp_row_off, int *entry_class, float *entry_w,
+                   int *item_off, int *items, uint32_t *members)
+{
+    if (!ctx || !sizes) return set_error(GD_ERR_INVALID_ARG, "NULL argument");
+    gd::Context &c = ctx->c;
+    gd::DeviceGuard g(c.device);
+    const gd::Dims &d = c.d;
+    std::vector<int> ioff(d.nxyz + 1);
+    GD_CUDA(cudaMemcpy(ioff.data(), c.d_D_item_off, sizeof(int) * (d.nxyz + 1), cudaMemcpyDeviceToHost));
+    const int64_t n_items = ioff[d.nxyz];
+    std::vector<int4> it(n_items + 1);
+    GD_CUDA(cudaMemcpy(it.data(), c.d_D_items, sizeof(int4) * n_items, cudaMemcpyDeviceToHost));
+    const int64_t n_members = n_items > 0 ? it[n_items - 1].z : 0;
+    sizes->n_groups = c.n_groups;
+    sizes->nclass = d.nclass;
+    sizes->n_entries = c.n_grp_entries;
+    sizes->n_items = n_items;
+    sizes->n_members = n_members;
+    if (grp_row_off) std::memcpy(grp_row_off, c.h_grp_row_off.data(), sizeof(int) * (c.n_groups + 1));
+    const uint32_t unit = (uint32_t)c.gain_cb * 4u;  // WEntry.off = class index x cells per block x 4
+    for (int64_t e = 0; e < c.n_grp_entries; e++) {
+        if (entry_class) entry_class[e] = (int)(c.h_grp_rows[e].off / unit);
+        if (entry_w) entry_w[e] = c.h_grp_rows[e].w;
+    }
+    if (item_off) std::memcpy(item_off, ioff.data(), sizeof(int) * (d.nxyz + 1));
+    if (items)
+        for (int64_t t = 0; t < n_items; t++) {
+            items[3 * t] = it[t].x;
+            items[3 * t + 1] = it[t].y;
+            items[3 * t + 2] = it[t].z;
+        }
+    if (members && n_members > 0)
+        GD_CUDA(cudaMemcpy(members, c.d_D_members, sizeof(uint32_t) * n_members, cudaMemcpyDeviceToHost));
+    return GD_OK;
+}
+
 int gd_export_tables(gd_ctx *ctx, float *b, float *a, gd_stream stream)
 {
     if (!ctx) return set_error(GD_ERR_INVALID_ARG, "context is NULL");
@@ -572,24 +608,35 @@ int gd_ctx_check(gd_ctx *ctx, gd_stream stream)
     gd::DeviceGuard g(ctx->c.device);
     gd::Context &c = ctx->c;
     cudaStream_t st = (cudaStream_t)stream;
+    // read every record first (each read clears its own), then report: a
+    // numeric record and a time-out of the same step come out in one message
     unsigned int h[2] = {0u, 0u};
     GD_CUDA(cudaMemcpyAsync(h, c.d_status, sizeof(h), cudaMemcpyDeviceToHost, st));
     GD_CUDA(cudaStreamSynchronize(st));
+    if (h[0]) {
+        static const unsigned int clear[2] = {0u, 0xffffffffu};
+        GD_CUDA(cudaMemcpyAsync(c.d_status, clear, sizeof(clear), cudaMemcpyHostToDevice, st));
+        GD_CUDA(cudaStreamSynchronize(st));
+    }
+    bool cm_timeout = false, pt_timeout = false;
     if (c.cmatrix) {
-        const int rc = gd_cmatrix_check(c.cmatrix, stream);
+        const int rc = gd::cmatrix_take_timeout(c.cmatrix, st, &cm_timeout);
         if (rc) return rc;
     }
     if (c.pair_tc) {
-        const int rc = gd::pair_tc_check(c, st);
+        const int rc = gd::pair_tc_take_timeout(c, st, &pt_timeout);
         if (rc) return rc;
     }
-    if (!h[0]) return GD_OK;
-    const unsigned int clear[2] = {0u, 0xffffffffu};
-    GD_CUDA(cudaMemcpy(c.d_status, clear, sizeof(clear), cudaMemcpyHostToDevice));
-    return set_error(GD_ERR_SINGULAR,
-                     std::string(h[0] & 1u ? "non-finite distribution, frequency or gain"
-                                           : "singular conservation system") +
-                         " in the projection (first affected cell " + std::to_string(h[1]) + ")");
+    std::string msg;
+    if (cm_timeout) msg += "collision-matrix kernel: a pipeline wait timed out";
+    if (pt_timeout) msg += std::string(msg.empty() ? "" : "; ") + "pair tensor-core gain kernel: a pipeline wait timed out";
+    if (h[0])
+        msg += std::string(msg.empty() ? "" : "; ") +
+               (h[0] & 1u ? "non-finite distribution, frequency or gain" : "singular conservation system") +
+               " in the projection (first affected cell " + std::to_string(h[1]) + ")";
+    if (cm_timeout || pt_timeout) return set_error(GD_ERR_CUDA, msg);
+    if (h[0]) return set_error(GD_ERR_SINGULAR, msg);
+    return GD_OK;
 }
 
 int gd_moments(gd_ctx *ctx, const float *f, int ncells, int ld, double *m5, gd_stream stream)

@@ -73,6 +73,14 @@ __device__ __forceinline__ int stage_len(const uint32_t *tiles, int j, int cnt, 
     return (__ldg(tiles + j) >> 16) == (__ldg(tiles + j + 1) >> 16) ? 2 : 1;
 }
 
+// The tensor cores' FP32 accumulation loses precision over long sums (the
+// collision-matrix gain against FP64 at 20^3: median relative error 2.5e-6
+// with whole b-tile runs of ~25 tiles per accumulation, 6.4e-7 with at most
+// four): by default at most four 64-column tiles (256 products per entry) go
+// into one accumulation, the epilogue adding the runs in FP32 with
+// compensation.  Cost: 2 % of the gain launch.
+constexpr int kDefaultChain = 4;
+
 struct CmParams {
     int ns;       // in-sphere nodes
     int ns_k;     // padded node count (multiple of BK)
@@ -83,6 +91,7 @@ struct CmParams {
     const int *node_off;     // [ns + 1] each node's range of stored tiles
     const uint32_t *tiles;   // stored tiles, n << 16 | k, n-major then k within each node
     int m_tiles;             // cell tiles, padded to whole clusters (the grid's x extent)
+    int chain;               // most stored tiles summed in one tensor-memory accumulation (even)
 };
 
 // G_i is symmetric in (a, b), so only its block upper triangle is stored and
@@ -238,7 +247,8 @@ __global__ void __launch_bounds__(kThreads, 1)
                 asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
                 const uint32_t d_tmem = tmem + (uint32_t)(buf * BN);
                 bool first = true;
-                while (j < cnt && (__ldg(p.tiles + l0 + j) >> 16) == n) {
+                const int jg = j;  // an accumulation: tiles of one b-tile, at most p.chain of them
+                while (j < cnt && (__ldg(p.tiles + l0 + j) >> 16) == n && j - jg < p.chain) {
                     const int s = it % S;
                     const uint32_t ph = (uint32_t)(it / S) & 1u;
                     if (!mbar_wait(smem_u32(&full_bar[s]), ph, p.err)) {
@@ -298,7 +308,12 @@ __global__ void __launch_bounds__(kThreads, 1)
         bool failed = false;
         const int cell = m_tile * BM + row;
         const bool live = cell < p.ncells;
-        float sum = 0.f;
+        // the gain of this cell (this half's columns): each accumulation's
+        // 128 products D[c][b] f_b are summed in four interleaved partials,
+        // and the accumulations' sums are added with compensated (Kahan)
+        // summation, so the rounding of one long FP32 chain of thousands of
+        // terms does not limit the result
+        float sum = 0.f, comp = 0.f;
         // f[b][cell] for this warp's 128 b of a group; rows b >= ns of G are
         // zero, so T[b] = 0 there and clamping b keeps every load in bounds
         // without a branch.  A group's values are requested as soon as the
@@ -313,8 +328,10 @@ __global__ void __launch_bounds__(kThreads, 1)
         int n = cnt > 0 ? (int)(__ldg(p.tiles + l0) >> 16) : 0;
         if (live && cnt > 0) load_f(n * BN + half * (BN / 2));
         for (; j < cnt; grp++) {
-            // b-tiles without stored tiles contribute nothing and are skipped
-            while (j < cnt && (int)(__ldg(p.tiles + l0 + j) >> 16) == n) j++;
+            // b-tiles without stored tiles contribute nothing and are skipped;
+            // a b-tile's run of tiles comes in accumulations of at most p.chain
+            const int jg = j;
+            while (j < cnt && (int)(__ldg(p.tiles + l0 + j) >> 16) == n && j - jg < p.chain) j++;
             const int n_next = j < cnt ? (int)(__ldg(p.tiles + l0 + j) >> 16) : -1;
             const int buf = grp & 1;
             const uint32_t use = (uint32_t)(grp >> 1);
@@ -328,14 +345,22 @@ __global__ void __launch_bounds__(kThreads, 1)
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
             const uint32_t taddr =
                 tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(buf * BN) + (uint32_t)(half * (BN / 2));
+            float ps[4] = {0.f, 0.f, 0.f, 0.f};
 #pragma unroll
             for (int c0 = 0; c0 < BN / 2; c0 += 16) {
                 float v[16];
                 tmem_ld16(taddr + (uint32_t)c0, v);
                 if (live) {
 #pragma unroll
-                    for (int q = 0; q < 16; q++) sum = __fmaf_rn(v[q], fv[c0 + q], sum);
+                    for (int q = 0; q < 16; q++) ps[q & 3] = __fmaf_rn(v[q], fv[c0 + q], ps[q & 3]);
                 }
+            }
+            {
+                const float part = __fadd_rn(__fadd_rn(ps[0], ps[1]), __fadd_rn(ps[2], ps[3]));
+                const float y = __fsub_rn(part, comp);
+                const float t = __fadd_rn(sum, y);
+                comp = __fsub_rn(__fsub_rn(t, sum), y);
+                sum = t;
             }
             asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
             __syncwarp();
@@ -346,7 +371,8 @@ __global__ void __launch_bounds__(kThreads, 1)
                 else
                     mbar_arrive(smem_u32(&acce_bar[buf]));
             }
-            if (live && n_next >= 0) load_f(n_next * BN + half * (BN / 2));
+            // the next accumulation of the same b-tile reuses fv
+            if (live && n_next >= 0 && n_next != n) load_f(n_next * BN + half * (BN / 2));
             n = n_next;
         }
         // the two column halves of a cell are added in a fixed order
@@ -524,6 +550,10 @@ struct gd_cmatrix {
     int f_cells = 0;
     __nv_bfloat16 *bh = nullptr, *bl = nullptr;  // loss matrix [node][ns_k] BF16 hi / lo
     int *err = nullptr;
+    int stall_next = 0;  // gd_ctx_inject_timeout: polls for the next tensor-core loss GEMM
+    // stored tiles per tensor-memory accumulation of the gain, and 64-column K
+    // chunks per launch of the tensor-core loss (gd_cmatrix_set_chain)
+    int chain = gd::kDefaultChain;
 };
 
 namespace gd {
@@ -665,6 +695,14 @@ extern "C" int gd_cmatrix_set_cluster(gd_cmatrix *h, int ctas)
     return GD_OK;
 }
 
+extern "C" int gd_cmatrix_set_chain(gd_cmatrix *h, int tiles)
+{
+    if (!h) return gd::set_error(GD_ERR_INVALID_ARG, "NULL argument");
+    if (tiles < 0 || (tiles & 1)) return gd::set_error(GD_ERR_INVALID_ARG, "chain must be 0 or a positive even count");
+    h->chain = tiles == 0 ? (1 << 30) : tiles;
+    return GD_OK;
+}
+
 extern "C" int gd_cmatrix_destroy(gd_cmatrix *h)
 {
     if (!h) return GD_OK;
@@ -717,7 +755,7 @@ extern "C" int gd_cmatrix_gain(gd_cmatrix *h, const float *f, int ncells, int ld
     }
     // cell tiles padded to whole clusters: a tile past ncells reads zeros and stores nothing
     const int m_tiles = ((ncells + BM - 1) / BM + cl - 1) / cl * cl;
-    CmParams prm{h->ns, h->ns_k, ncells, ld, f, gain, h->err, h->node_off, h->list, m_tiles};
+    CmParams prm{h->ns, h->ns_k, ncells, ld, f, gain, h->err, h->node_off, h->list, m_tiles, h->chain};
     // one CTA per (cell tile, node), cell tiles fastest so that the CTAs in flight
     // share a few nodes' matrix tiles in L2 (a persistent grid of one CTA per SM
     // taking the tiles round-robin measured 3-4 % slower at 20^3 / 4096 cells)
@@ -742,23 +780,47 @@ extern "C" int gd_cmatrix_gain(gd_cmatrix *h, const float *f, int ncells, int ld
     cfg.numAttrs = 1;
     GD_CUDA(cudaLaunchKernelEx(&cfg, kern, tFh, tFl, tGh, tGl, prm));
     GD_CUDA(cudaGetLastError());
-    // the kernel records a time-out instead of hanging; report it (inside a
-    // stream capture the flag stays set for gd_cmatrix_check after replay)
-    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
-    GD_CUDA(cudaStreamIsCapturing(st, &cap));
-    if (cap != cudaStreamCaptureStatusNone) return GD_OK;
-    return gd_cmatrix_check(h, stream);
+    // the kernel records a pipeline time-out in h->err instead of hanging; the
+    // call only enqueues work, and gd_cmatrix_check / gd_ctx_check report it
+    return GD_OK;
 }
+
+extern "C" int gd_ctx_inject_timeout(gd_ctx *ctx, int polls)
+{
+    using namespace gd;
+    if (!ctx || polls < 1 || polls > (1 << 20))
+        return set_error(GD_ERR_INVALID_ARG, "gd_ctx_inject_timeout: need a context and 1 <= polls <= 2^20");
+    if (!ctx->c.cmatrix || ctx->c.gain_path == GD_GAIN_PAIR || ctx->c.gain_path == GD_GAIN_PAIR_TC)
+        return set_error(GD_ERR_UNSUPPORTED, "gd_ctx_inject_timeout: the context's gain path has no tensor-core loss");
+    ctx->c.cmatrix->stall_next = polls;
+    return GD_OK;
+}
+
+namespace gd {
+// Reads the collision-matrix time-out record on st (synchronising) and clears
+// it; *timed_out receives whether it was set.
+int cmatrix_take_timeout(gd_cmatrix *h, cudaStream_t st, bool *timed_out)
+{
+    int flag = 0;
+    GD_CUDA(cudaMemcpyAsync(&flag, h->err, sizeof(int), cudaMemcpyDeviceToHost, st));
+    GD_CUDA(cudaStreamSynchronize(st));
+    *timed_out = flag != 0;
+    if (flag) {
+        GD_CUDA(cudaMemsetAsync(h->err, 0, sizeof(int), st));
+        GD_CUDA(cudaStreamSynchronize(st));
+    }
+    return GD_OK;
+}
+}  // namespace gd
 
 extern "C" int gd_cmatrix_check(gd_cmatrix *h, gd_stream stream)
 {
     using namespace gd;
     if (!h) return set_error(GD_ERR_INVALID_ARG, "NULL argument");
-    cudaStream_t st = (cudaStream_t)stream;
-    int flag = 0;
-    GD_CUDA(cudaMemcpyAsync(&flag, h->err, sizeof(int), cudaMemcpyDeviceToHost, st));
-    GD_CUDA(cudaStreamSynchronize(st));
-    if (flag) return set_error(GD_ERR_CUDA, "collision-matrix kernel: a pipeline wait timed out");
+    bool timed_out = false;
+    const int rc = cmatrix_take_timeout(h, (cudaStream_t)stream, &timed_out);
+    if (rc) return rc;
+    if (timed_out) return set_error(GD_ERR_CUDA, "collision-matrix kernel: a pipeline wait timed out");
     return GD_OK;
 }
 
@@ -787,9 +849,14 @@ int cmatrix_loss(gd_cmatrix *h, const float *f, int ncells, int ld, float *nu, c
     dim3 cb(32, 8), cg((h->ns_k + 31) / 32, (ncells + 31) / 32);
     convert_f_kernel<<<cg, cb, 0, st>>>(f, h->ns, h->ns_k, ncells, ld, h->fh, h->fl);
     GD_CUDA(cudaGetLastError());
-    if ((rc = gemm_bf16_nt_f32(h->bh, h->ns, h->fh, ncells, h->ns_k, nu, ld, false, h->err, st))) return rc;
-    if ((rc = gemm_bf16_nt_f32(h->bh, h->ns, h->fl, ncells, h->ns_k, nu, ld, true, h->err, st))) return rc;
-    return gemm_bf16_nt_f32(h->bl, h->ns, h->fh, ncells, h->ns_k, nu, ld, true, h->err, st);
+    const int stall = h->stall_next;  // a pending time-out injection fires here, once
+    h->stall_next = 0;
+    // the same bound on the products per tensor-core FP32 accumulation as the
+    // gain: chain x 64 columns of K per launch, chunks added in FP32
+    const int kc = h->chain < (1 << 30) ? h->chain * BK : 0;
+    if ((rc = gemm_bf16_nt_f32(h->bh, h->ns, h->fh, ncells, h->ns_k, nu, ld, false, h->err, st, stall, kc))) return rc;
+    if ((rc = gemm_bf16_nt_f32(h->bh, h->ns, h->fl, ncells, h->ns_k, nu, ld, true, h->err, st, 0, kc))) return rc;
+    return gemm_bf16_nt_f32(h->bl, h->ns, h->fh, ncells, h->ns_k, nu, ld, true, h->err, st, 0, kc);
 }
 
 int64_t cmatrix_stored_tiles(const gd_cmatrix *cm) { return cm ? cm->slots : 0; }

@@ -311,55 +311,19 @@ int gain_bounds_device(Context &c, int nchunks, const int **out)
 int run_gain(Context &c, const float *f, int ncells, int ld, float *gain, cudaStream_t st)
 {
     const Dims &d = c.d;
-    const int cb = c.gain_cb;
-    const size_t smem = c.gain_smem;
-    const int nblk = (ncells + cb - 1) / cb;
+    int cb = 0, nblk = 0, nchunks = 0;
+    size_t smem = 0;
+    int rc = gain_launch_shape(c, ncells, &cb, &smem, &nblk, &nchunks);
+    if (rc) return rc;
     const int cells_pad = nblk * cb;
-    // chunks of s: at least two CTAs per SM, whole waves preferred (one CTA
-    // per SM fits), bounded by the partial buffer
-    int nchunks = gain_chunk_count(c, nblk);
+    // the partial buffer [chunk][node][cells] is bounded at 16 GiB
     while (nchunks > 1 && (size_t)nchunks * d.n_pnt * cells_pad * sizeof(float) > ((size_t)16 << 30)) nchunks--;
     // work-balanced chunk boundaries over the linear s order, cached per count
     const int *d_bounds = nullptr;
-    int rc = gain_bounds_device(c, nchunks, &d_bounds);
-    if (rc) return rc;
-    const size_t part_bytes = (size_t)nchunks * d.n_pnt * cells_pad * sizeof(float);
-    rc = ensure_scratch(c, part_bytes);
-    if (rc) return rc;
-    float *part = static_cast<float *>(c.scratch.ptr);
-    GD_CUDA(cudaMemsetAsync(part, 0, part_bytes, st));
-
-    GainArgs a{d, f, ld, ncells, cells_pad, c.d_cmap, c.d_grp_row_off, c.d_grp_rows, c.d_D_item_off,
-               c.d_D_items, c.d_D_members, d_bounds, part, c.gain_cmap_smem ? 1 : 0};
-    dim3 grid(nblk, nchunks);
-    switch (cb) {
-#define GD_GAIN_CASE(CBV)                                                                       \
-    case CBV:                                                                                   \
-        if (a.cmap_smem) {                                                                      \
-            GD_CUDA(cudaFuncSetAttribute(gain_pair_kernel<CBV, true>,                           \
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)); \
-            gain_pair_kernel<CBV, true><<<grid, kThreads, smem, st>>>(a);                       \
-        } else {                                                                                \
-            GD_CUDA(cudaFuncSetAttribute(gain_pair_kernel<CBV, false>,                          \
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)); \
-            gain_pair_kernel<CBV, false><<<grid, kThreads, smem, st>>>(a);                      \
-        }                                                                                       \
-        break;
-        GD_GAIN_CASE(32)
-        GD_GAIN_CASE(16)
-        GD_GAIN_CASE(8)
-        GD_GAIN_CASE(4)
-#undef GD_GAIN_CASE
-    default:
-        return set_error(GD_ERR_UNSUPPORTED, "gain kernel cell block");
-    }
-    GD_CUDA(cudaGetLastError());
-    const int64_t outs = (int64_t)d.n_pnt * ncells;
-    int rblocks = (int)std::min<int64_t>((outs + 255) / 256, (int64_t)c.sm_count * 16);
-    gain_reduce_kernel<<<std::max(rblocks, 1), 256, 0, st>>>(part, nchunks, d.n_pnt, cells_pad,
-                                                              ncells, ld, gain);
-    GD_CUDA(cudaGetLastError());
-    return GD_OK;
+    if ((rc = gain_bounds_device(c, nchunks, &d_bounds))) return rc;
+    if ((rc = ensure_scratch(c, (size_t)nchunks * d.n_pnt * cells_pad * sizeof(float)))) return rc;
+    return launch_gain_pair(c, f, ncells, ld, gain, static_cast<float *>(c.scratch.ptr), nchunks, d_bounds, cb,
+                            smem, st);
 }
 
 int reduce_gain_partials(Context &c, const float *part, int nchunks, int cells_pad, int ncells, int ld,
@@ -374,10 +338,14 @@ int reduce_gain_partials(Context &c, const float *part, int nchunks, int cells_p
 }
 
 // ---------------------------------------------------------------------------
-// Launch pieces for callers that bring their own partial-sum buffer (the
-// allocation-free entry point in gd_noalloc.cu).  run_gain above does not
-// use them.
+// Launch pieces shared by run_gain above (partials in the context's scratch)
+// and the allocation-free entry point in gd_noalloc.cu (partials in its
+// fixed array): the launch shape, the chunk boundaries, and the one launch
+// routine (clear the partials, gain kernel, chunk reduction).
 
+// cells per lane row, shared memory, cell blocks and the s-chunk count
+// (at least two CTAs per SM, whole waves preferred), before any bound on the
+// partial buffer
 int gain_launch_shape(Context &c, int ncells, int *cb_out, size_t *smem_out, int *nblk_out,
                       int *chunks_out)
 {
@@ -436,12 +404,7 @@ int launch_gain_pair(Context &c, const float *f, int ncells, int ld, float *gain
         return set_error(GD_ERR_UNSUPPORTED, "gain kernel cell block");
     }
     GD_CUDA(cudaGetLastError());
-    const int64_t outs = (int64_t)d.n_pnt * ncells;
-    int rblocks = (int)std::min<int64_t>((outs + 255) / 256, (int64_t)c.sm_count * 16);
-    gain_reduce_kernel<<<std::max(rblocks, 1), 256, 0, st>>>(part, nchunks, d.n_pnt, cells_pad,
-                                                              ncells, ld, gain);
-    GD_CUDA(cudaGetLastError());
-    return GD_OK;
+    return reduce_gain_partials(c, part, nchunks, cells_pad, ncells, ld, gain, st);
 }
 
 }  // namespace gd

@@ -191,8 +191,11 @@ int pair_tc_build(Context &c);
 void pair_tc_free(Context &c);
 double pair_tc_bytes(const Context &c);
 int run_pair_tc(Context &c, const float *f, int ncells, int ld, float *gain, cudaStream_t st);
-// reports (and clears) a pipeline time-out of the pair tensor-core kernel
-int pair_tc_check(Context &c, cudaStream_t st);
+// reads (synchronising st) and clears the pipeline time-out record of the
+// pair tensor-core kernel; *timed_out receives whether it was set
+int pair_tc_take_timeout(Context &c, cudaStream_t st, bool *timed_out);
+// the same for a context's collision matrices (gd_cmatrix.cu)
+int cmatrix_take_timeout(gd_cmatrix *cm, cudaStream_t st, bool *timed_out);
 
 // BF16 tiled tensor map with 128-byte swizzle for the TMA loads of the
 // tensor-core kernels (gd_cmatrix.cu)
@@ -205,8 +208,13 @@ int ensure_scratch(Context &c, size_t bytes);
 // tensor-core GEMM (gd_mlp.cu): C[M][N] = (accumulate ? C : 0) + A B^T, A [M][K]
 // and B [N][K] K-major BF16 (K a multiple of 64), C FP32 with ldc % 4 == 0 and
 // 16-byte aligned rows.
+// stall_polls > 0 is the failure-detection test hook of gd_ctx_inject_timeout
+// (every CTA's bounded wait on a barrier nothing arrives at runs out).
+// k_chunk > 0 (a multiple of 64) splits K into launches of at most k_chunk,
+// whose FP32 results are added in order: the tensor cores then accumulate at
+// most k_chunk products per FP32 sum.
 int gemm_bf16_nt_f32(const void *A, int M, const void *B, int N, int K, float *C, int ldc, bool accumulate, int *err,
-                     cudaStream_t st);
+                     cudaStream_t st, int stall_polls = 0, int k_chunk = 0);
 // loss on the tensor cores when the context uses collision matrices
 // (gd_cmatrix.cu); GD_ERR_UNSUPPORTED when the layout does not allow it.
 int cmatrix_loss(gd_cmatrix *cm, const float *f, int ncells, int ld, float *nu, cudaStream_t st);

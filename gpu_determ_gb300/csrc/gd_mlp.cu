@@ -48,6 +48,13 @@ struct GemmArgs {
     bf16 *c16;          // [M][ld16] or null
     int ld32, ld16;
     int *err;
+    // K range of this launch: columns [k0, k0 + K) of A and B, whose rows
+    // hold ldk elements (ldk = 0: K, the whole rows)
+    int k0, ldk;
+    // failure-detection test hook: > 0 makes every CTA wait this many polls on
+    // a barrier that nothing arrives at (before any copy or MMA is issued),
+    // record the time-out, free its tensor memory and return
+    int stall_polls;
 };
 
 __device__ __forceinline__ float gelu(float x) { return 0.5f * x * (1.f + erff(x * 0.70710678118654752f)); }
@@ -79,7 +86,7 @@ __global__ void __launch_bounds__(kGThreads, 1)
     extern __shared__ __align__(1024) unsigned char dsmem[];
     unsigned char *base = reinterpret_cast<unsigned char *>(
         (reinterpret_cast<uintptr_t>(dsmem) + 1023) & ~static_cast<uintptr_t>(1023));
-    __shared__ __align__(8) uint64_t full_bar[GS], empty_bar[GS], acc_bar;
+    __shared__ __align__(8) uint64_t full_bar[GS], empty_bar[GS], acc_bar, stall_bar;
     __shared__ uint32_t tmem_holder;
     __shared__ int abort_flag;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -95,6 +102,7 @@ __global__ void __launch_bounds__(kGThreads, 1)
             mbar_init(smem_u32(&empty_bar[s]), 1);
         }
         mbar_init(smem_u32(&acc_bar), 1);
+        mbar_init(smem_u32(&stall_bar), 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     if (warp == 1) {
@@ -108,7 +116,19 @@ __global__ void __launch_bounds__(kGThreads, 1)
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = tmem_holder;
 
-    if (warp == 0) {
+    if (p.stall_polls > 0) {
+        // test hook: a bounded wait that must run out (stall_bar never
+        // completes a phase); nothing has been issued yet, so the CTA can go
+        // straight to the common exit below, which frees the tensor memory
+        if (threadIdx.x == 32) mbar_wait_limit(smem_u32(&stall_bar), 0u, p.err, (uint32_t)p.stall_polls);
+        __syncthreads();
+        if (threadIdx.x == 0) abort_flag = *(volatile int *)p.err;
+        __syncthreads();
+    }
+
+    if (abort_flag) {
+        // every thread skips the work alike and meets the barrier below
+    } else if (warp == 0) {
         if (lane == 0) {
             for (int k = 0; k < num_k; k++) {
                 const int s = k % GS;
@@ -117,8 +137,8 @@ __global__ void __launch_bounds__(kGThreads, 1)
                 unsigned char *st = base + (size_t)s * kStageBytes;
                 const uint32_t fb = smem_u32(&full_bar[s]);
                 mbar_expect_tx(fb, kStageBytes);
-                tma_load_2d(smem_u32(st), &tA, k * GK, m0, fb);
-                tma_load_2d(smem_u32(st + kA), &tB, k * GK, n0, fb);
+                tma_load_2d(smem_u32(st), &tA, p.k0 + k * GK, m0, fb);
+                tma_load_2d(smem_u32(st + kA), &tB, p.k0 + k * GK, n0, fb);
             }
         }
     } else if (warp == 1) {
@@ -445,11 +465,15 @@ int make_map(CUtensorMap *m, const bf16 *ptr, int rows, int K, int box_rows)
 // output strides ld32, ld16 multiples of 4.
 int gemm_nt(int epi, const bf16 *A, const bf16 *B, const GemmArgs &a, cudaStream_t st)
 {
-    if (a.K % GK || a.K <= 0 || a.M <= 0 || a.N <= 0 || (a.ld32 & 3) || (a.ld16 & 3))
-        return set_error(GD_ERR_INVALID_ARG, "GEMM shape: K a positive multiple of 64, strides multiples of 4");
+    const int ldk = a.ldk ? a.ldk : a.K;
+    if (a.K % GK || a.K <= 0 || a.M <= 0 || a.N <= 0 || (a.ld32 & 3) || (a.ld16 & 3) || a.k0 % GK || a.k0 < 0 ||
+        ldk % GK || a.k0 + a.K > ldk)
+        return set_error(GD_ERR_INVALID_ARG,
+                         "GEMM shape: K, k0 and the row length multiples of 64, k0 + K within the rows, strides "
+                         "multiples of 4");
     CUtensorMap tA, tB;
-    int rc = make_map(&tA, A, a.M, a.K, GM);
-    if (!rc) rc = make_map(&tB, B, a.N, a.K, GN);
+    int rc = make_map(&tA, A, a.M, ldk, GM);
+    if (!rc) rc = make_map(&tB, B, a.N, ldk, GN);
     if (rc) return rc;
     dim3 grid((a.M + GM - 1) / GM, (a.N + GN - 1) / GN);
     switch (epi) {
@@ -484,17 +508,28 @@ int pad64(int n) { return (n + 63) / 64 * 64; }
 // C[M][N] (FP32, row stride ldc) = (accumulate ? C : 0) + A B^T for K-major BF16
 // A [M][K] and B [N][K]; the collision-matrix path computes the loss with it.
 int gemm_bf16_nt_f32(const void *A, int M, const void *B, int N, int K, float *C, int ldc, bool accumulate, int *err,
-                     cudaStream_t st)
+                     cudaStream_t st, int stall_polls, int k_chunk)
 {
-    GemmArgs a{};
-    a.M = M;
-    a.N = N;
-    a.K = K;
-    a.err = err;
-    a.c32 = C;
-    a.ld32 = ldc;
-    a.add = accumulate ? C : nullptr;
-    return gemm_nt(EPI_NONE, static_cast<const bf16 *>(A), static_cast<const bf16 *>(B), a, st);
+    // one launch per K chunk: the tensor cores sum at most k_chunk products
+    // into one FP32 accumulator, and the chunks are added in FP32 by the
+    // epilogue (C += chunk, in chunk order)
+    const int kc = k_chunk > 0 ? k_chunk : K;
+    for (int k0 = 0; k0 < K; k0 += kc) {
+        GemmArgs a{};
+        a.M = M;
+        a.N = N;
+        a.K = std::min(kc, K - k0);
+        a.k0 = k0;
+        a.ldk = K;
+        a.err = err;
+        a.stall_polls = k0 == 0 ? stall_polls : 0;
+        a.c32 = C;
+        a.ld32 = ldc;
+        a.add = (accumulate || k0 > 0) ? C : nullptr;
+        const int rc = gemm_nt(EPI_NONE, static_cast<const bf16 *>(A), static_cast<const bf16 *>(B), a, st);
+        if (rc) return rc;
+    }
+    return GD_OK;
 }
 
 }  // namespace gd
@@ -513,6 +548,7 @@ struct gd_mlp {
     float in_gain = 1.f, out_gain = 1.f;  // global input / output normalisation
     Layer L[5];
     int64_t step = 0;
+    int stall_next = 0;  // gd_mlp_inject_timeout: polls for the next forward's first GEMM
     // activations, [cap][features]
     bf16 *xb = nullptr, *h0b = nullptr, *h1b = nullptr, *h2b = nullptr, *zb = nullptr;
     float *h0 = nullptr, *a1 = nullptr, *a2 = nullptr, *y = nullptr, *tt = nullptr;
@@ -590,6 +626,8 @@ int forward(gd_mlp *h, int B, cudaStream_t st)
     using namespace gd;
     int rc;
     GemmArgs a = args(B, 256, h->n_in_p, h->err);
+    a.stall_polls = h->stall_next;  // a pending time-out injection fires here, once
+    h->stall_next = 0;
     a.bias = h->L[0].b;
     a.c32 = h->h0;
     a.ld32 = 256;
@@ -704,7 +742,12 @@ int check_err(gd_mlp *h, cudaStream_t st)
     int flag = 0;
     GD_CUDA(cudaMemcpyAsync(&flag, h->err, sizeof(int), cudaMemcpyDeviceToHost, st));
     GD_CUDA(cudaStreamSynchronize(st));
-    if (flag) return gd::set_error(GD_ERR_CUDA, "surrogate GEMM: a pipeline wait timed out");
+    if (flag) {
+        // clear the record so that later calls start clean
+        GD_CUDA(cudaMemsetAsync(h->err, 0, sizeof(int), st));
+        GD_CUDA(cudaStreamSynchronize(st));
+        return gd::set_error(GD_ERR_CUDA, "surrogate GEMM: a pipeline wait timed out");
+    }
     return GD_OK;
 }
 
@@ -977,4 +1020,13 @@ extern "C" int gd_mlp_get_grads(gd_mlp *h, float *host)
 {
     if (!h || !host) return gd::set_error(GD_ERR_INVALID_ARG, "NULL argument");
     return copy_params(h, host, true, true);
+}
+
+extern "C" int gd_mlp_inject_timeout(gd_mlp *h, int polls)
+{
+    using namespace gd;
+    if (!h || polls < 1 || polls > (1 << 20))
+        return set_error(GD_ERR_INVALID_ARG, "gd_mlp_inject_timeout: need a network and 1 <= polls <= 2^20");
+    h->stall_next = polls;
+    return GD_OK;
 }

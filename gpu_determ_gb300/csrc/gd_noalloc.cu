@@ -13,8 +13,17 @@
 //
 // Set-up: the first call on a device looks up the array's device address
 // with cudaGetSymbolAddress (with that device current) and caches it; make
-// that first call before any stream capture.  Later calls only launch
-// kernels and clear the partial sums with cudaMemsetAsync.
+// that first call before any stream capture.  With lazy module loading (the
+// CUDA default) that lookup is also what loads this library's device code on
+// the device, and so reserves the 64 MiB array there: a caller that wants no
+// allocation of any kind inside its hot loop makes one warm-up call at
+// start-up.  Later calls only launch kernels and clear the partial sums with
+// cudaMemsetAsync.
+//
+// The chunking of the s walk is the one gd_collision picks when it fits the
+// array (at most kMaxChunks chunks); then the result is bitwise that of
+// gd_collision's FP32 pair gain.  When it does not fit, fewer chunks are
+// used, and the sums agree within FP32 rounding of the other order.
 //
 // All calls share the one array and it keeps the last call's contents; the
 // partial sums are cleared at the start of every call.  Calls whose work

@@ -569,15 +569,17 @@ int pair_tc_build(Context &c)
     return GD_OK;
 }
 
-int pair_tc_check(Context &c, cudaStream_t st)
+int pair_tc_take_timeout(Context &c, cudaStream_t st, bool *timed_out)
 {
+    *timed_out = false;
     if (!c.pair_tc) return GD_OK;
     int flag = 0;
     GD_CUDA(cudaMemcpyAsync(&flag, c.pair_tc->err, sizeof(int), cudaMemcpyDeviceToHost, st));
     GD_CUDA(cudaStreamSynchronize(st));
+    *timed_out = flag != 0;
     if (flag) {
-        GD_CUDA(cudaMemset(c.pair_tc->err, 0, sizeof(int)));
-        return set_error(GD_ERR_CUDA, "pair tensor-core gain kernel: a pipeline wait timed out");
+        GD_CUDA(cudaMemsetAsync(c.pair_tc->err, 0, sizeof(int), st));
+        GD_CUDA(cudaStreamSynchronize(st));
     }
     return GD_OK;
 }
@@ -626,13 +628,24 @@ int run_pair_tc(Context &c, const float *f, int ncells, int ld, float *gain, cud
         pair_tc_kernel<false><<<grid, kPtThreads, smem, st>>>(tWh, tWl, a);
     }
     GD_CUDA(cudaGetLastError());
-    if ((rc = reduce_gain_partials(c, part, nchunks, cells_pad, ncells, ld, gain, st))) return rc;
-    // the kernel records a time-out instead of hanging; report it (inside a
-    // stream capture the flag stays set for gd_ctx_check after replay)
-    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
-    GD_CUDA(cudaStreamIsCapturing(st, &cap));
-    if (cap != cudaStreamCaptureStatusNone) return GD_OK;
-    return pair_tc_check(c, st);
+    // the kernel records a pipeline time-out instead of hanging; the call only
+    // enqueues work, and gd_ctx_check reports the record
+    return reduce_gain_partials(c, part, nchunks, cells_pad, ncells, ld, gain, st);
 }
 
 }  // namespace gd
+
+extern "C" int gd_pair_tc_table(gd_ctx *ctx, int64_t *rows, int *wrow, uint16_t *wh, uint16_t *wl)
+{
+    using namespace gd;
+    if (!ctx || !rows) return set_error(GD_ERR_INVALID_ARG, "NULL argument");
+    Context &c = ctx->c;
+    if (!c.pair_tc) return set_error(GD_ERR_UNSUPPORTED, "the pair tensor-core weight table is not built");
+    DeviceGuard g(c.device);
+    *rows = c.pair_tc->rows;
+    if (wrow) GD_CUDA(cudaMemcpy(wrow, c.pair_tc->wrow, sizeof(int) * c.d.nxyz, cudaMemcpyDeviceToHost));
+    const size_t bytes = (size_t)c.pair_tc->rows * PT_KC * sizeof(__nv_bfloat16);
+    if (wh) GD_CUDA(cudaMemcpy(wh, c.pair_tc->wh, bytes, cudaMemcpyDeviceToHost));
+    if (wl) GD_CUDA(cudaMemcpy(wl, c.pair_tc->wl, bytes, cudaMemcpyDeviceToHost));
+    return GD_OK;
+}

@@ -43,18 +43,23 @@ __device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity)
     return ok != 0;
 }
 
-// Bounded wait for the phase with the given parity; false (and *err = 1)
-// when it did not complete.  Also gives up as soon as another CTA has
-// recorded a time-out, so a failing launch ends quickly.
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int *err)
+// Bounded wait for the phase with the given parity: at most `limit` polls;
+// false (and *err = 1) when it did not complete.  Also gives up as soon as
+// another CTA has recorded a time-out, so a failing launch ends quickly.
+__device__ __forceinline__ bool mbar_wait_limit(uint32_t bar, uint32_t parity, int *err, uint32_t limit)
 {
-    constexpr uint32_t kWaitLimit = 1u << 20;  // bounded polls per wait
-    for (uint32_t it = 0; it < kWaitLimit; it++) {
+    for (uint32_t it = 0; it < limit; it++) {
         if (mbar_try_wait(bar, parity)) return true;
         if ((it & 255u) == 255u && *(volatile int *)err) return false;
     }
     atomicExch(err, 1);
     return false;
+}
+
+// The pipeline waits of every kernel: 2^20 polls.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int *err)
+{
+    return mbar_wait_limit(bar, parity, err, 1u << 20);
 }
 
 __device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap *map, int c0, int c1, uint32_t bar)

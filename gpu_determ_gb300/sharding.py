@@ -31,13 +31,25 @@ def _dist():
     return dist if dist.is_available() and dist.is_initialized() else None
 
 
+def reduce_device(dist, device=None):
+    """Device of the one-scalar tensors the all-reduces use: the caller's
+    choice, else the current CUDA device under NCCL (which reduces only CUDA
+    tensors), else the CPU."""
+    if device is not None:
+        return device
+    import torch
+    if dist is not None and dist.get_backend() == "nccl":
+        return torch.device("cuda", torch.cuda.current_device())
+    return torch.device("cpu")
+
+
 def max_over_ranks(value: float, device=None) -> float:
     """Maximum of a host scalar over all ranks (the value itself alone)."""
     dist = _dist()
     if dist is None:
         return float(value)
     import torch
-    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    t = torch.tensor([float(value)], dtype=torch.float64, device=reduce_device(dist, device))
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
 
@@ -49,8 +61,10 @@ def global_courant_dt(local_max_nu, courant: float):
     tensor on the backend's device).  Returns a Python float."""
     dist = _dist()
     import torch
-    t = local_max_nu if torch.is_tensor(local_max_nu) else torch.tensor([float(local_max_nu)])
-    t = t.reshape(1).to(torch.float32).clone()
+    if torch.is_tensor(local_max_nu):
+        t = local_max_nu.reshape(1).to(torch.float32).clone()
+    else:
+        t = torch.tensor([float(local_max_nu)], dtype=torch.float32, device=reduce_device(dist))
     if dist is not None:
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
     m = float(t.item())

@@ -160,8 +160,10 @@ int gd_moments(gd_ctx *ctx, const float *f, int ncells, int ld, double *m5, gd_s
  * the stream and returns GD_ERR_SINGULAR when a projection met a cell with
  * non-finite f, nu or gain sums or a singular 5x5 system (that cell's
  * frequency was left uncorrected; the message names the first such cell),
- * or the error of a timed-out tensor-core pipeline wait; clears the record.
- * The collision, projection and step calls themselves never synchronise. */
+ * or GD_ERR_CUDA when a tensor-core pipeline wait of the context's gain or
+ * loss kernels timed out (the message names every record that was set);
+ * reads and clears all records.  The collision, projection and step calls
+ * themselves never synchronise, on any gain path. */
 int gd_ctx_check(gd_ctx *ctx, gd_stream stream);
 
 /* ---- collision-matrix path (tensor cores) ------------------------------ */
@@ -189,9 +191,19 @@ int gd_cmatrix_destroy(gd_cmatrix *cm);
  * of every collision-matrix tile; a call with at most 128 cells runs one CTA
  * per MMA.  Results are bitwise the same either way. */
 int gd_cmatrix_set_cluster(gd_cmatrix *cm, int ctas);
-/* gd_cmatrix_gain synchronises the stream and reports a pipeline time-out of
- * its kernel, except inside a stream capture; after replaying a captured
- * graph, gd_cmatrix_check (synchronising) reports it instead. */
+/* Longest run of stored tiles (an even count; 0 = unlimited; default 4)
+ * summed into one tensor-memory accumulator before the epilogue folds it
+ * into the FP32 gain (compensated), and the K chunk (tiles x 64 columns) of
+ * each launch of the tensor-core loss, whose FP32 results are added in
+ * order.  The tensor cores' FP32 accumulation loses precision over long
+ * sums: at 20^3 the BF16x3 gain is 6.4e-7 from FP64 (median over cells) with
+ * 4 tiles, 2.5e-6 unlimited; the loss carries a -1.2e-5 bias unchunked. */
+int gd_cmatrix_set_chain(gd_cmatrix *cm, int tiles);
+/* gd_cmatrix_gain only enqueues work on the stream.  Its kernels record a
+ * pipeline time-out (a bounded wait that ran out) instead of hanging;
+ * gd_cmatrix_check synchronises the stream, returns GD_ERR_CUDA when such a
+ * record is set, and clears it (gd_ctx_check does the same for a context's
+ * own matrices). */
 int gd_cmatrix_check(gd_cmatrix *cm, gd_stream stream);
 /* Gain algorithm used by gd_collision and gd_step for this context:
  * GD_GAIN_PAIR (default, FP32 pair-product kernel), GD_GAIN_CMATRIX_BF16 or
@@ -220,8 +232,15 @@ int gd_compact_to_box(gd_ctx *ctx, const float *compact, int ncells, int ld, flo
  * start-up).  Its partial sums live in a fixed 64 MiB array inside the
  * library image, held on every GPU that loads the library until exit; a batch
  * needing more (about 4500 cells on a 20^3 grid cut to R=4.8) is rejected with
- * GD_ERR_UNSUPPORTED.  The first call on a device looks the array's address
- * up (make it before any stream capture).  All calls share the array: calls
+ * GD_ERR_UNSUPPORTED.  The result is bitwise equal to gd_collision's FP32
+ * pair gain when the s-chunk count that call picks fits the array (at most
+ * 64 chunks; then both sum in the same order); otherwise the array holds
+ * fewer chunks and the sums, ordered differently, agree within FP32
+ * rounding.  The first call on a device looks the array's address up, which
+ * may also load the library's device code on that device and so reserve the
+ * 64 MiB there (the driver's allocation, not a cudaMalloc): a caller that
+ * wants no allocation at all inside its hot loop makes one warm-up call at
+ * start-up, before any stream capture.  All calls share the array: calls
  * that overlap on the GPU race, so order them. */
 int gd_gain_noalloc(gd_ctx *ctx, const float *f, int ncells, int ld, float *gain, gd_stream stream);
 
@@ -233,9 +252,9 @@ int gd_gain_noalloc(gd_ctx *ctx, const float *f, int ncells, int ld, float *gain
  * runs eagerly and sizes every buffer; with use_graph each later call replays
  * one CUDA graph captured on the second call (one cudaGraphLaunch per step).
  * Adding a group drops the graph.  Steps are ordered after earlier work on
- * `stream`, and later work on `stream` after them.  Inside the graph the
- * collision-matrix kernels do not report pipeline time-outs; gd_batch_check
- * (synchronising) does.  No reference counterpart: the reference steps one
+ * `stream`, and later work on `stream` after them.  Steps never synchronise;
+ * gd_batch_check (synchronising) runs gd_ctx_check on every group's context
+ * and returns the first error.  No reference counterpart: the reference steps one
  * grid, one batch of npx <= 1024 cells, from a host loop (determ.cu:62-80). */
 typedef struct gd_batch gd_batch;
 int gd_batch_create(gd_batch **out);
@@ -337,6 +356,55 @@ int gd_surrogate_gain(gd_surrogate *s, const float *f, int ncells, int ld, float
 /* out[c] = ||a[:,c] - b[:,c]||_2 / ||b[:,c]||_2 over n rows (FP64). */
 int gd_cell_rel_l2(const double *a, int lda, const double *b, int ldb, int n, int ncells, double *out,
                    gd_stream stream);
+
+/* The pair-product formulation's tables exactly as the gain kernels read
+ * them, copied to host buffers, for checks of the gain's index map against
+ * an independent enumeration of the reference's (i, i1, n) -> (l, l1) map
+ * (collision_integral.cu:88-94, 115-131, 154-155).  sizes is always filled;
+ * each array may be NULL (then it is not written).
+ *   grp_row_off[n_groups + 1]  entries of group m: [grp_row_off[m], grp_row_off[m+1])
+ *   entry_class[n_entries], entry_w[n_entries]: class-box index
+ *     (x2 * hy + y2) * hz + z2 of the offset n (n_a = 2 a2 + parity of the
+ *     pair sum) and the FP32 weight (rows padded with w = 0 to multiples of 8)
+ *   item_off[nx*ny*nz + 1]: work items of D (box-indexed, D_a = min(s_a,
+ *     2 n_a - 2 - s_a)): [item_off[D], item_off[D+1])
+ *   items[3 * n_items]: {group, first member, end member} per item
+ *   members[n_members]: member g as x2 | y2 << 6 | z2 << 12 (g_a = 2 a2 +
+ *     parity), the members of the group that lie in B(D)
+ * gd_pair_tc_table copies the per-D weight table of GD_GAIN_PAIR_TC (built
+ * when that path is selected, else GD_ERR_UNSUPPORTED): *rows rows of 64
+ * BF16 (hi and lo parts, raw bits), wrow[nx*ny*nz] the first row of each D;
+ * row wrow[D] + chunk * pad16(items of D) + item holds the item's weights at
+ * the box's class offsets (x2 * ey + y2) * ez + z2 = chunk * 64 + column.
+ * No reference counterpart (the reference has only the dense table a). */
+typedef struct {
+    int n_groups, nclass;
+    int64_t n_entries, n_items, n_members;
+} gd_pair_table_sizes;
+int gd_pair_tables(gd_ctx *ctx, gd_pair_table_sizes *sizes, int *grp_row_off, int *entry_class, float *entry_w,
+                   int *item_off, int *items, uint32_t *members);
+int gd_pair_tc_table(gd_ctx *ctx, int64_t *rows, int *wrow, uint16_t *wh, uint16_t *wl);
+
+/* Failure-detection test hooks (host-side injection; nothing faults).  The
+ * next launch of the named tensor-core GEMM makes every CTA wait `polls`
+ * polls (1..2^20) on an mbarrier that nothing arrives at, before it has
+ * issued any copy or MMA.  That bounded wait runs out, the CTA records the
+ * time-out, frees its tensor memory and returns; later kernels of the same
+ * object see the record and skip their work.  The record is reported and
+ * cleared by gd_mlp_check (for gd_mlp_inject_timeout: the first GEMM of the
+ * next forward pass or training step) or gd_ctx_check (for
+ * gd_ctx_inject_timeout: the first GEMM of the next tensor-core loss of a
+ * context on a collision-matrix gain path, else GD_ERR_UNSUPPORTED).  The
+ * call after that computes normally.  No reference counterpart: the
+ * reference has no failure handling (collision_integral.cu:601,622). */
+int gd_mlp_inject_timeout(gd_mlp *net, int polls);
+int gd_ctx_inject_timeout(gd_ctx *ctx, int polls);
+
+/* Measured fused multiply-add throughput of `device` in FLOP/s (2 per FMA),
+ * precision 32 (FP32 FFMA) or 64 (FP64 DFMA): the roofline denominator of the
+ * SIMT kernels.  Synchronous; allocates a few bytes.  No reference
+ * counterpart (the reference only times whole phases, gputimer.hpp:10-46). */
+int gd_fma_peak(int device, int precision, double *flops_per_s);
 
 #ifdef __cplusplus
 }

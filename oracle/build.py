@@ -8,7 +8,9 @@
 ``oracle/_ref/libref_weights.so``, reading them where they lie in the
 reference checkout and streaming them through the compiler's standard input
 between ``ref_prelude.h`` and ``ref_epilogue.cpp``; no reference source is
-written into the repository.  It is skipped when the checkout is absent.
+written into the repository.  The checkout is $GD_REFERENCE_DIR, else a
+directory ``reference`` beside this repository; the step is skipped (returns
+None) when it is absent, e.g. on a machine that has only this repository.
 """
 from __future__ import annotations
 
@@ -17,7 +19,9 @@ import subprocess
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF_DIR_DEFAULT = "/root/reference"
+# the reference checkout: $GD_REFERENCE_DIR, else a directory "reference"
+# beside this repository
+REF_DIR_DEFAULT = os.path.normpath(os.path.join(HERE, "..", "..", "reference"))
 ORACLE_SO = os.path.join(HERE, "liboracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libref_weights.so")
 

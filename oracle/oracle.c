@@ -509,6 +509,63 @@ void or_count_work(const or_ctx *c, int64_t *out3)
     out3[2] = subterms;
 }
 
+/* The index map of the gain as a digest: every (output node i in the sphere,
+ * partner i1 in the box, post-collision offset n) with a nonzero weight whose
+ * post-collision nodes l, l1 stay in the box (collision_integral.cu:88-94,
+ * 115-131; out-of-box partners hit the N_YZ sentinel, :130-131, 154-155), as
+ * the key k = i << 32 | s << 15 | n with i the compact index, s = i + i1 the
+ * linear pair-sum index over (2nx-1)(2ny-1)(2nz-1) and n the box index of the
+ * offset.  out4 = {count, sum of mix_a(k), xor of mix_b(k), sum of the FP64
+ * weights}; the sums wrap mod 2^64, so the digest is independent of the
+ * enumeration order and any other enumeration of the same set reproduces it. */
+static inline uint64_t or_mix_a(uint64_t z)
+{
+    z += 0x9e3779b97f4a7c15ull; /* splitmix64 finaliser */
+    z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+    z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+    return z ^ (z >> 31);
+}
+
+static inline uint64_t or_mix_b(uint64_t z)
+{
+    z ^= 0x5851f42d4c957f2dull;
+    z = (z ^ (z >> 33)) * 0xff51afd7ed558ccdull; /* murmur3 finaliser */
+    z = (z ^ (z >> 33)) * 0xc4ceb9fe1a85ec53ull;
+    return z ^ (z >> 33);
+}
+
+void or_index_map_digest(const or_ctx *c, uint64_t *out4)
+{
+    const int sy = 2 * c->ny - 1, sz = 2 * c->nz - 1;
+    uint64_t cnt = 0, sa = 0, xb = 0;
+    double wsum = 0.0;
+#pragma omp parallel for schedule(dynamic, 1) reduction(+ : cnt, sa, wsum) reduction(^ : xb)
+    for (int p = 0; p < c->n_pnt; p++) {
+        const int ix = c->ui[p], iy = c->vi[p], iz = c->wi[p];
+        for (int jx = 0; jx < c->nx; jx++)
+            for (int jy = 0; jy < c->ny; jy++)
+                for (int jz = 0; jz < c->nz; jz++) {
+                    const int gidx = (abs(ix - jx) * c->ny + abs(iy - jy)) * c->nz + abs(iz - jz);
+                    const uint64_t s_lin = ((uint64_t)(ix + jx) * sy + (iy + jy)) * sz + (iz + jz);
+                    for (int64_t e = c->list_off[gidx]; e < c->list_off[gidx + 1]; e++) {
+                        or_octet o;
+                        const int16_t *n = c->list[e].n;
+                        if (!octet_for(c, ix + jx, iy + jy, iz + jz, n, &o)) continue;
+                        const uint64_t n_box = ((uint64_t)n[0] * c->ny + n[1]) * c->nz + n[2];
+                        const uint64_t k = ((uint64_t)p << 32) | (s_lin << 15) | n_box;
+                        cnt++;
+                        sa += or_mix_a(k);
+                        xb ^= or_mix_b(k);
+                        wsum += c->list[e].w;
+                    }
+                }
+    }
+    out4[0] = cnt;
+    out4[1] = sa;
+    out4[2] = xb;
+    memcpy(&out4[3], &wsum, sizeof(double));
+}
+
 /* ------------------------------------------------------------------------ */
 /* Loss                                                                      */
 /* ------------------------------------------------------------------------ */

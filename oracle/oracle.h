@@ -47,6 +47,10 @@ const int *or_compact_of_box(const or_ctx *c);
 /* counts of the work: nonzero weight entries, valid (i,i1,n) terms with the
  * output node in the sphere, sub-terms whose two nodes are both in the sphere */
 void or_count_work(const or_ctx *c, int64_t *out3);
+/* digest of the gain's index map (i, s = i + i1, n) over in-sphere outputs,
+ * box partners, nonzero weights and in-box post-collision pairs:
+ * {count, sum mix_a(key), xor mix_b(key), FP64 sum of the weights as bits} */
+void or_index_map_digest(const or_ctx *c, uint64_t *out4);
 
 /* ---- loss / gain on box-layout f (zero outside the sphere) -------------- */
 /* FP64: nu[k][cell] = sum_j b(|i-j|) f[j][cell] for box node i = nodes[k]

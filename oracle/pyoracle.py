@@ -49,6 +49,7 @@ def lib():
         L.or_compact_of_box.argtypes = [C.c_void_p]
         L.or_compact_of_box.restype = C.POINTER(C.c_int)
         L.or_count_work.argtypes = [C.c_void_p, _i64p]
+        L.or_index_map_digest.argtypes = [C.c_void_p, np.ctypeslib.ndpointer(np.uint64, flags="C_CONTIGUOUS")]
         for name, outp in (("or_loss_f64", _f64p), ("or_gain_f64", _f64p),
                            ("or_loss_f32", _f32p), ("or_gain_f32", _f32p)):
             getattr(L, name).argtypes = [C.c_void_p, _f32p, C.c_int, _i32p, C.c_int, outp]
@@ -131,6 +132,13 @@ class Oracle:
         out = np.zeros(3, np.int64)
         lib().or_count_work(self._c, out)
         return {"nonzero_weights": int(out[0]), "terms": int(out[1]), "subterms": int(out[2])}
+
+    def index_map_digest(self):
+        """Digest of the gain's index map: (count, sum mix_a, xor mix_b,
+        FP64 weight sum) over keys i << 32 | s << 15 | n (or_index_map_digest)."""
+        out = np.zeros(4, np.uint64)
+        lib().or_index_map_digest(self._c, out)
+        return int(out[0]), int(out[1]), int(out[2]), float(out[3:4].view(np.float64)[0])
 
     # layouts --------------------------------------------------------------
     def to_box(self, f_compact):

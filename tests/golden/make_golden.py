@@ -1,7 +1,7 @@
 """Generate the golden fixtures in this directory from the reference checkout.
 
-Run in a container that has the savthe/gpu_determ checkout (default
-/root/reference, or $GD_REFERENCE_DIR):
+Run on a machine that has the savthe/gpu_determ checkout ($GD_REFERENCE_DIR,
+else a directory "reference" beside this repository):
 
     python tests/golden/make_golden.py
 
@@ -93,7 +93,9 @@ def ref_tables() -> dict:
 
 
 def main():
-    ref_dir = os.environ.get("GD_REFERENCE_DIR", "/root/reference")
+    ref_dir = os.environ.get("GD_REFERENCE_DIR", obuild.REF_DIR_DEFAULT)
+    if not os.path.exists(os.path.join(ref_dir, "true_results.out")):
+        raise SystemExit(f"reference checkout not found at {ref_dir}: set GD_REFERENCE_DIR")
     with open(os.path.join(HERE, "true_results_nodes.json"), "w") as fh:
         json.dump(golden_nodes(ref_dir), fh, indent=1)
     with open(os.path.join(HERE, "ref_tables.json"), "w") as fh:

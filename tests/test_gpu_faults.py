@@ -1,6 +1,9 @@
 """Failure handling injected on the host (no GPU fault): non-finite inputs and
 singular systems reach the caller as a status from gd_ctx_check, a memory cap
-makes object creation fail cleanly with GD_ERR_OUT_OF_MEMORY."""
+makes object creation fail cleanly with GD_ERR_OUT_OF_MEMORY, and a bounded
+device wait that is made to run out (an mbarrier that nothing arrives at,
+waited on before any copy or MMA is issued) is reported once by the check,
+leaves the tensor memory free, and the next call is bitwise the clean one."""
 import numpy as np
 import pytest
 
@@ -74,3 +77,52 @@ def test_memory_limit(gdlib, cuda):
     ctx.check()
     ctx.set_gain_path(gdlib.GAIN_PAIR_TC)
     ctx.check()
+
+
+def test_timed_out_wait_on_context_is_reported_once(gdlib, cuda):
+    """The collision calls only enqueue work on the tensor-core path; a timed
+    out pipeline wait of the tensor-core loss GEMM reaches the caller through
+    gd_ctx_check, which clears it."""
+    torch = cuda
+    ctx, f = _setup(gdlib, torch)      # 64 cells: one CTA per tensor-core MMA
+    ctx.set_gain_path(gdlib.GAIN_CMATRIX_BF16)
+    nu0, g0 = torch.empty_like(f), torch.empty_like(f)
+    ctx.collision(f, 64, 64, nu0, g0)
+    ctx.check()
+    ctx.inject_timeout(256)
+    nu1, g1 = torch.empty_like(f), torch.empty_like(f)
+    ctx.collision(f, 64, 64, nu1, g1)  # enqueues; reports nothing itself
+    with pytest.raises(gdlib.GDError) as e:
+        ctx.check()
+    assert e.value.code == 2 and "timed out" in str(e.value)
+    ctx.check()                        # the record was cleared
+    nu2, g2 = torch.empty_like(f), torch.empty_like(f)
+    ctx.collision(f, 64, 64, nu2, g2)  # a new tcgen05 allocation succeeds: the stalled CTAs freed theirs
+    ctx.check()
+    assert torch.equal(nu2, nu0) and torch.equal(g2, g0)
+    with pytest.raises(gdlib.GDError):
+        ctx.inject_timeout(0)
+    ctx.set_gain_path(gdlib.GAIN_PAIR)
+    with pytest.raises(gdlib.GDError) as e:
+        ctx.inject_timeout(256)        # the FP32 path has no tensor-core wait to stall
+    assert e.value.code == 4
+
+
+def test_timed_out_wait_on_network_is_reported_once(gdlib, cuda):
+    torch = cuda
+    ctx, f = _setup(gdlib, torch)
+    net = gdlib.Mlp(ctx.n_pnt, ctx.n_pnt, batch_cap=64)
+    y0 = torch.empty_like(f)
+    net.forward(f, 64, 64, y0, 64)
+    net.check()
+    net.inject_timeout(256)
+    y1 = torch.empty_like(f)
+    net.forward(f, 64, 64, y1, 64)
+    with pytest.raises(gdlib.GDError) as e:
+        net.check()
+    assert e.value.code == 2 and "timed out" in str(e.value)
+    net.check()
+    y2 = torch.empty_like(f)
+    net.forward(f, 64, 64, y2, 64)
+    net.check()
+    assert torch.equal(y2, y0)

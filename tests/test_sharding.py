@@ -27,6 +27,23 @@ def test_single_process_fallbacks():
     assert sharding.global_courant_dt(100.0, 0.5) == pytest.approx(0.005)
 
 
+class _FakeDist:
+    def __init__(self, backend):
+        self.backend = backend
+
+    def get_backend(self):
+        return self.backend
+
+
+def test_reduce_device_follows_backend(monkeypatch):
+    torch = pytest.importorskip("torch")
+    monkeypatch.setattr(torch.cuda, "current_device", lambda: 3)
+    assert sharding.reduce_device(_FakeDist("nccl")) == torch.device("cuda", 3)   # NCCL reduces CUDA tensors
+    assert sharding.reduce_device(_FakeDist("gloo")) == torch.device("cpu")
+    assert sharding.reduce_device(None) == torch.device("cpu")
+    assert sharding.reduce_device(_FakeDist("nccl"), device="cpu") == "cpu"      # the caller's choice wins
+
+
 def _free_port():
     with socket.socket() as s:
         s.bind(("127.0.0.1", 0))
