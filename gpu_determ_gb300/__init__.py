@@ -29,6 +29,8 @@ GAIN_PAIR = 0
 GAIN_CMATRIX_BF16 = 1
 GAIN_CMATRIX_BF16X3 = 2
 GAIN_PAIR_TC = 3
+BATCH_STREAMS = 0
+BATCH_FUSED_PAIR_TC = 1
 MLP_SCALE_INPUT = 1
 MLP_SCALE_OUTPUT = 2
 MLP_LOSS_MSE = 4
@@ -140,6 +142,7 @@ def lib():
     L.gd_batch_destroy.argtypes = [vp]
     L.gd_batch_add.argtypes = [vp, vp, vp, i, i, i, f, vp, vp, vp]
     L.gd_batch_step.argtypes = [vp, i, vp]
+    L.gd_batch_set_mode.argtypes = [vp, i]
     L.gd_batch_check.argtypes = [vp]
     L.gd_batch_info.argtypes = [vp, P(i), P(i), P(i), P(C.c_int64)]
     L.gd_ctx_autotune.argtypes = [vp, vp, i, i, i, C.c_double, P(_Autotune), vp]
@@ -157,7 +160,7 @@ def lib():
                  "gd_mlp_loss", "gd_mlp_check", "gd_mlp_get_params", "gd_mlp_set_params", "gd_mlp_get_grads",
                  "gd_surrogate_create", "gd_surrogate_destroy", "gd_surrogate_gain", "gd_cell_rel_l2",
                  "gd_cmatrix_check", "gd_batch_create", "gd_batch_destroy", "gd_batch_add", "gd_batch_step",
-                 "gd_batch_check", "gd_batch_info", "gd_ctx_autotune", "gd_fma_peak",
+                 "gd_batch_check", "gd_batch_info", "gd_batch_set_mode", "gd_ctx_autotune", "gd_fma_peak",
                  "gd_mlp_inject_timeout", "gd_ctx_inject_timeout", "gd_pair_tables", "gd_pair_tc_table"):
         getattr(L, name).restype = i
     _lib = L
@@ -516,6 +519,11 @@ class Batch:
 
     def step(self, use_graph=True, stream=None):
         _check(lib().gd_batch_step(self._h, int(bool(use_graph)), _stream(stream)))
+
+    def set_mode(self, mode: int):
+        """BATCH_STREAMS (per-group steps on forked streams) or
+        BATCH_FUSED_PAIR_TC (every group's gain in one persistent launch)."""
+        _check(lib().gd_batch_set_mode(self._h, int(mode)))
 
     def check(self):
         _check(lib().gd_batch_check(self._h))

@@ -1,7 +1,7 @@
 """Batched cells on uneven velocity grids, stepped as one CUDA graph.
 
     python -m gpu_determ_gb300.batched [--cells 4096] [--grids 12 16 20 24] [--steps 50]
-                                       [--radius 4.8] [--mach 3] [--no-graph] [--no-autotune]
+                                       [--radius 4.8] [--mach 3] [--no-graph] [--no-autotune] [--fused]
 
 The cells sample a Mach-3 normal shock (inputs.shock_profile: tanh blend of
 the Rankine-Hugoniot upstream and downstream Maxwellians, gamma = 5/3,
@@ -21,12 +21,17 @@ import sys
 
 import numpy as np
 
-from . import DT_COURANT, GAIN_CMATRIX_BF16X3, GAIN_PAIR, GAIN_PAIR_TC, Batch, Context, GridSpec, inputs
+from . import (BATCH_FUSED_PAIR_TC, DT_COURANT, GAIN_CMATRIX_BF16X3, GAIN_PAIR, GAIN_PAIR_TC, Batch, Context, GridSpec,
+               inputs)
 
 
 def build(cells: int = 4096, grids=(12, 16, 20, 24), radius: float = 4.8, mach: float = 3.0,
-          courant: float = 0.5, autotune: bool = True, mem_budget: float = 120e9, device: int = 0):
-    """Contexts, device arrays and the batch; returns a dict of them."""
+          courant: float = 0.5, autotune: bool = True, mem_budget: float = 120e9, device: int = 0,
+          fused: bool = False):
+    """Contexts, device arrays and the batch; returns a dict of them.  With
+    fused, every grid runs the pair products with the contraction on the
+    tensor cores and the batch computes all gains in one persistent launch
+    (BATCH_FUSED_PAIR_TC) instead of autotuned per-grid launches."""
     import torch
     dev = torch.device("cuda", device)
     groups = []
@@ -40,7 +45,9 @@ def build(cells: int = 4096, grids=(12, 16, 20, 24), radius: float = 4.8, mach: 
         f = torch.from_numpy(np.ascontiguousarray(f_all[:, mine])).to(dev)
         nc = len(mine)
         tune = None
-        if autotune:
+        if fused:
+            ctx.set_gain_path(GAIN_PAIR_TC)
+        elif autotune:
             tune = ctx.autotune(f, nc, nc,
                                 path_mask=(1 << GAIN_PAIR) | (1 << GAIN_PAIR_TC) | (1 << GAIN_CMATRIX_BF16X3),
                                 mem_budget=mem_budget)
@@ -49,7 +56,9 @@ def build(cells: int = 4096, grids=(12, 16, 20, 24), radius: float = 4.8, mach: 
         b.add(ctx, f, nc, nc, DT_COURANT, courant, m5=m5, time=t)
         groups.append({"grid": n, "n_pnt": ctx.n_pnt, "cells": nc, "ctx": ctx, "f": f, "m5": m5, "time": t,
                        "autotune": tune})
-    return {"batch": b, "groups": groups, "device": dev}
+    if fused:
+        b.set_mode(BATCH_FUSED_PAIR_TC)
+    return {"batch": b, "groups": groups, "device": dev, "fused": fused}
 
 
 def run(state: dict, steps: int = 50, use_graph: bool = True, warmup: int = 2) -> dict:
@@ -70,7 +79,8 @@ def run(state: dict, steps: int = 50, use_graph: bool = True, warmup: int = 2) -
     torch.cuda.synchronize(state["device"])
     ms = e0.elapsed_time(e1)
     cells = sum(g["cells"] for g in state["groups"])
-    out = {"cells": cells, "steps": steps, "graph": bool(use_graph), "ms_total": ms,
+    out = {"cells": cells, "steps": steps, "graph": bool(use_graph), "fused_gain_launch": state.get("fused", False),
+           "ms_total": ms,
            "cell_steps_per_s": cells * steps / (ms * 1e-3), "batch": b.info(), "grids": []}
     for g, m0 in zip(state["groups"], m_first):
         m1 = g["m5"]
@@ -95,8 +105,10 @@ def main(argv=None):
     p.add_argument("--no-graph", action="store_true")
     p.add_argument("--no-autotune", action="store_true")
     p.add_argument("--compare-eager", action="store_true", help="also time the same steps without the graph")
+    p.add_argument("--fused", action="store_true",
+                   help="every grid's gain in one persistent launch (pair products, contraction on tensor cores)")
     a = p.parse_args(argv)
-    state = build(a.cells, a.grids, a.radius, a.mach, autotune=not a.no_autotune)
+    state = build(a.cells, a.grids, a.radius, a.mach, autotune=not a.no_autotune, fused=a.fused)
     res = run(state, a.steps, use_graph=not a.no_graph)
     if a.compare_eager:
         res["eager"] = {k: v for k, v in run(state, a.steps, use_graph=False, warmup=0).items()

@@ -5,10 +5,12 @@
 // gd_step for every group: groups on different contexts run concurrently on
 // their own streams (forked from and joined back into the batch's stream);
 // groups sharing a context run in order on one stream, since a context's
-// scratch serves one launch at a time.  The first step runs eagerly (it sizes
-// every buffer and uploads every launch table); with use_graph the second
-// step captures the whole fork/join sequence into a CUDA graph and every
-// later step is one cudaGraphLaunch.
+// scratch serves one launch at a time.  In the fused mode every group's gain
+// is instead one persistent launch of the pair-product kernel over a device
+// list of (grid, cell tile, s-chunk) units of all groups.  The first step runs
+// eagerly (it sizes every buffer and uploads every launch table); with
+// use_graph the second step captures the whole sequence into a CUDA graph and
+// every later step is one cudaGraphLaunch.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -38,6 +40,7 @@ struct gd_batch {
     cudaGraphExec_t exec = nullptr;
     int device = 0;
     int64_t steps = 0;
+    int mode = GD_BATCH_STREAMS;
 };
 
 namespace {
@@ -67,7 +70,73 @@ int enqueue_steps(gd_batch *b)
     return GD_OK;
 }
 
+// GD_BATCH_FUSED_PAIR_TC: every group's loss, then ONE persistent launch of
+// the pair-product gain (contraction on the tensor cores) for all groups,
+// then every group's projection and relaxation, all on the batch stream.
+// Each group's results equal gd_step on its context's GD_GAIN_PAIR_TC path
+// bit for bit (the same kernels, chunks and unit partials).
+int enqueue_fused(gd_batch *b)
+{
+    using namespace gd;
+    const size_t ng = b->groups.size();
+    std::vector<float *> nu(ng), gain(ng);
+    std::vector<double *> q(ng);
+    std::vector<PtJob> jobs(ng);
+    for (size_t k = 0; k < ng; k++) {
+        const gd_batch::Group &g = b->groups[k];
+        Context &c = g.ctx->c;
+        nu[k] = gain[k] = nullptr;
+        q[k] = nullptr;
+        int rc = step_buffers(c, g.ld, b->main, &nu[k], &gain[k], &q[k]);
+        if (!rc) rc = run_loss_path(c, g.f, g.ncells, g.ld, nu[k], b->main);
+        if (rc) return rc;
+        jobs[k] = PtJob{&c, g.f, g.ncells, g.ld, gain[k]};
+    }
+    int rc = launch_pair_tc(jobs.data(), (int)ng, b->main);
+    if (rc) return rc;
+    for (size_t k = 0; k < ng; k++) {
+        const gd_batch::Group &g = b->groups[k];
+        Context &c = g.ctx->c;
+        rc = run_project(c, g.f, nu[k], gain[k], g.ncells, g.ld, nu[k], q[k], nullptr, 0, 0.f, nullptr, g.m5, b->main);
+        if (!rc)
+            rc = run_relax_q(c, g.f, nu[k], gain[k], q[k], g.ncells, g.ld, g.mode, g.param, g.time_dev, g.dt_dev,
+                             b->main);
+        if (rc) return rc;
+    }
+    return GD_OK;
+}
+
+int check_fused(const gd_batch *b)
+{
+    using namespace gd;
+    if (b->groups.size() > 4) return set_error(GD_ERR_UNSUPPORTED, "fused batch: at most 4 groups");
+    for (size_t k = 0; k < b->groups.size(); k++) {
+        const Context &c = b->groups[k].ctx->c;
+        if (c.gain_path != GD_GAIN_PAIR_TC || !c.pair_tc)
+            return set_error(GD_ERR_UNSUPPORTED, "fused batch: every group's context needs gain path GD_GAIN_PAIR_TC");
+        for (size_t j = 0; j < k; j++)
+            if (b->groups[j].ctx == b->groups[k].ctx)
+                return set_error(GD_ERR_UNSUPPORTED, "fused batch: one group per context");
+    }
+    return GD_OK;
+}
+
 }  // namespace
+
+extern "C" int gd_batch_set_mode(gd_batch *b, int mode)
+{
+    using namespace gd;
+    if (!b) return set_error(GD_ERR_INVALID_ARG, "NULL argument");
+    if (mode != GD_BATCH_STREAMS && mode != GD_BATCH_FUSED_PAIR_TC)
+        return set_error(GD_ERR_INVALID_ARG, "unknown batch mode");
+    if (mode == GD_BATCH_FUSED_PAIR_TC) {
+        const int rc = check_fused(b);
+        if (rc) return rc;
+    }
+    b->mode = mode;
+    drop_graph(b);
+    return GD_OK;
+}
 
 extern "C" int gd_batch_create(gd_batch **out)
 {
@@ -144,12 +213,14 @@ extern "C" int gd_batch_step(gd_batch *b, int use_graph, gd_stream stream)
     GD_CUDA(cudaEventRecord(b->joined, user));
     GD_CUDA(cudaStreamWaitEvent(b->main, b->joined, 0));
     int rc = GD_OK;
+    if (b->mode == GD_BATCH_FUSED_PAIR_TC && (rc = check_fused(b))) return rc;
+    auto enqueue = [&]() { return b->mode == GD_BATCH_FUSED_PAIR_TC ? enqueue_fused(b) : enqueue_steps(b); };
     if (!use_graph || b->steps == 0) {
-        rc = enqueue_steps(b);
+        rc = enqueue();
     } else {
         if (!b->exec) {
             GD_CUDA(cudaStreamBeginCapture(b->main, cudaStreamCaptureModeRelaxed));
-            rc = enqueue_steps(b);
+            rc = enqueue();
             cudaGraph_t g = nullptr;
             cudaError_t e = cudaStreamEndCapture(b->main, &g);
             if (!rc && e != cudaSuccess) rc = cuda_error(e, "batch graph capture");

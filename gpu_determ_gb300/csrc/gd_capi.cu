@@ -203,6 +203,29 @@ int build_row_groups(Context &c)
     return build_s_schedule(c, gid);
 }
 
+// gd_step's buffers: nu, gain (FP32) and Q (FP64) for every one the caller
+// does not provide (NULL), context-owned and grown on demand (the growth
+// synchronises st; no allocation per step once sized).
+int step_buffers(Context &c, int ld, cudaStream_t st, float **nu, float **gain, double **q)
+{
+    if (*nu && *gain && *q) return GD_OK;
+    const size_t n = (size_t)c.d.n_pnt * ld;
+    const size_t need = n * (2 * sizeof(float) + sizeof(double));
+    if (c.step_buf.bytes < need) {
+        GD_CUDA(cudaStreamSynchronize(st));
+        cudaFree(c.step_buf.ptr);
+        c.step_buf.ptr = nullptr;
+        c.step_buf.bytes = 0;
+        GD_CUDA(cudaMalloc(&c.step_buf.ptr, need));
+        c.step_buf.bytes = need;
+    }
+    unsigned char *p = static_cast<unsigned char *>(c.step_buf.ptr);
+    if (!*q) *q = reinterpret_cast<double *>(p);
+    if (!*nu) *nu = reinterpret_cast<float *>(p + n * sizeof(double));
+    if (!*gain) *gain = reinterpret_cast<float *>(p + n * (sizeof(double) + sizeof(float)));
+    return GD_OK;
+}
+
 int set_error(int code, const std::string &msg)
 {
     g_last_error = msg;
@@ -254,6 +277,8 @@ static void destroy_context(Context &c)
     cudaFree(c.d_D_members);
     for (auto &kv : c.s_bounds_dev) cudaFree(kv.second);
     c.s_bounds_dev.clear();
+    for (auto &kv : c.pt_units_dev) cudaFree(kv.second.first);
+    c.pt_units_dev.clear();
     cudaFree(c.d_reduce);
     cudaFree(c.d_status);
     cudaFree(c.scratch.ptr);
@@ -569,26 +594,9 @@ int gd_step(gd_ctx *ctx, float *f, int ncells, int ld, int mode, float param, fl
     gd::DeviceGuard g(ctx->c.device);
     gd::Context &c = ctx->c;
     cudaStream_t st = (cudaStream_t)stream;
-    // step buffers: nu, gain (FP32) and Q (FP64) unless the caller provides
-    // them; context-owned and grown on demand (no allocation per step)
-    const size_t n = (size_t)c.d.n_pnt * ld;
     float *nu_b = nu, *gain_b = gain;
     double *q_b = q;
-    if (!nu_b || !gain_b || !q_b) {
-        const size_t need = n * (2 * sizeof(float) + sizeof(double));
-        if (c.step_buf.bytes < need) {
-            GD_CUDA(cudaStreamSynchronize(st));
-            cudaFree(c.step_buf.ptr);
-            c.step_buf.ptr = nullptr;
-            c.step_buf.bytes = 0;
-            GD_CUDA(cudaMalloc(&c.step_buf.ptr, need));
-            c.step_buf.bytes = need;
-        }
-        unsigned char *p = static_cast<unsigned char *>(c.step_buf.ptr);
-        if (!q_b) q_b = reinterpret_cast<double *>(p);
-        if (!nu_b) nu_b = reinterpret_cast<float *>(p + n * sizeof(double));
-        if (!gain_b) gain_b = reinterpret_cast<float *>(p + n * (sizeof(double) + sizeof(float)));
-    }
+    if ((rc = gd::step_buffers(c, ld, st, &nu_b, &gain_b, &q_b))) return rc;
     rc = gd::run_loss_path(c, f, ncells, ld, nu_b, st);
     if (!rc) rc = gd::run_gain_path(c, f, ncells, ld, gain_b, st);
     if (!rc) rc = gd::run_project(c, f, nu_b, gain_b, ncells, ld, nu_b, q_b, nullptr, 0, 0.f, nullptr, m5, st);

@@ -105,6 +105,9 @@ struct Context {
     // chunk boundaries on the device per chunk count, uploaded once (a
     // replayed CUDA graph reads them without any host copy)
     std::map<int, int *> s_bounds_dev;
+    // work-unit lists of pair tensor-core launches led by this context, per
+    // launch shape (device array, count), uploaded once
+    std::map<std::string, std::pair<int4 *, int>> pt_units_dev;
     int gain_waves = 2;         // gain launch: at least this many CTAs per SM (autotuned)
     float *d_reduce = nullptr;  // small device scalars (max nu, dt)
     unsigned int *d_status = nullptr;  // numeric status of projections: flags, first failing cell
@@ -191,6 +194,16 @@ int pair_tc_build(Context &c);
 void pair_tc_free(Context &c);
 double pair_tc_bytes(const Context &c);
 int run_pair_tc(Context &c, const float *f, int ncells, int ld, float *gain, cudaStream_t st);
+// several grids' pair tensor-core gains in one persistent launch (1-4 jobs on
+// distinct contexts with built tables); results equal separate launches bit
+// for bit
+struct PtJob {
+    Context *c;
+    const float *f;
+    int ncells, ld;
+    float *gain;
+};
+int launch_pair_tc(const PtJob *jobs, int njobs, cudaStream_t st);
 // reads (synchronising st) and clears the pipeline time-out record of the
 // pair tensor-core kernel; *timed_out receives whether it was set
 int pair_tc_take_timeout(Context &c, cudaStream_t st, bool *timed_out);
@@ -204,6 +217,8 @@ int encode_bf16_sw128(CUtensorMap *m, void *ptr, int rank, const uint64_t *dims,
 
 // scratch -------------------------------------------------------------------
 int ensure_scratch(Context &c, size_t bytes);
+// gd_step's nu / gain / Q buffers for the ones passed as NULL (gd_capi.cu)
+int step_buffers(Context &c, int ld, cudaStream_t st, float **nu, float **gain, double **q);
 
 // tensor-core GEMM (gd_mlp.cu): C[M][N] = (accumulate ? C : 0) + A B^T, A [M][K]
 // and B [N][K] K-major BF16 (K a multiple of 64), C FP32 with ldc % 4 == 0 and

@@ -60,7 +60,10 @@ constexpr int kEpiWarps = 12;            // three per TMEM lane quadrant
 constexpr int kProdWarps = 8;            // two groups of four
 constexpr int kPtThreads = 32 * (2 + kEpiWarps + kProdWarps);
 
-struct PtArgs {
+constexpr int kPtMaxGrids = 4;          // velocity grids one launch can serve
+
+// One velocity grid's tables and arrays as the kernel reads them.
+struct PtGrid {
     Dims d;
     const float *f;
     int ld, ncells, cells_pad;
@@ -71,7 +74,22 @@ struct PtArgs {
     const int *wrow;        // [nxyz] first weight row of each D
     const int *s_bounds;    // [chunks + 1]
     float *part;            // [chunk][n_pnt][cells_pad]
+};
+
+// A launch: up to kPtMaxGrids grids and the device list of work units
+// {grid, 128-cell tile, s-chunk, 0} that the persistent CTAs pull, one at a
+// time, from a device counter.
+struct PtLaunch {
+    PtGrid g[kPtMaxGrids];
+    const int4 *units;
+    int nunits;
+    int *next;  // the next unit to hand out (zeroed before the launch)
     int *err;
+};
+
+// The weight tables' tensor maps per grid (hi and lo parts).
+struct PtMaps {
+    CUtensorMap wh[kPtMaxGrids], wl[kPtMaxGrids];
 };
 
 // One (s, pass) of the walk: its class box, groups and weight rows.
@@ -84,7 +102,7 @@ struct Unit {
     int npass;
 };
 
-__device__ __forceinline__ void unit_of(const PtArgs &a, int sl, int q, Unit &u)
+__device__ __forceinline__ void unit_of(const PtGrid &a, int sl, int q, Unit &u)
 {
     const Dims &d = a.d;
     u.sz = sl % d.sz;
@@ -110,7 +128,7 @@ __device__ __forceinline__ void unit_of(const PtArgs &a, int sl, int q, Unit &u)
     u.wrow = __ldg(a.wrow + Did);
 }
 
-__device__ __forceinline__ int npass_of(const PtArgs &a, int sl)
+__device__ __forceinline__ int npass_of(const PtGrid &a, int sl)
 {
     const Dims &d = a.d;
     const int sz = sl % d.sz, sy = (sl / d.sz) % d.sy, sx = sl / (d.sz * d.sy);
@@ -130,7 +148,7 @@ __device__ __forceinline__ uint32_t pack_bf16(float first, float second)
 
 template <bool CMAP_SMEM>
 __global__ void __launch_bounds__(kPtThreads, 1)
-    pair_tc_kernel(const __grid_constant__ CUtensorMap tmWh, const __grid_constant__ CUtensorMap tmWl, PtArgs a)
+    pair_tc_kernel(const __grid_constant__ PtMaps maps, const __grid_constant__ PtLaunch L)
 {
     extern __shared__ __align__(1024) unsigned char dsmem[];
     unsigned char *base = reinterpret_cast<unsigned char *>(
@@ -139,11 +157,12 @@ __global__ void __launch_bounds__(kPtThreads, 1)
     __shared__ __align__(8) uint64_t full_bar[kPtStages], empty_bar[kPtStages], accf_bar[2], acce_bar[2];
     __shared__ uint32_t tmem_base_holder;
     __shared__ int epi_fail;
+    __shared__ int unit_slot, stop_flag;
 
-    const Dims &d = a.d;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (threadIdx.x == 0) {
         epi_fail = 0;
+        stop_flag = 0;
         for (int s = 0; s < kPtStages; s++) {
             mbar_init(smem_u32(&full_bar[s]), 4 + 1);  // four producer warps + the TMA arrival
             mbar_init(smem_u32(&empty_bar[s]), 1);      // the MMA commit
@@ -154,8 +173,8 @@ __global__ void __launch_bounds__(kPtThreads, 1)
         }
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
-    if (CMAP_SMEM)
-        for (int t = threadIdx.x; t < d.nxyz; t += blockDim.x) cmap_s[t] = a.cmap[t];
+    if (CMAP_SMEM)  // single-grid launches only: the box -> compact map of grid 0
+        for (int t = threadIdx.x; t < L.g[0].d.nxyz; t += blockDim.x) cmap_s[t] = L.g[0].cmap[t];
     if (warp == 1) {
         tmem_alloc<1>(smem_u32(&tmem_base_holder), 2 * PT_NMAX);
         asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -163,16 +182,34 @@ __global__ void __launch_bounds__(kPtThreads, 1)
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = tmem_base_holder;
-    const int16_t *cmap = CMAP_SMEM ? cmap_s : a.cmap;
 
-    const int m_tile = blockIdx.x, chunk = blockIdx.y;
-    const int s_begin = __ldg(a.s_bounds + chunk), s_end = __ldg(a.s_bounds + chunk + 1);
+    // per-role state that runs on across units: pipeline counters (stage,
+    // accumulator) and whether this thread's role is still healthy
+    int ck = 0, uc = 0;
+    bool ok = true;
+
+    // Units are pulled one at a time from the device counter by thread 0 and
+    // shared through unit_slot; every thread of the CTA meets the two barriers
+    // of each round, so all roles work on the same unit and the pipeline
+    // drains between units (units are long: a chunk of s for 128 cells).  A
+    // role that gave up after a timed-out wait raises stop_flag, and the CTA
+    // takes no further unit.
+    for (;;) {
+        if (threadIdx.x == 0) unit_slot = stop_flag ? L.nunits : atomicAdd(L.next, 1);
+        __syncthreads();
+        const int ui_ = unit_slot;
+        if (ui_ >= L.nunits) break;
+        const int4 un_ = L.units[ui_];
+        const PtGrid &a = L.g[un_.x];
+        const Dims &d = a.d;
+        const int m_tile = un_.y, chunk = un_.z;
+        const int s_begin = __ldg(a.s_bounds + chunk), s_end = __ldg(a.s_bounds + chunk + 1);
 
     if (warp == 0) {
         // ---- TMA: weight rows of every chunk --------------------------------------
-        if (lane == 0) {
-            int ck = 0;
-            bool ok = true;
+        if (lane == 0 && ok) {
+            {
+            const CUtensorMap *tmWh = &maps.wh[un_.x], *tmWl = &maps.wl[un_.x];
             for (int sl = s_begin; ok && sl < s_end; sl++) {
                 const int np = npass_of(a, sl);
                 for (int q = 0; ok && q < np; q++) {
@@ -180,7 +217,7 @@ __global__ void __launch_bounds__(kPtThreads, 1)
                     unit_of(a, sl, q, u);
                     for (int ch = 0; ch < u.nch; ch++, ck++) {
                         const int st = ck & 1;
-                        if (!mbar_wait(smem_u32(&empty_bar[st]), ((uint32_t)(ck >> 1) & 1u) ^ 1u, a.err)) {
+                        if (!mbar_wait(smem_u32(&empty_bar[st]), ((uint32_t)(ck >> 1) & 1u) ^ 1u, L.err)) {
                             ok = false;
                             break;
                         }
@@ -189,26 +226,26 @@ __global__ void __launch_bounds__(kPtThreads, 1)
                         mbar_expect_tx(fb, 2u * (uint32_t)u.npad * (PT_KC * 2));
                         const int row0 = u.wrow + ch * u.mpad + q * PT_NMAX;
                         for (int r = 0; r < u.npad; r += 16) {
-                            tma_load_2d(smem_u32(sb + 2 * kPTile + r * (PT_KC * 2)), &tmWh, 0, row0 + r, fb);
-                            tma_load_2d(smem_u32(sb + 2 * kPTile + kWTile + r * (PT_KC * 2)), &tmWl, 0, row0 + r,
+                            tma_load_2d(smem_u32(sb + 2 * kPTile + r * (PT_KC * 2)), tmWh, 0, row0 + r, fb);
+                            tma_load_2d(smem_u32(sb + 2 * kPTile + kWTile + r * (PT_KC * 2)), tmWl, 0, row0 + r,
                                         fb);
                         }
                     }
                 }
             }
+            }
         }
     } else if (warp == 1) {
         // ---- MMA ---------------------------------------------------------------------
-        if (lane == 0) {
-            int ck = 0, uc = 0;
-            bool ok = true;
+        if (lane == 0 && ok) {
+            {
             for (int sl = s_begin; ok && sl < s_end; sl++) {
                 const int np = npass_of(a, sl);
                 for (int q = 0; ok && q < np; q++, uc++) {
                     Unit u;
                     unit_of(a, sl, q, u);
                     const int buf = uc & 1;
-                    if (!mbar_wait(smem_u32(&acce_bar[buf]), ((uint32_t)(uc >> 1) & 1u) ^ 1u, a.err)) {
+                    if (!mbar_wait(smem_u32(&acce_bar[buf]), ((uint32_t)(uc >> 1) & 1u) ^ 1u, L.err)) {
                         ok = false;
                         break;
                     }
@@ -217,7 +254,7 @@ __global__ void __launch_bounds__(kPtThreads, 1)
                     const uint32_t idesc = umma_idesc_bf16(PT_BM, u.npad);
                     for (int ch = 0; ch < u.nch; ch++, ck++) {
                         const int st = ck & 1;
-                        if (!mbar_wait(smem_u32(&full_bar[st]), (uint32_t)(ck >> 1) & 1u, a.err)) {
+                        if (!mbar_wait(smem_u32(&full_bar[st]), (uint32_t)(ck >> 1) & 1u, L.err)) {
                             ok = false;
                             break;
                         }
@@ -238,6 +275,7 @@ __global__ void __launch_bounds__(kPtThreads, 1)
                     umma_commit(smem_u32(&accf_bar[buf]));
                 }
             }
+            }
         }
     } else if (warp < 2 + kEpiWarps) {
         // ---- epilogue: thread = cell = TMEM lane (warp % 4 is the lane quadrant it
@@ -245,18 +283,18 @@ __global__ void __launch_bounds__(kPtThreads, 1)
         const int quad = warp & 3;
         const int third = (warp - 2) >> 2;  // which of the quadrant's warps
         const int row = quad * 32 + lane;
+        if (ok) {
+        const int16_t *cmap = CMAP_SMEM ? cmap_s : a.cmap;
         const int cell = m_tile * PT_BM + row;
         const bool live = cell < a.ncells;
         float *part = a.part + (size_t)chunk * d.n_pnt * a.cells_pad + cell;
-        int uc = 0;
-        bool ok = true;
         for (int sl = s_begin; ok && sl < s_end; sl++) {
             const int np = npass_of(a, sl);
             for (int q = 0; ok && q < np; q++, uc++) {
                 Unit u;
                 unit_of(a, sl, q, u);
                 const int buf = uc & 1;
-                if (lane == 0 && !mbar_wait(smem_u32(&accf_bar[buf]), (uint32_t)(uc >> 1) & 1u, a.err)) epi_fail = 1;
+                if (lane == 0 && !mbar_wait(smem_u32(&accf_bar[buf]), (uint32_t)(uc >> 1) & 1u, L.err)) epi_fail = 1;
                 // all warps of a cell finish one unit before any starts the next
                 // (their targets may coincide across units); the decision to stop
                 // is taken after the barrier, by all of them alike
@@ -306,18 +344,19 @@ __global__ void __launch_bounds__(kPtThreads, 1)
                 if (lane == 0) mbar_arrive(smem_u32(&acce_bar[buf]));
             }
         }
+        }
     } else {
         // ---- pair products ------------------------------------------------------------
         const int pw = warp - 2 - kEpiWarps;
         const int grp = pw >> 2;             // fills the stages of chunks ck with ck % 2 == grp
         const int row = (pw & 3) * 32 + lane;  // cell row of the P tile
+        const uint32_t swz = (uint32_t)(row & 7);
+        const uint32_t rowoff = (uint32_t)(row >> 3) * 1024u + (uint32_t)(row & 7) * 128u;
+        if (ok) {
+        const int16_t *cmap = CMAP_SMEM ? cmap_s : a.cmap;
         const int cell = m_tile * PT_BM + row;
         const bool live = cell < a.ncells;
         const float *fcol = a.f + (live ? cell : 0);
-        const uint32_t swz = (uint32_t)(row & 7);
-        const uint32_t rowoff = (uint32_t)(row >> 3) * 1024u + (uint32_t)(row & 7) * 128u;
-        int ck = 0;
-        bool ok = true;
         for (int sl = s_begin; ok && sl < s_end; sl++) {
             const int np = npass_of(a, sl);
             for (int q = 0; ok && q < np; q++) {
@@ -327,7 +366,7 @@ __global__ void __launch_bounds__(kPtThreads, 1)
                     const int st = ck & 1;
                     if (st != grp) continue;
                     bool w = true;
-                    if (lane == 0) w = mbar_wait(smem_u32(&empty_bar[st]), ((uint32_t)(ck >> 1) & 1u) ^ 1u, a.err);
+                    if (lane == 0) w = mbar_wait(smem_u32(&empty_bar[st]), ((uint32_t)(ck >> 1) & 1u) ^ 1u, L.err);
                     if (__shfl_sync(0xffffffffu, w ? 1 : 0, 0) == 0) {
                         ok = false;
                         break;
@@ -404,7 +443,12 @@ __global__ void __launch_bounds__(kPtThreads, 1)
                 }
             }
         }
+        }
     }
+    if (!ok) stop_flag = 1;
+    // the unit is done in every role before unit_slot is written again
+    __syncthreads();
+    }  // units
     __syncthreads();
     if (warp == 1) {
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
@@ -421,7 +465,8 @@ __global__ void __launch_bounds__(kPtThreads, 1)
 struct PairTc {
     __nv_bfloat16 *wh = nullptr, *wl = nullptr;
     int *wrow = nullptr;
-    int *err = nullptr;  // set by the kernel when a pipeline wait times out
+    int *err = nullptr;   // set by the kernel when a pipeline wait times out
+    int *next = nullptr;  // unit counter of the launches led by this context
     int64_t rows = 0;
     int max_items = 0;
 };
@@ -467,6 +512,7 @@ void pair_tc_free(Context &c)
     cudaFree(c.pair_tc->wl);
     cudaFree(c.pair_tc->wrow);
     cudaFree(c.pair_tc->err);
+    cudaFree(c.pair_tc->next);
     delete c.pair_tc;
     c.pair_tc = nullptr;
 }
@@ -489,12 +535,14 @@ int pair_tc_build(Context &c)
     PairTc *pt = new PairTc;
     pt->rows = rows;
     cudaError_t e1 = cudaMalloc(&pt->wh, bytes), e2 = cudaMalloc(&pt->wl, bytes),
-                e3 = cudaMalloc(&pt->wrow, sizeof(int) * d.nxyz), e4 = cudaMalloc(&pt->err, sizeof(int));
-    if (e1 != cudaSuccess || e2 != cudaSuccess || e3 != cudaSuccess || e4 != cudaSuccess) {
+                e3 = cudaMalloc(&pt->wrow, sizeof(int) * d.nxyz), e4 = cudaMalloc(&pt->err, sizeof(int)),
+                e5 = cudaMalloc(&pt->next, sizeof(int));
+    if (e1 != cudaSuccess || e2 != cudaSuccess || e3 != cudaSuccess || e4 != cudaSuccess || e5 != cudaSuccess) {
         cudaFree(pt->wh);
         cudaFree(pt->wl);
         cudaFree(pt->wrow);
         cudaFree(pt->err);
+        cudaFree(pt->next);
         delete pt;
         cudaGetLastError();
         return set_error(GD_ERR_OUT_OF_MEMORY, "pair weight table allocation");
@@ -584,53 +632,126 @@ int pair_tc_take_timeout(Context &c, cudaStream_t st, bool *timed_out)
     return GD_OK;
 }
 
-int run_pair_tc(Context &c, const float *f, int ncells, int ld, float *gain, cudaStream_t st)
+namespace {
+
+// s-chunks of one grid's walk for ncells cells: about four waves of one CTA
+// per SM, within a 16 GiB partial buffer
+int pt_chunks(const Context &c, int ncells)
 {
-    if (!c.pair_tc) return set_error(GD_ERR_INVALID_ARG, "pair weight table not built");
     const Dims &d = c.d;
-    const PairTc &pt = *c.pair_tc;
     const int tiles = (ncells + PT_BM - 1) / PT_BM;
     const int cells_pad = tiles * PT_BM;
-    // chunks of s: about four waves of one CTA per SM, within the partial buffer
     const int sms = std::max(1, c.sm_count);
     int nchunks = (int)std::min<int64_t>(std::max(1, (4 * sms + tiles - 1) / tiles), d.ns);
     while (nchunks > 1 && (size_t)nchunks * d.n_pnt * cells_pad * sizeof(float) > ((size_t)16 << 30)) nchunks--;
-    const int *d_bounds = nullptr;
-    int rc = gain_bounds_device(c, nchunks, &d_bounds);
-    if (rc) return rc;
-    const size_t part_bytes = (size_t)nchunks * d.n_pnt * cells_pad * sizeof(float);
-    if ((rc = ensure_scratch(c, part_bytes))) return rc;
-    float *part = static_cast<float *>(c.scratch.ptr);
-    GD_CUDA(cudaMemsetAsync(part, 0, part_bytes, st));
+    return nchunks;
+}
 
-    CUtensorMap tWh, tWl;
-    const uint64_t dims[2] = {(uint64_t)PT_KC, (uint64_t)std::max<int64_t>(pt.rows, 16)};
-    const uint64_t strides[1] = {(uint64_t)PT_KC * 2};
-    const uint32_t box[2] = {PT_KC, 16};
-    if ((rc = encode_bf16_sw128(&tWh, pt.wh, 2, dims, strides, box))) return rc;
-    if ((rc = encode_bf16_sw128(&tWl, pt.wl, 2, dims, strides, box))) return rc;
+}  // namespace
 
-    int max_smem = 0;
-    GD_CUDA(cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, c.device));
-    const size_t cmap_bytes = ((size_t)d.nxyz * 2 + 15) & ~(size_t)15;
+// The pair-product gain with the contraction on the tensor cores for one or
+// more grids (each with its own context, cells and output) in one launch:
+// each grid's walk over s is split into work-balanced chunks, and every
+// (grid, 128-cell tile, chunk) unit writes its own partial sums, so the
+// results do not depend on how the units are spread over the CTAs and equal
+// those of separate launches bit for bit.  The units are ordered by their
+// work, largest first (within a grid chunk-major, tiles fastest, so that the
+// CTAs in flight share weight rows in L2), and pulled from a device counter
+// by one persistent CTA per SM as each finishes its previous unit.  The unit list is uploaded once per launch shape and cached on the
+// first job's context (a replayed graph reads it without a host copy); a
+// pipeline time-out is recorded on that context.  Then the chunk partials of
+// every grid are added in chunk order.
+int launch_pair_tc(const PtJob *jobs, int njobs, cudaStream_t st)
+{
+    if (njobs < 1 || njobs > kPtMaxGrids) return set_error(GD_ERR_UNSUPPORTED, "pair tensor-core launch: 1-4 grids");
+    Context &c0 = *jobs[0].c;
+    PtLaunch L{};
+    PtMaps maps{};
+    std::vector<int> chunks(njobs), cells_pad(njobs);
+    std::vector<double> unit_cost(njobs);
+    std::string key;
     size_t smem = (size_t)kPtStages * kPtStage + 1024;
-    const bool cmap_smem = smem + cmap_bytes + 512 <= (size_t)max_smem;
+    int max_smem = 0;
+    GD_CUDA(cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, c0.device));
+    for (int j = 0; j < njobs; j++) {
+        Context &c = *jobs[j].c;
+        if (!c.pair_tc) return set_error(GD_ERR_INVALID_ARG, "pair weight table not built");
+        for (int k = 0; k < j; k++)
+            if (jobs[k].c == jobs[j].c) return set_error(GD_ERR_UNSUPPORTED, "one launch serves distinct contexts");
+        const Dims &d = c.d;
+        const int tiles = (jobs[j].ncells + PT_BM - 1) / PT_BM;
+        cells_pad[j] = tiles * PT_BM;
+        chunks[j] = pt_chunks(c, jobs[j].ncells);
+        unit_cost[j] = (double)c.s_work_prefix[d.ns] / chunks[j];
+        const int *d_bounds = nullptr;
+        int rc = gain_bounds_device(c, chunks[j], &d_bounds);
+        if (rc) return rc;
+        const size_t part_bytes = (size_t)chunks[j] * d.n_pnt * cells_pad[j] * sizeof(float);
+        if ((rc = ensure_scratch(c, part_bytes))) return rc;
+        float *part = static_cast<float *>(c.scratch.ptr);
+        GD_CUDA(cudaMemsetAsync(part, 0, part_bytes, st));
+        const uint64_t dims[2] = {(uint64_t)PT_KC, (uint64_t)std::max<int64_t>(c.pair_tc->rows, 16)};
+        const uint64_t strides[1] = {(uint64_t)PT_KC * 2};
+        const uint32_t box[2] = {PT_KC, 16};
+        if ((rc = encode_bf16_sw128(&maps.wh[j], c.pair_tc->wh, 2, dims, strides, box))) return rc;
+        if ((rc = encode_bf16_sw128(&maps.wl[j], c.pair_tc->wl, 2, dims, strides, box))) return rc;
+        L.g[j] = PtGrid{d, jobs[j].f, jobs[j].ld, jobs[j].ncells, cells_pad[j], c.d_cmap, c.d_D_item_off,
+                        c.d_D_items, c.d_D_members, c.pair_tc->wrow, d_bounds, part};
+        key += std::to_string(tiles) + "x" + std::to_string(chunks[j]) + "c" +
+               std::to_string((long long)unit_cost[j]) + ";";
+    }
+    // a single grid keeps its box -> compact map in shared memory when it fits
+    const size_t cmap_bytes = ((size_t)c0.d.nxyz * 2 + 15) & ~(size_t)15;
+    const bool cmap_smem = njobs == 1 && smem + cmap_bytes + 512 <= (size_t)max_smem;
     if (cmap_smem) smem += cmap_bytes;
     if (smem > (size_t)max_smem) return set_error(GD_ERR_UNSUPPORTED, "pair tensor-core kernel: shared memory");
-    PtArgs a{d, f, ld, ncells, cells_pad, c.d_cmap, c.d_D_item_off, c.d_D_items, c.d_D_members, pt.wrow,
-             d_bounds, part, pt.err};
-    dim3 grid((unsigned)tiles, (unsigned)nchunks);
+
+    auto it = c0.pt_units_dev.find(key);
+    if (it == c0.pt_units_dev.end()) {
+        std::vector<int> order(njobs);
+        for (int j = 0; j < njobs; j++) order[j] = j;
+        std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return unit_cost[a] > unit_cost[b]; });
+        std::vector<int4> units;
+        for (int j : order)
+            for (int ch = 0; ch < chunks[j]; ch++)
+                for (int t = 0; t < cells_pad[j] / PT_BM; t++) units.push_back(make_int4(j, t, ch, 0));
+        int4 *dev = nullptr;
+        GD_CUDA(cudaMalloc(&dev, sizeof(int4) * units.size()));
+        cudaError_t e = cudaMemcpy(dev, units.data(), sizeof(int4) * units.size(), cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) {
+            cudaFree(dev);
+            return cuda_error(e, "pair tensor-core unit list");
+        }
+        it = c0.pt_units_dev.emplace(key, std::make_pair(dev, (int)units.size())).first;
+    }
+    L.units = it->second.first;
+    L.nunits = it->second.second;
+    L.err = c0.pair_tc->err;
+    L.next = c0.pair_tc->next;
+    GD_CUDA(cudaMemsetAsync(L.next, 0, sizeof(int), st));
+    const int ctas = std::min(L.nunits, std::max(1, c0.sm_count));
     if (cmap_smem) {
         GD_CUDA(cudaFuncSetAttribute(pair_tc_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        pair_tc_kernel<true><<<grid, kPtThreads, smem, st>>>(tWh, tWl, a);
+        pair_tc_kernel<true><<<ctas, kPtThreads, smem, st>>>(maps, L);
     } else {
         GD_CUDA(cudaFuncSetAttribute(pair_tc_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        pair_tc_kernel<false><<<grid, kPtThreads, smem, st>>>(tWh, tWl, a);
+        pair_tc_kernel<false><<<ctas, kPtThreads, smem, st>>>(maps, L);
     }
     GD_CUDA(cudaGetLastError());
     // the kernel records a pipeline time-out instead of hanging; the call only
     // enqueues work, and gd_ctx_check reports the record
-    return reduce_gain_partials(c, part, nchunks, cells_pad, ncells, ld, gain, st);
+    for (int j = 0; j < njobs; j++) {
+        const int rc = reduce_gain_partials(*jobs[j].c, L.g[j].part, chunks[j], cells_pad[j], jobs[j].ncells,
+                                            jobs[j].ld, jobs[j].gain, st);
+        if (rc) return rc;
+    }
+    return GD_OK;
+}
+
+int run_pair_tc(Context &c, const float *f, int ncells, int ld, float *gain, cudaStream_t st)
+{
+    const PtJob job{&c, f, ncells, ld, gain};
+    return launch_pair_tc(&job, 1, st);
 }
 
 }  // namespace gd

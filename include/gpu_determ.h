@@ -262,6 +262,16 @@ int gd_batch_destroy(gd_batch *b);
 int gd_batch_add(gd_batch *b, gd_ctx *ctx, float *f, int ncells, int ld, int mode, float param, double *m5,
                  float *time_dev, float *dt_dev);
 int gd_batch_step(gd_batch *b, int use_graph, gd_stream stream);
+/* GD_BATCH_STREAMS (default): each group's gd_step on its context's stream,
+ * as above.  GD_BATCH_FUSED_PAIR_TC: the gains of all groups (at most 4, on
+ * distinct contexts whose gain path is GD_GAIN_PAIR_TC) in one persistent
+ * launch of the pair-product kernel that walks a device list of (grid,
+ * 128-cell tile, s-chunk) units, each group's loss, projection and
+ * relaxation around it on the batch stream; results equal gd_step on each
+ * group's context bit for bit.  A pipeline time-out of the fused launch is
+ * recorded on the first group's context. */
+enum { GD_BATCH_STREAMS = 0, GD_BATCH_FUSED_PAIR_TC = 1 };
+int gd_batch_set_mode(gd_batch *b, int mode);
 int gd_batch_check(gd_batch *b);
 int gd_batch_info(const gd_batch *b, int *groups, int *streams, int *graph_nodes, int64_t *steps);
 

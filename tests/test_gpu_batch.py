@@ -93,3 +93,58 @@ def test_autotune_picks_a_measured_candidate(gdlib, cuda):
     # a budget too small for the matrices leaves only the pair kernel
     r2 = ctx.autotune(f, cells, cells, path_mask=mask, mem_budget=1e3)
     assert r2["path"] == "pair" and len(r2["candidates"]) == 3
+
+
+def test_fused_batch_one_launch_matches_single_steps(gdlib, cuda):
+    """GD_BATCH_FUSED_PAIR_TC: the gains of uneven grids (8^3, 12^3, 16^3 with
+    200-300 cells, so some grids have more than one 128-cell tile) come from
+    one persistent launch over a device list of (grid, cell tile, s-chunk)
+    units; each grid's distribution and time after a few steps, eager and
+    replayed from the graph, equal gd_step on its own context (pair products
+    with the contraction on the tensor cores) bit for bit."""
+    torch = cuda
+    from gpu_determ_gb300 import inputs
+    specs = [(8, 200, 11), (12, 300, 12), (16, 130, 13)]
+    groups = []
+    for n, cells, seed in specs:
+        spec = gdlib.GridSpec(n, R=4.8)
+        ctx = gdlib.Context(spec)
+        ctx.set_gain_path(gdlib.GAIN_PAIR_TC)
+        groups.append((ctx, inputs.shock_profile(spec.fill(), cells) if n != 12 else
+                       inputs.mixtures(spec.fill(), cells, seed=seed), cells))
+    f_ref, t_ref = _run_single(gdlib, torch, groups)
+    for use_graph in (False, True):
+        b = gdlib.Batch()
+        fs, ts = [], []
+        for ctx, f0, cells in groups:
+            f = torch.from_numpy(f0).cuda()
+            t = torch.zeros(1, dtype=torch.float32, device="cuda")
+            b.add(ctx, f, cells, cells, gdlib.DT_COURANT, 0.5, time=t)
+            fs.append(f)
+            ts.append(t)
+        b.set_mode(gdlib.BATCH_FUSED_PAIR_TC)
+        for _ in range(STEPS):
+            b.step(use_graph)
+        b.check()
+        info = b.info()
+        b.close()
+        torch.cuda.synchronize()
+        for a, f in zip(f_ref, fs):
+            assert np.array_equal(a, f.cpu().numpy())
+        assert t_ref == [float(t.item()) for t in ts]
+        if use_graph:
+            assert info["graph_nodes"] > 0
+
+
+def test_fused_batch_rejects_other_gain_paths(gdlib, cuda):
+    torch = cuda
+    from gpu_determ_gb300 import inputs
+    spec = gdlib.GridSpec(8, R=4.8)
+    ctx = gdlib.Context(spec)
+    f = torch.from_numpy(inputs.mixtures(spec.fill(), 32, seed=1)).cuda()
+    b = gdlib.Batch()
+    b.add(ctx, f, 32, 32, gdlib.DT_COURANT, 0.5)
+    with pytest.raises(gdlib.GDError) as e:
+        b.set_mode(gdlib.BATCH_FUSED_PAIR_TC)     # the context is on the FP32 pair kernel
+    assert e.value.code == 4
+    b.close()

@@ -155,12 +155,15 @@ def test_headline_grid_against_pair_kernel(cuda, gdlib):
 def test_c2_batch_against_fp64_oracle(cuda, gdlib):
     """Config C2 (16^3, R = 4.8): seeded mixtures of 1-3 Maxwellians with
     n ~ lognormal(0, 0.3), u ~ N(0, 0.7^2) per axis, T ~ U[0.6, 1.8]; the gain
-    and the FP64-projected Q of every gain path against the FP64 oracle.
-    GD_C2_CELLS sets the batch (the config's 1024; 256 by default so the
-    oracle's CPU time stays short)."""
+    and the FP64-projected Q of every gain path against the FP64 oracle, on
+    the config's batch of 1024 (GD_C2_CELLS overrides it).  The paths with
+    FP32-equivalent arithmetic (FP32 pair kernel, pair products on tensor
+    cores, BF16x3 collision matrices with the tensor-core loss) also keep
+    every cell's projected Q within the metric's relative L2 of 1e-3; one-pass
+    BF16 does not (its per-cell tail is reported, not asserted)."""
     import os
     torch = cuda
-    nc = int(os.environ.get("GD_C2_CELLS", "256"))
+    nc = int(os.environ.get("GD_C2_CELLS", "1024"))
     spec = gdlib.GridSpec(16, R=4.8)
     ctx = gdlib.Context(spec)
     f = inputs.mixtures(spec.fill(), nc, seed=2024)
@@ -184,6 +187,9 @@ def test_c2_batch_against_fp64_oracle(cuda, gdlib):
         rel_i = np.linalg.norm(g - i_ref) / np.linalg.norm(i_ref)
         rel_q = np.linalg.norm(qq - q_ref) / np.linalg.norm(q_ref)
         cell_q = np.linalg.norm(qq - q_ref, axis=0) / np.linalg.norm(q_ref, axis=0)
-        report[path] = (rel_i, rel_q, float(np.median(cell_q)), float(np.quantile(cell_q, 0.99)))
+        report[path] = (rel_i, rel_q, float(np.median(cell_q)), float(np.quantile(cell_q, 0.99)),
+                        float(cell_q.max()))
         assert rel_i <= tol_i and rel_q <= tol_q, (path, report[path])
-    print("C2 16^3,", nc, "cells: path -> (gain rel-L2, Q rel-L2, Q per-cell median, p99) vs FP64:", report)
+        if path != gdlib.GAIN_CMATRIX_BF16:
+            assert cell_q.max() <= 1e-3, (path, report[path])
+    print("C2 16^3,", nc, "cells: path -> (gain rel-L2, Q rel-L2, Q per-cell median, p99, max) vs FP64:", report)
