@@ -76,10 +76,15 @@ __device__ __forceinline__ int stage_len(const uint32_t *tiles, int j, int cnt, 
 // The tensor cores' FP32 accumulation loses precision over long sums (the
 // collision-matrix gain against FP64 at 20^3: median relative error 2.5e-6
 // with whole b-tile runs of ~25 tiles per accumulation, 6.4e-7 with at most
-// four): by default at most four 64-column tiles (256 products per entry) go
-// into one accumulation, the epilogue adding the runs in FP32 with
-// compensation.  Cost: 2 % of the gain launch.
-constexpr int kDefaultChain = 4;
+// four): in BF16x3 mode by default at most four 64-column tiles (256
+// products per entry) go into one accumulation, the epilogue adding the runs
+// in FP32 with compensation (2 % of the gain launch).  One BF16 pass is
+// limited by the rounding of its operands (~3e-4), not by the accumulation,
+// so it keeps whole b-tile runs (unlimited chain).  The tensor-core loss
+// always sums K in chunks of kLossChunk columns per launch.
+constexpr int kDefaultChainBf16x3 = 4;
+constexpr int kChainUnlimited = 1 << 30;
+constexpr int kLossChunk = 256;
 
 struct CmParams {
     int ns;       // in-sphere nodes
@@ -553,7 +558,7 @@ struct gd_cmatrix {
     int stall_next = 0;  // gd_ctx_inject_timeout: polls for the next tensor-core loss GEMM
     // stored tiles per tensor-memory accumulation of the gain, and 64-column K
     // chunks per launch of the tensor-core loss (gd_cmatrix_set_chain)
-    int chain = gd::kDefaultChain;
+    int chain = gd::kChainUnlimited;
 };
 
 namespace gd {
@@ -574,6 +579,7 @@ extern "C" int gd_cmatrix_create(gd_ctx *ctx, int mode, gd_cmatrix **out)
     gd_cmatrix *h = new gd_cmatrix();
     h->ctx = ctx;
     h->mode = mode;
+    h->chain = mode == GD_CMATRIX_BF16X3 ? kDefaultChainBf16x3 : kChainUnlimited;
     h->ns = d.n_pnt;
     h->ns_k = (d.n_pnt + BK - 1) / BK * BK;
     const int num_n = (h->ns + BN - 1) / BN, num_k = h->ns_k / BK;
@@ -699,7 +705,7 @@ extern "C" int gd_cmatrix_set_chain(gd_cmatrix *h, int tiles)
 {
     if (!h) return gd::set_error(GD_ERR_INVALID_ARG, "NULL argument");
     if (tiles < 0 || (tiles & 1)) return gd::set_error(GD_ERR_INVALID_ARG, "chain must be 0 or a positive even count");
-    h->chain = tiles == 0 ? (1 << 30) : tiles;
+    h->chain = tiles == 0 ? gd::kChainUnlimited : tiles;
     return GD_OK;
 }
 
@@ -851,9 +857,9 @@ int cmatrix_loss(gd_cmatrix *h, const float *f, int ncells, int ld, float *nu, c
     GD_CUDA(cudaGetLastError());
     const int stall = h->stall_next;  // a pending time-out injection fires here, once
     h->stall_next = 0;
-    // the same bound on the products per tensor-core FP32 accumulation as the
-    // gain: chain x 64 columns of K per launch, chunks added in FP32
-    const int kc = h->chain < (1 << 30) ? h->chain * BK : 0;
+    // at most kLossChunk products per tensor-core FP32 accumulation: one
+    // launch per K chunk, the chunks added in FP32
+    const int kc = kLossChunk;
     if ((rc = gemm_bf16_nt_f32(h->bh, h->ns, h->fh, ncells, h->ns_k, nu, ld, false, h->err, st, stall, kc))) return rc;
     if ((rc = gemm_bf16_nt_f32(h->bh, h->ns, h->fl, ncells, h->ns_k, nu, ld, true, h->err, st, 0, kc))) return rc;
     return gemm_bf16_nt_f32(h->bl, h->ns, h->fh, ncells, h->ns_k, nu, ld, true, h->err, st, 0, kc);

@@ -287,7 +287,12 @@ __global__ void __launch_bounds__(kPtThreads, 1)
         const int16_t *cmap = CMAP_SMEM ? cmap_s : a.cmap;
         const int cell = m_tile * PT_BM + row;
         const bool live = cell < a.ncells;
-        float *part = a.part + (size_t)chunk * d.n_pnt * a.cells_pad + cell;
+        // the unit's fields used in the scatter loop, held in registers (the
+        // reductions' memory clobber would otherwise reload them each time)
+        const int cells_pad = a.cells_pad, nyz = d.nyz, nz = d.nz;
+        const int4 *D_items = a.D_items;
+        const uint32_t *D_members = a.D_members;
+        float *part = a.part + (size_t)chunk * d.n_pnt * cells_pad + cell;
         for (int sl = s_begin; ok && sl < s_end; sl++) {
             const int np = npass_of(a, sl);
             for (int q = 0; ok && q < np; q++, uc++) {
@@ -311,7 +316,7 @@ __global__ void __launch_bounds__(kPtThreads, 1)
                     if (!live) continue;
                     const int mend = min(16, u.mcnt - m0);
                     for (int t = 0; t < mend; t++) {
-                        const int4 item = __ldg(a.D_items + u.it0 + m0 + t);
+                        const int4 item = __ldg(D_items + u.it0 + m0 + t);
                         const float acc = v[t];
                         // fire-and-forget reductions: within one s every target
                         // receives one update, and the units of one cell are
@@ -320,11 +325,11 @@ __global__ void __launch_bounds__(kPtThreads, 1)
                         // like the tensor-core products, the reduction flushes
                         // subnormal contributions to zero
                         for (int mm = item.y; mm < item.z; mm++) {
-                            const uint32_t pk = __ldg(a.D_members + mm);
+                            const uint32_t pk = __ldg(D_members + mm);
                             const int gx = 2 * (int)(pk & 31) + u.px, gy = 2 * (int)((pk >> 6) & 31) + u.py,
                                       gz = 2 * (int)((pk >> 12) & 31) + u.pz;
-                            const int X0 = ((u.sx - gx) >> 1) * d.nyz, X1 = X0 + gx * d.nyz;
-                            const int Y0 = ((u.sy - gy) >> 1) * d.nz, Y1 = Y0 + gy * d.nz;
+                            const int X0 = ((u.sx - gx) >> 1) * nyz, X1 = X0 + gx * nyz;
+                            const int Y0 = ((u.sy - gy) >> 1) * nz, Y1 = Y0 + gy * nz;
                             const int Z0 = (u.sz - gz) >> 1, Z1 = Z0 + gz;
 #pragma unroll
                             for (int sg = 0; sg < 8; sg++) {
@@ -332,7 +337,7 @@ __global__ void __launch_bounds__(kPtThreads, 1)
                                 const bool dup = (hx && gx == 0) || (hy && gy == 0) || (hz && gz == 0);
                                 const int tg = dup ? -1 : cmap[(hx ? X1 : X0) + (hy ? Y1 : Y0) + (hz ? Z1 : Z0)];
                                 if (tg >= 0)
-                                    asm volatile("red.relaxed.gpu.global.add.f32 [%0], %1;" ::"l"(part + (size_t)tg * a.cells_pad),
+                                    asm volatile("red.relaxed.gpu.global.add.f32 [%0], %1;" ::"l"(part + (size_t)tg * cells_pad),
                                                  "f"(acc)
                                                  : "memory");
                             }
@@ -357,6 +362,7 @@ __global__ void __launch_bounds__(kPtThreads, 1)
         const int cell = m_tile * PT_BM + row;
         const bool live = cell < a.ncells;
         const float *fcol = a.f + (live ? cell : 0);
+        const int ldf = a.ld, nyz = d.nyz, nz = d.nz;  // in registers for the gather loop
         for (int sl = s_begin; ok && sl < s_end; sl++) {
             const int np = npass_of(a, sl);
             for (int q = 0; ok && q < np; q++) {
@@ -380,8 +386,8 @@ __global__ void __launch_bounds__(kPtThreads, 1)
                     int A = 0, B = 0, Cc = 0, Dd = 0;
                     auto set_run = [&]() {
                         const int nxv = 2 * x2 + u.px, nyv = 2 * y2 + u.py;
-                        const int X0 = ((u.sx + nxv) >> 1) * d.nyz, X1 = ((u.sx - nxv) >> 1) * d.nyz;
-                        const int Y0 = ((u.sy + nyv) >> 1) * d.nz, Y1 = ((u.sy - nyv) >> 1) * d.nz;
+                        const int X0 = ((u.sx + nxv) >> 1) * nyz, X1 = ((u.sx - nxv) >> 1) * nyz;
+                        const int Y0 = ((u.sy + nyv) >> 1) * nz, Y1 = ((u.sy - nyv) >> 1) * nz;
                         A = X0 + Y0;
                         B = X1 + Y1;
                         Cc = X0 + Y1;
@@ -399,7 +405,7 @@ __global__ void __launch_bounds__(kPtThreads, 1)
                                 const int lz = zc0 + z2, l1z = zc1 - z2;
                                 const int k0 = cmap[A + lz], k1 = cmap[B + l1z], k2 = cmap[Cc + l1z], k3 = cmap[Dd + lz];
                                 const int k4 = cmap[A + l1z], k5 = cmap[B + lz], k6 = cmap[Cc + lz], k7 = cmap[Dd + l1z];
-#define GD_F(kk) (((kk) >= 0 && live) ? __ldg(fcol + (size_t)(kk) * a.ld) : 0.f)
+#define GD_F(kk) (((kk) >= 0 && live) ? __ldg(fcol + (size_t)(kk) * ldf) : 0.f)
                                 const float f0 = GD_F(k0), f1 = GD_F(k1), f2 = GD_F(k2), f3 = GD_F(k3);
                                 const float f4 = GD_F(k4), f5 = GD_F(k5), f6 = GD_F(k6), f7 = GD_F(k7);
 #undef GD_F

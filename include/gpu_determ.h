@@ -191,13 +191,14 @@ int gd_cmatrix_destroy(gd_cmatrix *cm);
  * of every collision-matrix tile; a call with at most 128 cells runs one CTA
  * per MMA.  Results are bitwise the same either way. */
 int gd_cmatrix_set_cluster(gd_cmatrix *cm, int ctas);
-/* Longest run of stored tiles (an even count; 0 = unlimited; default 4)
- * summed into one tensor-memory accumulator before the epilogue folds it
- * into the FP32 gain (compensated), and the K chunk (tiles x 64 columns) of
- * each launch of the tensor-core loss, whose FP32 results are added in
- * order.  The tensor cores' FP32 accumulation loses precision over long
- * sums: at 20^3 the BF16x3 gain is 6.4e-7 from FP64 (median over cells) with
- * 4 tiles, 2.5e-6 unlimited; the loss carries a -1.2e-5 bias unchunked. */
+/* Longest run of stored tiles (an even count; 0 = unlimited) summed into
+ * one tensor-memory accumulator before the epilogue folds it into the FP32
+ * gain (compensated).  The tensor cores' FP32 accumulation loses precision
+ * over long sums: at 20^3 the BF16x3 gain is 6.4e-7 from FP64 (median over
+ * cells) with 4 tiles, 2.5e-6 unlimited.  Default: 4 in BF16x3 mode,
+ * unlimited for one BF16 pass (whose error is the operands' rounding).  The
+ * tensor-core loss always sums K in 256-column chunks, added in FP32 (one
+ * chain over K carried a -1.2e-5 bias). */
 int gd_cmatrix_set_chain(gd_cmatrix *cm, int tiles);
 /* gd_cmatrix_gain only enqueues work on the stream.  Its kernels record a
  * pipeline time-out (a bounded wait that ran out) instead of hanging;
