@@ -569,11 +569,14 @@ def gain_roofline(name, ctx, f0, nc, stream, flush, peak, reps):
         work = "7 FLOP per pair product + 2 per nonzero-weight term + 1 per scatter update"
         bound, pk, src = "fp32", peak["fp32"], peak["fma_source"]
     else:
-        # stored tiles: the nonzero 256 x 64 tiles of each G_i's block upper triangle
-        tiles = ctx._info()["cmatrix_tiles"]
-        flop = 2.0 * ((nc + 127) // 128 * 128) * 256 * 64 * tiles * (3 if name == "bf16x3" else 1)
+        # stored tiles: the nonzero 256 x 64 tiles of each G_i's block upper
+        # triangle; issued: their 256 x 16 slices with a nonzero entry (one MMA
+        # K step each; the all-zero slices are skipped)
+        inf = ctx._info()
+        tiles, slices = inf["cmatrix_tiles"], inf["cmatrix_slices"]
+        flop = 2.0 * ((nc + 127) // 128 * 128) * 256 * 16 * slices * (3 if name == "bf16x3" else 1)
         kernel, work = "cmatrix_gain_kernel (tcgen05)", \
-            "MACs x 2 of the 128x256x64 tiles issued (nonzero tiles of the block upper triangle of each symmetric G_i; x3 for bf16x3)"
+            "MACs x 2 of the 128x256x16 MMA K steps issued (nonzero slices of the stored tiles of the block upper triangle of each symmetric G_i; x3 for bf16x3)"
         bound, pk, src = "tensor", peak["bf16"], peak["bf16_source"]
         # DRAM bytes per launch: the collision matrices stream through once.  An
         # ncu capture of the same kernel (CTA pairs, one pass) on 14^3 / 4096

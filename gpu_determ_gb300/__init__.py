@@ -61,7 +61,8 @@ class _Info(C.Structure):
                 ("du", C.c_float), ("dv", C.c_float), ("dw", C.c_float), ("d3v", C.c_float),
                 ("nonzero_weights", C.c_int64), ("table_a_elems", C.c_int64),
                 ("pair_products", C.c_int64), ("contraction_terms", C.c_int64),
-                ("scatter_terms", C.c_int64), ("cmatrix_tiles", C.c_int64)]
+                ("scatter_terms", C.c_int64), ("cmatrix_tiles", C.c_int64),
+                ("cmatrix_slices", C.c_int64)]
 
 
 class _PairSizes(C.Structure):

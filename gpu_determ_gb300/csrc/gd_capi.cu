@@ -496,6 +496,7 @@ int gd_ctx_info(const gd_ctx *ctx, gd_info *out)
     out->contraction_terms = ctx->c.contraction_terms;
     out->scatter_terms = ctx->c.scatter_terms;
     out->cmatrix_tiles = gd::cmatrix_stored_tiles(ctx->c.cmatrix);
+    out->cmatrix_slices = gd::cmatrix_issued_slices(ctx->c.cmatrix);
     return GD_OK;
 }
 

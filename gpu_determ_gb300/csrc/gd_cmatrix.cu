@@ -40,6 +40,7 @@ namespace {
 constexpr int BM = 128;  // cells per tile (MMA M, TMEM lanes)
 constexpr int BN = 256;  // b per accumulator tile (MMA N, TMEM columns)
 constexpr int BK = 64;   // a per stage (128 bytes of BF16: one swizzle row)
+constexpr int kSlices = BK / 16;  // MMA K steps per tile, skipped one by one when all zero
 constexpr int kEpiWarps = 8;  // two per TMEM lane quadrant, 128 accumulator columns each
 constexpr int kThreads = 64 + 32 * kEpiWarps;
 constexpr uint32_t kTileA = BM * BK * 2;  // 16 KB
@@ -67,10 +68,18 @@ __host__ __device__ constexpr int cm_stages(int npass, int cl) { return (int)((1
 
 // Stored tiles in the stage that starts at list entry j of a node's cnt
 // tiles: two when allowed and entry j + 1 belongs to the same b-tile group.
+// A stored tile's list entry: mask << 28 | n << 16 | k, with n its 256-row
+// b-tile, k its 64-column a-tile and bit kk of mask set when columns
+// 16 kk .. 16 kk + 15 hold a nonzero entry (the MMAs of all-zero 16-column
+// slices are skipped).
+__device__ __forceinline__ uint32_t tile_n(uint32_t e) { return (e >> 16) & 0xfffu; }
+__device__ __forceinline__ uint32_t tile_k(uint32_t e) { return e & 0xffffu; }
+__device__ __forceinline__ uint32_t tile_mask(uint32_t e) { return e >> 28; }
+
 __device__ __forceinline__ int stage_len(const uint32_t *tiles, int j, int cnt, int tps)
 {
     if (tps == 1 || j + 1 >= cnt) return 1;
-    return (__ldg(tiles + j) >> 16) == (__ldg(tiles + j + 1) >> 16) ? 2 : 1;
+    return tile_n(__ldg(tiles + j)) == tile_n(__ldg(tiles + j + 1)) ? 2 : 1;
 }
 
 // The tensor cores' FP32 accumulation loses precision over long sums (the
@@ -90,7 +99,8 @@ struct CmParams {
     int ns;       // in-sphere nodes
     int ns_k;     // padded node count (multiple of BK)
     int ncells, ld;
-    const float *f;  // [ns][ld] FP32 distribution (epilogue)
+    const float *f;  // [ns_k][ldf] FP32 distribution in matrix order (epilogue)
+    int ldf;
     float *gain;     // [ns][ld]
     int *err;        // set to 1 when a wait times out
     const int *node_off;     // [ns + 1] each node's range of stored tiles
@@ -199,7 +209,7 @@ __global__ void __launch_bounds__(kThreads, 1)
                 for (int t = 0; t < len; t++) {
                     // F: this CTA's cells; G: stored tile l0 + j + t ([slot][BN rows][BK]),
                     // this CTA's BN / CL rows of it
-                    const int k = (int)(__ldg(tl + j + t) & 0xffffu);
+                    const int k = (int)tile_k(__ldg(tl + j + t));
                     unsigned char *ts = st + (size_t)t * kTileSlot;
                     tma_load_2d(smem_u32(ts), &tmFh, k * BK, m_tile * BM, fb);
                     tma_load_3d(smem_u32(ts + kTileA), &tmGh, 0, (int)crank * (BN / CL), l0 + j + t, fb);
@@ -242,7 +252,7 @@ __global__ void __launch_bounds__(kThreads, 1)
             int it = 0, grp = 0;  // stage counter; groups of tiles sharing one b-tile n
             int j = 0;
             while (ok && j < cnt) {
-                const uint32_t n = __ldg(p.tiles + l0 + j) >> 16;
+                const uint32_t n = tile_n(__ldg(p.tiles + l0 + j));
                 const int buf = grp & 1;
                 const uint32_t use = (uint32_t)(grp >> 1);
                 if (!mbar_wait(smem_u32(&acce_bar[buf]), (use & 1u) ^ 1u, p.err)) {
@@ -253,23 +263,30 @@ __global__ void __launch_bounds__(kThreads, 1)
                 const uint32_t d_tmem = tmem + (uint32_t)(buf * BN);
                 bool first = true;
                 const int jg = j;  // an accumulation: tiles of one b-tile, at most p.chain of them
-                while (j < cnt && (__ldg(p.tiles + l0 + j) >> 16) == n && j - jg < p.chain) {
+                while (j < cnt && tile_n(__ldg(p.tiles + l0 + j)) == n && j - jg < p.chain) {
                     const int s = it % S;
                     const uint32_t ph = (uint32_t)(it / S) & 1u;
+                    // the stage's tile entries, read before the wait so that
+                    // their latency hides behind it
+                    const int len = stage_len(p.tiles + l0, j, cnt, TPS);
+                    const uint32_t masks = tile_mask(__ldg(p.tiles + l0 + j)) |
+                                           (len > 1 ? tile_mask(__ldg(p.tiles + l0 + j + 1)) << 4 : 0u);
                     if (!mbar_wait(smem_u32(&full_bar[s]), ph, p.err)) {
                         ok = false;
                         break;
                     }
                     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-                    const int len = stage_len(p.tiles + l0, j, cnt, TPS);
                     for (int t = 0; t < len; t++) {
                         const uint32_t ts = smem_u32(base + (size_t)s * kStage + (size_t)t * kTileSlot);
                         const uint32_t aH = ts, bH = ts + kTileA;
                         const uint32_t aL = ts + kTileA + kTileBc, bL = ts + 2 * kTileA + kTileBc;
+                        const uint32_t mask = (masks >> (4 * t)) & 0xfu;
 #pragma unroll
                         for (int kk = 0; kk < BK / 16; kk++) {
+                            if (!((mask >> kk) & 1u)) continue;  // an all-zero slice of G
                             const uint32_t off = (uint32_t)kk * 32u;  // 16 BF16 along K
-                            const uint32_t acc = (!first || kk > 0) ? 1u : 0u;
+                            const uint32_t acc = first ? 0u : 1u;
+                            first = false;
                             if (PAIR) {
                                 umma_bf16_pair(d_tmem, umma_desc(aH + off), umma_desc(bH + off), kIdescT, acc);
                                 if (NPASS == 3) {
@@ -284,7 +301,6 @@ __global__ void __launch_bounds__(kThreads, 1)
                                 }
                             }
                         }
-                        first = false;
                     }
                     // the stage is free in both CTAs once these MMAs have read it
                     if (PAIR)
@@ -327,17 +343,17 @@ __global__ void __launch_bounds__(kThreads, 1)
         float fv[BN / 2];
         auto load_f = [&](int b0) {
 #pragma unroll
-            for (int q = 0; q < BN / 2; q++) fv[q] = __ldg(fcell + (size_t)min(b0 + q, p.ns - 1) * p.ld);
+            for (int q = 0; q < BN / 2; q++) fv[q] = __ldg(fcell + (size_t)min(b0 + q, p.ns - 1) * p.ldf);
         };
         int j = 0;
-        int n = cnt > 0 ? (int)(__ldg(p.tiles + l0) >> 16) : 0;
+        int n = cnt > 0 ? (int)tile_n(__ldg(p.tiles + l0)) : 0;
         if (live && cnt > 0) load_f(n * BN + half * (BN / 2));
         for (; j < cnt; grp++) {
             // b-tiles without stored tiles contribute nothing and are skipped;
             // a b-tile's run of tiles comes in accumulations of at most p.chain
             const int jg = j;
-            while (j < cnt && (int)(__ldg(p.tiles + l0 + j) >> 16) == n && j - jg < p.chain) j++;
-            const int n_next = j < cnt ? (int)(__ldg(p.tiles + l0 + j) >> 16) : -1;
+            while (j < cnt && (int)tile_n(__ldg(p.tiles + l0 + j)) == n && j - jg < p.chain) j++;
+            const int n_next = j < cnt ? (int)tile_n(__ldg(p.tiles + l0 + j)) : -1;
             const int buf = grp & 1;
             const uint32_t use = (uint32_t)(grp >> 1);
             bool ok = true;
@@ -404,12 +420,13 @@ __global__ void __launch_bounds__(kThreads, 1)
 // Two passes: with nz set, only mark the triangle tiles holding a nonzero
 // entry (every writer stores 1); otherwise write each entry into the stored
 // slot slot_of[i * tiles + t] of its tile (tiles that are all zero have no slot).
-__global__ void assemble_g_kernel(Dims d, int tiles, const int2 *__restrict__ tile_nk,
-                                  const uint32_t *__restrict__ nodes, const float *__restrict__ w_dense,
+__global__ void assemble_g_kernel(Dims d, int nout, int tiles, const int2 *__restrict__ tile_nk,
+                                  const uint32_t *__restrict__ nodes, const uint32_t *__restrict__ mnodes,
+                                  const float *__restrict__ w_dense,
                                   uint8_t *__restrict__ nz, const int *__restrict__ slot_of,
                                   __nv_bfloat16 *__restrict__ gh, __nv_bfloat16 *__restrict__ gl)
 {
-    const int64_t rows = (int64_t)d.n_pnt * tiles * BN;  // (i, t, b) rows of BK entries
+    const int64_t rows = (int64_t)nout * tiles * BN;  // (i, t, b) rows of BK entries, i < nout
     constexpr int vec = BK / 8;
     for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < rows * vec;
          q += (int64_t)gridDim.x * blockDim.x) {
@@ -426,14 +443,14 @@ __global__ void assemble_g_kernel(Dims d, int tiles, const int2 *__restrict__ ti
         const uint32_t qi = nodes[i];
         const int ix = qi & 1023, iy = (qi >> 10) & 1023, iz = qi >> 20;
         const bool bin = b < d.n_pnt;
-        const uint32_t qb = bin ? nodes[b] : 0u;
+        const uint32_t qb = bin ? mnodes[b] : 0u;
         const int bx = qb & 1023, by = (qb >> 10) & 1023, bz = qb >> 20;
 #pragma unroll
         for (int j = 0; j < 8; j++) {
             const int a = a0 + j;
             float v = 0.f;
             if (bin && a < d.n_pnt && a <= b) {
-                const uint32_t qa = nodes[a];
+                const uint32_t qa = mnodes[a];
                 const int ax = qa & 1023, ay = (qa >> 10) & 1023, az = qa >> 20;
                 const int sx = ax + bx, sy = ay + by, sz = az + bz;
                 const int jx = sx - ix, jy = sy - iy, jz = sz - iz;  // partner i1
@@ -451,11 +468,11 @@ __global__ void assemble_g_kernel(Dims d, int tiles, const int2 *__restrict__ ti
             hv[j] = __float2bfloat16_rn(v);
             lv[j] = __float2bfloat16_rn(v - __bfloat162float(hv[j]));
         }
-        if (nz) {
+        if (nz) {  // one byte per 16-column slice of the tile
             bool any = false;
 #pragma unroll
             for (int j = 0; j < 8; j++) any |= __bfloat162float(hv[j]) != 0.f;
-            if (any) nz[it] = 1;
+            if (any) nz[it * (BK / 16) + (int)(q % vec) / 2] = 1;
             continue;
         }
         const size_t o = ((size_t)slot * BN + rr) * BK + (size_t)(q % vec) * 8;
@@ -466,7 +483,8 @@ __global__ void assemble_g_kernel(Dims d, int tiles, const int2 *__restrict__ ti
 
 // Loss matrix B[i][j] = b(|i - j|) (hi/lo BF16, j padded to ns_k with zeros),
 // so that nu = B f is a GEMM: nu[i][c] = sum_j B[i][j] f[j][c].
-__global__ void assemble_b_kernel(Dims d, int ns_k, const uint32_t *__restrict__ nodes, const float *__restrict__ b,
+__global__ void assemble_b_kernel(Dims d, int ns_k, const uint32_t *__restrict__ nodes,
+                                  const uint32_t *__restrict__ mnodes, const float *__restrict__ b,
                                   __nv_bfloat16 *__restrict__ bh, __nv_bfloat16 *__restrict__ bl)
 {
     const int64_t total = (int64_t)d.n_pnt * ns_k;
@@ -474,7 +492,7 @@ __global__ void assemble_b_kernel(Dims d, int ns_k, const uint32_t *__restrict__
         const int i = (int)(q / ns_k), j = (int)(q % ns_k);
         float v = 0.f;
         if (j < d.n_pnt) {
-            const uint32_t pi = nodes[i], pj = nodes[j];
+            const uint32_t pi = nodes[i], pj = mnodes[j];
             const int dx = abs((int)(pi & 1023) - (int)(pj & 1023));
             const int dy = abs((int)((pi >> 10) & 1023) - (int)((pj >> 10) & 1023));
             const int dz = abs((int)(pi >> 20) - (int)(pj >> 20));
@@ -486,15 +504,20 @@ __global__ void assemble_b_kernel(Dims d, int ns_k, const uint32_t *__restrict__
     }
 }
 
-// F[c][a] (BF16 hi/lo, a contiguous, padded to ns_k) from f[a][c] (FP32).
+// F[c][a] (BF16 hi/lo, a contiguous, padded to ns_k) from f (FP32, [node][c])
+// in matrix order: column a holds node inv[a].  With fp set, also the FP32
+// rows in matrix order, fp[a][c] (leading dimension ldf), for the epilogue.
 __global__ void convert_f_kernel(const float *__restrict__ f, int ns, int ns_k, int ncells, int ld,
-                                 __nv_bfloat16 *__restrict__ fh, __nv_bfloat16 *__restrict__ fl)
+                                 const int *__restrict__ inv, __nv_bfloat16 *__restrict__ fh,
+                                 __nv_bfloat16 *__restrict__ fl, float *__restrict__ fp, int ldf)
 {
     __shared__ float tile[32][33];
     const int a0 = blockIdx.x * 32, c0 = blockIdx.y * 32;
     for (int r = threadIdx.y; r < 32; r += blockDim.y) {
         const int a = a0 + r, c = c0 + threadIdx.x;
-        tile[r][threadIdx.x] = (a < ns && c < ncells) ? f[(size_t)a * ld + c] : 0.f;
+        const float v = (a < ns && c < ncells) ? f[(size_t)__ldg(inv + a) * ld + c] : 0.f;
+        tile[r][threadIdx.x] = v;
+        if (fp && a < ns_k && c < ncells) fp[(size_t)a * ldf + c] = v;
     }
     __syncthreads();
     for (int r = threadIdx.y; r < 32; r += blockDim.y) {
@@ -548,11 +571,19 @@ struct gd_cmatrix {
     int tiles = 0;       // BN x BK tiles of one node's block upper triangle
     int cluster = 2;     // CTAs per MMA: 2 (CTA-pair MMA, M = 256 cells; the default) or 1
     int64_t slots = 0;   // stored (not all-zero) tiles over all nodes
+    int64_t slices = 0;  // their 16-column slices with a nonzero entry (MMA K steps issued)
     int *node_off = nullptr;    // [ns + 1] into list
     uint32_t *list = nullptr;   // stored tiles per node, n << 16 | k
     __nv_bfloat16 *gh = nullptr, *gl = nullptr;
-    __nv_bfloat16 *fh = nullptr, *fl = nullptr;  // f as [cell][node] BF16 hi / lo
+    __nv_bfloat16 *fh = nullptr, *fl = nullptr;  // f as [cell][matrix index] BF16 hi / lo
+    float *fp = nullptr;                         // f as [matrix index][cell] FP32 (epilogue)
     int f_cells = 0;
+    // matrix order of the nodes: a 3-D Hilbert curve over the lattice, which
+    // packs the nonzero entries of the G_i into fewer 256 x 64 tiles than
+    // the compact (i, j, k) order; inv[m] is the node at matrix index m,
+    // mnodes[m] its packed lattice coordinates
+    int *inv = nullptr;
+    uint32_t *mnodes = nullptr;
     __nv_bfloat16 *bh = nullptr, *bl = nullptr;  // loss matrix [node][ns_k] BF16 hi / lo
     int *err = nullptr;
     int stall_next = 0;  // gd_ctx_inject_timeout: polls for the next tensor-core loss GEMM
@@ -563,6 +594,68 @@ struct gd_cmatrix {
 
 namespace gd {
 int ensure_f(gd_cmatrix *h, int ncells);
+
+// Index of (x, y, z) along a 3-D Hilbert curve through the 2^bits cube
+// (Skilling's transpose algorithm: "Programming the Hilbert curve", AIP Conf.
+// Proc. 707, 2004).
+uint64_t hilbert_index(uint32_t x, uint32_t y, uint32_t z, int bits)
+{
+    uint32_t X[3] = {x, y, z};
+    const uint32_t M = 1u << (bits - 1);
+    for (uint32_t Q = M; Q > 1; Q >>= 1) {  // inverse undo excess work
+        const uint32_t P = Q - 1;
+        for (int i = 0; i < 3; i++) {
+            if (X[i] & Q) {
+                X[0] ^= P;
+            } else {
+                const uint32_t t = (X[0] ^ X[i]) & P;
+                X[0] ^= t;
+                X[i] ^= t;
+            }
+        }
+    }
+    for (int i = 1; i < 3; i++) X[i] ^= X[i - 1];  // Gray encode
+    uint32_t t = 0;
+    for (uint32_t Q = M; Q > 1; Q >>= 1)
+        if (X[2] & Q) t ^= Q - 1;
+    for (int i = 0; i < 3; i++) X[i] ^= t;
+    uint64_t h = 0;  // interleave the transposed bits, most significant first
+    for (int b = bits - 1; b >= 0; b--)
+        for (int i = 0; i < 3; i++) h = (h << 1) | ((X[i] >> b) & 1u);
+    return h;
+}
+
+// Side of the smallest power-of-two cube holding the lattice, as bits.
+int hilbert_bits(const Dims &d)
+{
+    int bits = 1;
+    while ((1 << bits) < std::max(d.nx, std::max(d.ny, d.nz))) bits++;
+    return bits;
+}
+
+// The nodes' matrix order: sorted by their index along a Hilbert curve
+// through the 2^bits cube, the lattice placed at (off, off, off) inside it.
+// A run of consecutive matrix indices is then a compact block of nodes,
+// which packs the orthogonality shells of each G_i ((a - i) . (b - i) near 0)
+// into fewer 256 x 64 tiles than the compact (i, j, k) order (20^3, R = 4.8:
+// 335-349 stored tiles per node, by offset, instead of 381).
+void matrix_order(const Context &c, int off, std::vector<int> &inv, std::vector<uint32_t> &mnodes)
+{
+    const int ns = c.d.n_pnt;
+    const int bits = hilbert_bits(c.d);
+    std::vector<std::pair<uint64_t, int>> key(ns);
+    for (int m = 0; m < ns; m++)
+        key[m] = {hilbert_index((uint32_t)(c.ui[m] + off), (uint32_t)(c.vi[m] + off), (uint32_t)(c.wi[m] + off), bits),
+                  m};
+    std::sort(key.begin(), key.end());
+    inv.resize(ns);
+    mnodes.resize(ns);
+    for (int m = 0; m < ns; m++) {
+        const int node = key[m].second;
+        inv[m] = node;
+        mnodes[m] = (uint32_t)c.ui[node] | ((uint32_t)c.vi[node] << 10) | ((uint32_t)c.wi[node] << 20);
+    }
+}
 }
 
 extern "C" int gd_cmatrix_create(gd_ctx *ctx, int mode, gd_cmatrix **out)
@@ -596,21 +689,73 @@ extern "C" int gd_cmatrix_create(gd_ctx *ctx, int mode, gd_cmatrix **out)
     const int64_t work = (int64_t)ntri * BN * (BK / 8);
     const int blocks = (int)std::min<int64_t>((work + 255) / 256, (int64_t)c.sm_count * 64);
     int rc = GD_OK;
-    // pass 1: which triangle tiles hold a nonzero entry
-    cudaError_t e = cudaMalloc(&h->err, sizeof(int));
+    cudaError_t e = cudaMalloc(&h->inv, sizeof(int) * h->ns);
+    if (e == cudaSuccess) e = cudaMalloc(&h->mnodes, sizeof(uint32_t) * h->ns);
+    if (e == cudaSuccess) e = cudaMalloc(&h->err, sizeof(int));
     if (e == cudaSuccess) e = cudaMalloc(&w, na * sizeof(float));
     if (e == cudaSuccess) e = cudaMalloc(&d_tiles, sizeof(int2) * tile_nk.size());
-    if (e == cudaSuccess) e = cudaMalloc(&d_nz, ntri);
-    if (e == cudaSuccess) e = cudaMemset(d_nz, 0, ntri);
+    if (e == cudaSuccess) e = cudaMalloc(&d_nz, ntri * kSlices);
     if (e == cudaSuccess)
         e = cudaMemcpy(d_tiles, tile_nk.data(), sizeof(int2) * tile_nk.size(), cudaMemcpyHostToDevice);
     if (e != cudaSuccess) rc = cuda_error(e, "collision-matrix allocation");
     if (!rc) rc = launch_dense_tables(d, nullptr, w, nullptr);
-    std::vector<uint8_t> nz(ntri);
+    // the matrix order of the nodes: of the lattice's placements inside the
+    // Hilbert cube, the one whose matrices store the fewest tiles, counted on
+    // a sample of output nodes (the same for every placement)
+    std::vector<int> inv;
+    std::vector<uint32_t> mnodes;
     if (!rc) {
-        assemble_g_kernel<<<blocks, 256>>>(d, h->tiles, d_tiles, c.d_nodes, w, d_nz, nullptr, nullptr, nullptr);
+        const int span = (1 << hilbert_bits(d)) - std::max(d.nx, std::max(d.ny, d.nz));
+        const int nsample = std::min(h->ns, 128);
+        std::vector<uint32_t> sample(nsample), h_nodes(h->ns);
+        uint32_t *d_sample = nullptr;
+        e = cudaMemcpy(h_nodes.data(), c.d_nodes, sizeof(uint32_t) * h->ns, cudaMemcpyDeviceToHost);
+        for (int k = 0; k < nsample; k++) sample[k] = h_nodes[(size_t)k * h->ns / nsample];
+        if (e == cudaSuccess) e = cudaMalloc(&d_sample, sizeof(uint32_t) * nsample);
+        if (e == cudaSuccess)
+            e = cudaMemcpy(d_sample, sample.data(), sizeof(uint32_t) * nsample, cudaMemcpyHostToDevice);
+        const size_t nsz = (size_t)nsample * h->tiles * kSlices;
+        std::vector<uint8_t> snz(nsz);
+        int64_t best = -1;
+        for (int off = 0; e == cudaSuccess && off <= span; off++) {
+            std::vector<int> inv_o;
+            std::vector<uint32_t> mnodes_o;
+            matrix_order(c, off, inv_o, mnodes_o);
+            if (span > 0) {
+                e = cudaMemcpy(h->mnodes, mnodes_o.data(), sizeof(uint32_t) * h->ns, cudaMemcpyHostToDevice);
+                if (e == cudaSuccess) e = cudaMemset(d_nz, 0, nsz);
+                if (e != cudaSuccess) break;
+                const int sblocks =
+                    (int)std::min<int64_t>(((int64_t)nsample * h->tiles * BN * (BK / 8) + 255) / 256,
+                                           (int64_t)c.sm_count * 64);
+                assemble_g_kernel<<<std::max(sblocks, 1), 256>>>(d, nsample, h->tiles, d_tiles, d_sample, h->mnodes, w,
+                                                                 d_nz, nullptr, nullptr, nullptr);
+                e = cudaGetLastError();
+                if (e == cudaSuccess) e = cudaMemcpy(snz.data(), d_nz, nsz, cudaMemcpyDeviceToHost);
+                if (e != cudaSuccess) break;
+            }
+            int64_t stored = 0;  // MMA slices the sampled nodes' matrices issue
+            for (uint8_t v : snz) stored += v;
+            if (best < 0 || stored < best) {
+                best = stored;
+                inv.swap(inv_o);
+                mnodes.swap(mnodes_o);
+            }
+        }
+        cudaFree(d_sample);
+        if (e == cudaSuccess) e = cudaMemcpy(h->inv, inv.data(), sizeof(int) * h->ns, cudaMemcpyHostToDevice);
+        if (e == cudaSuccess)
+            e = cudaMemcpy(h->mnodes, mnodes.data(), sizeof(uint32_t) * h->ns, cudaMemcpyHostToDevice);
+        if (e == cudaSuccess) e = cudaMemset(d_nz, 0, ntri * kSlices);
+        if (e != cudaSuccess) rc = cuda_error(e, "collision-matrix node order");
+    }
+    // pass 1: which triangle tiles hold a nonzero entry
+    std::vector<uint8_t> nz(ntri * kSlices);
+    if (!rc) {
+        assemble_g_kernel<<<blocks, 256>>>(d, h->ns, h->tiles, d_tiles, c.d_nodes, h->mnodes, w, d_nz, nullptr,
+                                           nullptr, nullptr);
         e = cudaGetLastError();
-        if (e == cudaSuccess) e = cudaMemcpy(nz.data(), d_nz, ntri, cudaMemcpyDeviceToHost);
+        if (e == cudaSuccess) e = cudaMemcpy(nz.data(), d_nz, ntri * kSlices, cudaMemcpyDeviceToHost);
         if (e != cudaSuccess) rc = cuda_error(e, "collision-matrix tile scan");
     }
     // per-node lists of the stored tiles (n-major, k ascending) and their slots
@@ -619,11 +764,16 @@ extern "C" int gd_cmatrix_create(gd_ctx *ctx, int mode, gd_cmatrix **out)
     if (!rc) {
         for (int i = 0; i < h->ns; i++) {
             node_off[i] = (int)list.size();
-            for (int t = 0; t < h->tiles; t++)
-                if (nz[(size_t)i * h->tiles + t]) {
+            for (int t = 0; t < h->tiles; t++) {
+                uint32_t mask = 0;
+                for (int q = 0; q < kSlices; q++)
+                    if (nz[((size_t)i * h->tiles + t) * kSlices + q]) mask |= 1u << q;
+                if (mask) {
+                    h->slices += __builtin_popcount(mask);
                     slot_of[(size_t)i * h->tiles + t] = (int)list.size();
-                    list.push_back(((uint32_t)tile_nk[t].x << 16) | (uint32_t)tile_nk[t].y);
+                    list.push_back(mask << 28 | ((uint32_t)tile_nk[t].x << 16) | (uint32_t)tile_nk[t].y);
                 }
+            }
         }
         node_off[h->ns] = (int)list.size();
         h->slots = (int64_t)list.size();
@@ -660,14 +810,15 @@ extern "C" int gd_cmatrix_create(gd_ctx *ctx, int mode, gd_cmatrix **out)
     }
     // pass 2: the stored tiles, and the loss matrix
     if (!rc) {
-        assemble_g_kernel<<<blocks, 256>>>(d, h->tiles, d_tiles, c.d_nodes, w, nullptr, d_slot, h->gh, h->gl);
+        assemble_g_kernel<<<blocks, 256>>>(d, h->ns, h->tiles, d_tiles, c.d_nodes, h->mnodes, w, nullptr, d_slot, h->gh,
+                                           h->gl);
         e = cudaGetLastError();
         const size_t nb = (size_t)h->ns * h->ns_k;
         if (e == cudaSuccess) e = cudaMalloc(&h->bh, nb * 2);
         if (e == cudaSuccess) e = cudaMalloc(&h->bl, nb * 2);
         if (e == cudaSuccess) {
             assemble_b_kernel<<<(int)std::min<size_t>((nb + 255) / 256, (size_t)c.sm_count * 64), 256>>>(
-                d, h->ns_k, c.d_nodes, c.d_b, h->bh, h->bl);
+                d, h->ns_k, c.d_nodes, h->mnodes, c.d_b, h->bh, h->bl);
             e = cudaGetLastError();
         }
         if (e == cudaSuccess) e = cudaMemset(h->err, 0, sizeof(int));
@@ -686,6 +837,8 @@ extern "C" int gd_cmatrix_create(gd_ctx *ctx, int mode, gd_cmatrix **out)
         cudaFree(h->node_off);
         cudaFree(h->list);
         cudaFree(h->err);
+        cudaFree(h->inv);
+        cudaFree(h->mnodes);
         delete h;
         return rc;
     }
@@ -720,7 +873,10 @@ extern "C" int gd_cmatrix_destroy(gd_cmatrix *h)
     cudaFree(h->gl);
     cudaFree(h->fh);
     cudaFree(h->fl);
+    cudaFree(h->fp);
     cudaFree(h->err);
+    cudaFree(h->inv);
+    cudaFree(h->mnodes);
     delete h;
     return GD_OK;
 }
@@ -735,7 +891,8 @@ extern "C" int gd_cmatrix_gain(gd_cmatrix *h, const float *f, int ncells, int ld
     int rc0 = gd::ensure_f(h, ncells);
     if (rc0) return rc0;
     dim3 cb(32, 8), cg((h->ns_k + 31) / 32, (ncells + 31) / 32);
-    convert_f_kernel<<<cg, cb, 0, st>>>(f, h->ns, h->ns_k, ncells, ld, h->fh, split ? h->fl : nullptr);
+    convert_f_kernel<<<cg, cb, 0, st>>>(f, h->ns, h->ns_k, ncells, ld, h->inv, h->fh, split ? h->fl : nullptr, h->fp,
+                                        h->f_cells);
     GD_CUDA(cudaGetLastError());
 
     EncodeTiled enc;
@@ -761,7 +918,7 @@ extern "C" int gd_cmatrix_gain(gd_cmatrix *h, const float *f, int ncells, int ld
     }
     // cell tiles padded to whole clusters: a tile past ncells reads zeros and stores nothing
     const int m_tiles = ((ncells + BM - 1) / BM + cl - 1) / cl * cl;
-    CmParams prm{h->ns, h->ns_k, ncells, ld, f, gain, h->err, h->node_off, h->list, m_tiles, h->chain};
+    CmParams prm{h->ns, h->ns_k, ncells, ld, h->fp, h->f_cells, gain, h->err, h->node_off, h->list, m_tiles, h->chain};
     // one CTA per (cell tile, node), cell tiles fastest so that the CTAs in flight
     // share a few nodes' matrix tiles in L2 (a persistent grid of one CTA per SM
     // taking the tiles round-robin measured 3-4 % slower at 20^3 / 4096 cells)
@@ -837,10 +994,13 @@ int ensure_f(gd_cmatrix *h, int ncells)
     if (h->f_cells >= ncells) return GD_OK;
     cudaFree(h->fh);
     cudaFree(h->fl);
+    cudaFree(h->fp);
     h->fh = h->fl = nullptr;
+    h->fp = nullptr;
     h->f_cells = 0;
     GD_CUDA(cudaMalloc(&h->fh, (size_t)ncells * h->ns_k * 2));
     GD_CUDA(cudaMalloc(&h->fl, (size_t)ncells * h->ns_k * 2));
+    GD_CUDA(cudaMalloc(&h->fp, (size_t)ncells * h->ns_k * 4));
     h->f_cells = ncells;
     return GD_OK;
 }
@@ -853,7 +1013,7 @@ int cmatrix_loss(gd_cmatrix *h, const float *f, int ncells, int ld, float *nu, c
     int rc = ensure_f(h, ncells);
     if (rc) return rc;
     dim3 cb(32, 8), cg((h->ns_k + 31) / 32, (ncells + 31) / 32);
-    convert_f_kernel<<<cg, cb, 0, st>>>(f, h->ns, h->ns_k, ncells, ld, h->fh, h->fl);
+    convert_f_kernel<<<cg, cb, 0, st>>>(f, h->ns, h->ns_k, ncells, ld, h->inv, h->fh, h->fl, nullptr, 0);
     GD_CUDA(cudaGetLastError());
     const int stall = h->stall_next;  // a pending time-out injection fires here, once
     h->stall_next = 0;
@@ -866,6 +1026,7 @@ int cmatrix_loss(gd_cmatrix *h, const float *f, int ncells, int ld, float *nu, c
 }
 
 int64_t cmatrix_stored_tiles(const gd_cmatrix *cm) { return cm ? cm->slots : 0; }
+int64_t cmatrix_issued_slices(const gd_cmatrix *cm) { return cm ? cm->slices : 0; }
 
 double cmatrix_bytes_bound(const Context &c, int mode)
 {

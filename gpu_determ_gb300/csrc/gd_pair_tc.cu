@@ -27,11 +27,15 @@
 //                into one of two TMEM accumulators per (s, pass);
 //   warps 2..13  read C^T from TMEM (thread = cell; three warps per lane
 //                quadrant taking every third block of 16 groups) and add each
-//                group's sum, by fire-and-forget reductions, to the CTA's
-//                partial outputs at its members' targets (s +- g)/2.
-// Within one s every target receives one update and the epilogue takes the
-// units in s order, so every partial sum is formed in a fixed order; the
-// chunk partials are added in chunk order.  Results are bitwise reproducible.
+//                group's sum, by fire-and-forget reductions, to the outputs
+//                at its members' targets (s +- g)/2.
+// The outputs accumulate in 64-bit fixed point: each cell has a power-of-two
+// scale 2^k, set before the launch from a bound on its gain (max|f|^2 times
+// the largest gain of f = 1), and a group's sum enters as round(C * 2^k).
+// Integer addition is associative, so every unit of every s-chunk adds into
+// one accumulator per grid, in whatever order the hardware runs them, and the
+// result is still bitwise reproducible; no per-chunk partial buffers cross
+// DRAM and no reduction pass is needed, only a conversion back to FP32.
 // Every mbarrier wait is bounded (a time-out sets the error flag).
 #include <cuda.h>
 #include <cuda_bf16.h>
@@ -39,6 +43,7 @@
 
 #include <algorithm>
 #include <cstring>
+#include <map>
 #include <vector>
 
 #include "gd_internal.h"
@@ -61,6 +66,8 @@ constexpr int kProdWarps = 8;            // two groups of four
 constexpr int kPtThreads = 32 * (2 + kEpiWarps + kProdWarps);
 
 constexpr int kPtMaxGrids = 4;          // velocity grids one launch can serve
+constexpr int kBadScale = -0x7fffffff;  // scale exponent of a cell with a non-finite f
+constexpr int kAccBits = 60;            // |sum of contributions| * 2^k < 2^60
 
 // One velocity grid's tables and arrays as the kernel reads them.
 struct PtGrid {
@@ -72,12 +79,13 @@ struct PtGrid {
     const int4 *D_items;
     const uint32_t *D_members;
     const int *wrow;        // [nxyz] first weight row of each D
-    const int *s_bounds;    // [chunks + 1]
-    float *part;            // [chunk][n_pnt][cells_pad]
+    const int *s_bounds;    // [ranges + 1] bounds of the D ranges
+    unsigned long long *acc;  // [n_pnt][cells_pad] fixed-point gain (two's complement)
+    const int *kcell;       // [cells_pad] scale exponent k of each cell
 };
 
 // A launch: up to kPtMaxGrids grids and the device list of work units
-// {grid, 128-cell tile, s-chunk, 0} that the persistent CTAs pull, one at a
+// {grid, 128-cell tile, D range, octant} that the persistent CTAs pull, one at a
 // time, from a device counter.
 struct PtLaunch {
     PtGrid g[kPtMaxGrids];
@@ -102,14 +110,30 @@ struct Unit {
     int npass;
 };
 
-__device__ __forceinline__ void unit_of(const PtGrid &a, int sl, int q, Unit &u)
+// The walk visits the pair sums octant by octant: a unit covers a range of
+// class boxes D (linear order, Dz fastest) in one octant r, whose pair sum
+// has axis a equal to D_a (bit a of r clear) or to its reflection
+// 2 n_a - 2 - D_a (bit a set).  A reflection of D_a = n_a - 1 is that value
+// itself, so such positions repeat octant 0's and are empty.  Along a range
+// consecutive pair sums are neighbours (their gathers of f overlap), and the
+// eight octants' units of one D range are handed out one after another, so
+// the CTAs running them read each box's weight rows at about the same time:
+// from DRAM about once per launch instead of once per pair sum.
+__device__ __forceinline__ int walk_D(const Dims &d, int Did, int r, int &sx, int &sy, int &sz)
+{
+    const int Dz = Did % d.nz, Dy = (Did / d.nz) % d.ny, Dx = Did / d.nyz;
+    if (((r & 1) && Dx == d.nx - 1) || ((r & 2) && Dy == d.ny - 1) || ((r & 4) && Dz == d.nz - 1)) return -1;
+    sx = (r & 1) ? 2 * d.nx - 2 - Dx : Dx;
+    sy = (r & 2) ? 2 * d.ny - 2 - Dy : Dy;
+    sz = (r & 4) ? 2 * d.nz - 2 - Dz : Dz;
+    return Did;
+}
+
+__device__ __forceinline__ void unit_of(const PtGrid &a, int sl, int oct, int q, Unit &u)
 {
     const Dims &d = a.d;
-    u.sz = sl % d.sz;
-    u.sy = (sl / d.sz) % d.sy;
-    u.sx = sl / (d.sz * d.sy);
-    const int Dx = min(u.sx, 2 * d.nx - 2 - u.sx), Dy = min(u.sy, 2 * d.ny - 2 - u.sy),
-              Dz = min(u.sz, 2 * d.nz - 2 - u.sz);
+    const int Did = walk_D(d, sl, oct, u.sx, u.sy, u.sz);  // the caller skips empty positions
+    const int Dz = Did % d.nz, Dy = (Did / d.nz) % d.ny, Dx = Did / d.nyz;
     u.ex = (Dx >> 1) + 1;
     u.ey = (Dy >> 1) + 1;
     u.ez = (Dz >> 1) + 1;
@@ -118,7 +142,6 @@ __device__ __forceinline__ void unit_of(const PtGrid &a, int sl, int q, Unit &u)
     u.pz = u.sz & 1;
     u.K = u.ex * u.ey * u.ez;
     u.nch = (u.K + PT_KC - 1) / PT_KC;
-    const int Did = (Dx * d.ny + Dy) * d.nz + Dz;
     const int i0 = __ldg(a.D_item_off + Did), m = __ldg(a.D_item_off + Did + 1) - i0;
     u.npass = (m + PT_NMAX - 1) / PT_NMAX;
     u.it0 = i0 + q * PT_NMAX;
@@ -128,12 +151,12 @@ __device__ __forceinline__ void unit_of(const PtGrid &a, int sl, int q, Unit &u)
     u.wrow = __ldg(a.wrow + Did);
 }
 
-__device__ __forceinline__ int npass_of(const PtGrid &a, int sl)
+__device__ __forceinline__ int npass_of(const PtGrid &a, int sl, int oct)
 {
     const Dims &d = a.d;
-    const int sz = sl % d.sz, sy = (sl / d.sz) % d.sy, sx = sl / (d.sz * d.sy);
-    const int Dx = min(sx, 2 * d.nx - 2 - sx), Dy = min(sy, 2 * d.ny - 2 - sy), Dz = min(sz, 2 * d.nz - 2 - sz);
-    const int Did = (Dx * d.ny + Dy) * d.nz + Dz;
+    int sx, sy, sz;
+    const int Did = walk_D(d, sl, oct, sx, sy, sz);
+    if (Did < 0) return 0;
     const int m = __ldg(a.D_item_off + Did + 1) - __ldg(a.D_item_off + Did);
     return (m + PT_NMAX - 1) / PT_NMAX;
 }
@@ -202,7 +225,7 @@ __global__ void __launch_bounds__(kPtThreads, 1)
         const int4 un_ = L.units[ui_];
         const PtGrid &a = L.g[un_.x];
         const Dims &d = a.d;
-        const int m_tile = un_.y, chunk = un_.z;
+        const int m_tile = un_.y, chunk = un_.z, oct = un_.w;
         const int s_begin = __ldg(a.s_bounds + chunk), s_end = __ldg(a.s_bounds + chunk + 1);
 
     if (warp == 0) {
@@ -211,10 +234,10 @@ __global__ void __launch_bounds__(kPtThreads, 1)
             {
             const CUtensorMap *tmWh = &maps.wh[un_.x], *tmWl = &maps.wl[un_.x];
             for (int sl = s_begin; ok && sl < s_end; sl++) {
-                const int np = npass_of(a, sl);
+                const int np = npass_of(a, sl, oct);
                 for (int q = 0; ok && q < np; q++) {
                     Unit u;
-                    unit_of(a, sl, q, u);
+                    unit_of(a, sl, oct, q, u);
                     for (int ch = 0; ch < u.nch; ch++, ck++) {
                         const int st = ck & 1;
                         if (!mbar_wait(smem_u32(&empty_bar[st]), ((uint32_t)(ck >> 1) & 1u) ^ 1u, L.err)) {
@@ -240,10 +263,10 @@ __global__ void __launch_bounds__(kPtThreads, 1)
         if (lane == 0 && ok) {
             {
             for (int sl = s_begin; ok && sl < s_end; sl++) {
-                const int np = npass_of(a, sl);
+                const int np = npass_of(a, sl, oct);
                 for (int q = 0; ok && q < np; q++, uc++) {
                     Unit u;
-                    unit_of(a, sl, q, u);
+                    unit_of(a, sl, oct, q, u);
                     const int buf = uc & 1;
                     if (!mbar_wait(smem_u32(&acce_bar[buf]), ((uint32_t)(uc >> 1) & 1u) ^ 1u, L.err)) {
                         ok = false;
@@ -292,17 +315,21 @@ __global__ void __launch_bounds__(kPtThreads, 1)
         const int cells_pad = a.cells_pad, nyz = d.nyz, nz = d.nz;
         const int4 *D_items = a.D_items;
         const uint32_t *D_members = a.D_members;
-        float *part = a.part + (size_t)chunk * d.n_pnt * cells_pad + cell;
+        unsigned long long *acc = a.acc + cell;
+        // the cell's fixed-point scale 2^k as two exact power-of-two factors
+        const int kc = live ? __ldg(a.kcell + cell) : 0;
+        const int k1 = kc == kBadScale ? 0 : kc / 2, k2 = kc == kBadScale ? 0 : kc - kc / 2;
+        const float s1 = __int_as_float((127 + k1) << 23), s2 = __int_as_float((127 + k2) << 23);
         for (int sl = s_begin; ok && sl < s_end; sl++) {
-            const int np = npass_of(a, sl);
+            const int np = npass_of(a, sl, oct);
             for (int q = 0; ok && q < np; q++, uc++) {
                 Unit u;
-                unit_of(a, sl, q, u);
+                unit_of(a, sl, oct, q, u);
                 const int buf = uc & 1;
                 if (lane == 0 && !mbar_wait(smem_u32(&accf_bar[buf]), (uint32_t)(uc >> 1) & 1u, L.err)) epi_fail = 1;
-                // all warps of a cell finish one unit before any starts the next
-                // (their targets may coincide across units); the decision to stop
-                // is taken after the barrier, by all of them alike
+                // the epilogue warps take each unit together, so that the
+                // decision to stop is taken after the barrier, by all of them
+                // alike
                 asm volatile("bar.sync 1, %0;" ::"n"(32 * kEpiWarps) : "memory");
                 if (*(volatile int *)&epi_fail) {
                     ok = false;
@@ -316,14 +343,12 @@ __global__ void __launch_bounds__(kPtThreads, 1)
                     if (!live) continue;
                     const int mend = min(16, u.mcnt - m0);
                     for (int t = 0; t < mend; t++) {
+                        // the group's sum in the cell's fixed point; integer
+                        // fire-and-forget reductions, whose order does not
+                        // matter (contributions below 2^-k round away)
+                        const long long qv = __float2ll_rn(__fmul_rn(__fmul_rn(v[t], s1), s2));
+                        if (qv == 0) continue;
                         const int4 item = __ldg(D_items + u.it0 + m0 + t);
-                        const float acc = v[t];
-                        // fire-and-forget reductions: within one s every target
-                        // receives one update, and the units of one cell are
-                        // ordered by the epilogue barrier, so each partial sum
-                        // still accumulates in s order (bitwise reproducible);
-                        // like the tensor-core products, the reduction flushes
-                        // subnormal contributions to zero
                         for (int mm = item.y; mm < item.z; mm++) {
                             const uint32_t pk = __ldg(D_members + mm);
                             const int gx = 2 * (int)(pk & 31) + u.px, gy = 2 * (int)((pk >> 6) & 31) + u.py,
@@ -337,8 +362,8 @@ __global__ void __launch_bounds__(kPtThreads, 1)
                                 const bool dup = (hx && gx == 0) || (hy && gy == 0) || (hz && gz == 0);
                                 const int tg = dup ? -1 : cmap[(hx ? X1 : X0) + (hy ? Y1 : Y0) + (hz ? Z1 : Z0)];
                                 if (tg >= 0)
-                                    asm volatile("red.relaxed.gpu.global.add.f32 [%0], %1;" ::"l"(part + (size_t)tg * cells_pad),
-                                                 "f"(acc)
+                                    asm volatile("red.relaxed.gpu.global.add.u64 [%0], %1;" ::"l"(acc + (size_t)tg * cells_pad),
+                                                 "l"((unsigned long long)qv)
                                                  : "memory");
                             }
                         }
@@ -364,10 +389,10 @@ __global__ void __launch_bounds__(kPtThreads, 1)
         const float *fcol = a.f + (live ? cell : 0);
         const int ldf = a.ld, nyz = d.nyz, nz = d.nz;  // in registers for the gather loop
         for (int sl = s_begin; ok && sl < s_end; sl++) {
-            const int np = npass_of(a, sl);
+            const int np = npass_of(a, sl, oct);
             for (int q = 0; ok && q < np; q++) {
                 Unit u;
-                unit_of(a, sl, q, u);
+                unit_of(a, sl, oct, q, u);
                 for (int ch = 0; ch < u.nch; ch++, ck++) {
                     const int st = ck & 1;
                     if (st != grp) continue;
@@ -464,6 +489,72 @@ __global__ void __launch_bounds__(kPtThreads, 1)
 
 }  // namespace
 
+namespace {
+
+// Scale exponent of every cell: k = kAccBits - e with bound = max|f|^2 * imax1
+// < 2^e, imax1 the largest gain of f = 1 on this grid.  Every pair product
+// obeys |P(f)| <= max|f|^2 P(1), so every output's sum of |contributions| is at
+// most the bound (the BF16 split of P and W changes it by ~1e-5 relative), and
+// the fixed-point sums stay below 2^60.  Block = 32 cells x 8 node strides.
+__global__ void pt_scale_kernel(const float *__restrict__ f, int ld, int n_pnt, int ncells, int cells_pad,
+                                double imax1, int *__restrict__ kcell)
+{
+    __shared__ float fmax_s[8][32];
+    __shared__ int bad_s[8][32];
+    const int cx = threadIdx.x, cy = threadIdx.y;
+    const int cell = blockIdx.x * 32 + cx;
+    float fm = 0.f;
+    int bad = 0;
+    if (cell < ncells)
+        for (int p = cy; p < n_pnt; p += 8) {
+            const float v = fabsf(__ldg(f + (size_t)p * ld + cell));
+            if (!(v <= 3.402823466e38f)) bad = 1;  // NaN or infinity
+            else fm = fmaxf(fm, v);
+        }
+    fmax_s[cy][cx] = fm;
+    bad_s[cy][cx] = bad;
+    __syncthreads();
+    if (cy == 0 && cell < cells_pad) {
+        for (int y = 1; y < 8; y++) {
+            fm = fmaxf(fm, fmax_s[y][cx]);
+            bad |= bad_s[y][cx];
+        }
+        int k = 0;
+        if (bad) {
+            k = kBadScale;
+        } else if (fm > 0.f && cell < ncells) {
+            int e = 0;
+            frexp((double)fm * (double)fm * imax1, &e);
+            k = min(240, max(-120, kAccBits - e));
+        }
+        kcell[cell] = k;
+    }
+}
+
+// Fixed-point sums back to FP32: acc * 2^-k, rounded once (the power-of-two
+// factors are exact while the result is normal); NaN for a non-finite f.
+__global__ void pt_convert_kernel(const long long *__restrict__ acc, const int *__restrict__ kcell, int n_pnt,
+                                  int cells_pad, int ncells, int ld, float *__restrict__ gain)
+{
+    const int64_t outs = (int64_t)n_pnt * ncells;
+    for (int64_t o = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; o < outs; o += (int64_t)gridDim.x * blockDim.x) {
+        const int p = (int)(o / ncells), cell = (int)(o - (int64_t)p * ncells);
+        const int k = __ldg(kcell + cell);
+        float g;
+        if (k == kBadScale) {
+            g = __int_as_float(0x7fc00000);
+        } else {
+            const int k1 = k / 2, k2 = k - k / 2;
+            g = __fmul_rn(__fmul_rn(__ll2float_rn(__ldg(acc + (size_t)p * cells_pad + cell)),
+                                    __int_as_float((127 - k1) << 23)),
+                          __int_as_float((127 - k2) << 23));
+        }
+        gain[(size_t)p * ld + cell] = g;
+    }
+}
+
+}  // namespace
+
 // Weight table of the tensor-core pair path: for every D (box-indexed like g),
 // its groups' rows restricted to B(D), in chunks of 64 class offsets: rows
 // wrow[D] + ch * mpad(D) + m hold group m's weights at offsets ch * 64 .. +63
@@ -475,6 +566,9 @@ struct PairTc {
     int *next = nullptr;  // unit counter of the launches led by this context
     int64_t rows = 0;
     int max_items = 0;
+    double imax1 = 0.0;   // largest gain of f = 1 (sets the cells' fixed-point scales)
+    std::vector<int64_t> walk_prefix;          // [nxyz + 1] cumulative work over the class boxes D
+    std::map<int, int *> bounds_dev;           // D-range bounds, per range count
 };
 
 namespace {
@@ -519,6 +613,7 @@ void pair_tc_free(Context &c)
     cudaFree(c.pair_tc->wrow);
     cudaFree(c.pair_tc->err);
     cudaFree(c.pair_tc->next);
+    for (auto &kv : c.pair_tc->bounds_dev) cudaFree(kv.second);
     delete c.pair_tc;
     c.pair_tc = nullptr;
 }
@@ -620,8 +715,73 @@ int pair_tc_build(Context &c)
         return rc;
     }
     pt->max_items = max_items;
+    // the largest gain of f = 1, by the FP32 pair kernel on one cell
+    float *ones = nullptr, *g1 = nullptr;
+    cudaError_t e = cudaMalloc(&ones, sizeof(float) * d.n_pnt);
+    if (e == cudaSuccess) e = cudaMalloc(&g1, sizeof(float) * d.n_pnt);
+    std::vector<float> h1(d.n_pnt, 1.0f);
+    if (e == cudaSuccess) e = cudaMemcpy(ones, h1.data(), sizeof(float) * d.n_pnt, cudaMemcpyHostToDevice);
+    rc = e == cudaSuccess ? run_gain(c, ones, 1, 1, g1, 0) : cuda_error(e, "pair weight table: unit gain");
+    if (!rc && (e = cudaMemcpy(h1.data(), g1, sizeof(float) * d.n_pnt, cudaMemcpyDeviceToHost)) != cudaSuccess)
+        rc = cuda_error(e, "pair weight table: unit gain");
+    cudaFree(ones);
+    cudaFree(g1);
+    if (rc) {
+        pair_tc_free(c);
+        return rc;
+    }
+    double m1 = 0.0;
+    for (float v : h1) m1 = std::max(m1, (double)v);
+    if (!(m1 > 0.0 && m1 < 1e300)) {
+        pair_tc_free(c);
+        return set_error(GD_ERR_CUDA, "pair weight table: unit gain not finite");
+    }
+    pt->imax1 = m1;
+    // work of one octant's pass over the class boxes D (the pair sum s = D of
+    // octant 0 stands for all eight, whose work is the same)
+    pt->walk_prefix.assign((size_t)d.nxyz + 1, 0);
+    int64_t acc = 0;
+    for (int Did = 0; Did < d.nxyz; Did++) {
+        const int Dz = Did % d.nz, Dy = (Did / d.nz) % d.ny, Dx = Did / d.nyz;
+        const int64_t sl = ((int64_t)Dx * d.sy + Dy) * d.sz + Dz;
+        pt->walk_prefix[Did] = acc;
+        acc += c.s_work_prefix[sl + 1] - c.s_work_prefix[sl];
+    }
+    pt->walk_prefix[d.nxyz] = acc;
     return GD_OK;
 }
+
+namespace {
+
+// Work-balanced D-range bounds, uploaded once per range count.
+int pt_bounds_device(Context &c, int nchunks, const int **out)
+{
+    PairTc &pt = *c.pair_tc;
+    auto it = pt.bounds_dev.find(nchunks);
+    if (it == pt.bounds_dev.end()) {
+        const std::vector<int64_t> &pre = pt.walk_prefix;
+        const int npos = (int)pre.size() - 1;
+        std::vector<int> bounds(nchunks + 1);
+        bounds[0] = 0;
+        for (int k = 1; k < nchunks; k++) {
+            const int64_t target = pre[npos] * k / nchunks;
+            bounds[k] = std::max(bounds[k - 1], (int)(std::lower_bound(pre.begin(), pre.end(), target) - pre.begin()));
+        }
+        bounds[nchunks] = npos;
+        int *dev = nullptr;
+        GD_CUDA(cudaMalloc(&dev, sizeof(int) * (nchunks + 1)));
+        cudaError_t e = cudaMemcpy(dev, bounds.data(), sizeof(int) * (nchunks + 1), cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) {
+            cudaFree(dev);
+            return cuda_error(e, "pair tensor-core chunk bounds");
+        }
+        it = pt.bounds_dev.emplace(nchunks, dev).first;
+    }
+    *out = it->second;
+    return GD_OK;
+}
+
+}  // namespace
 
 int pair_tc_take_timeout(Context &c, cudaStream_t st, bool *timed_out)
 {
@@ -640,33 +800,40 @@ int pair_tc_take_timeout(Context &c, cudaStream_t st, bool *timed_out)
 
 namespace {
 
-// s-chunks of one grid's walk for ncells cells: about four waves of one CTA
-// per SM, within a 16 GiB partial buffer
+// D ranges of one grid's walk for ncells cells (each run in all eight
+// octants): about four waves of one CTA per SM
 int pt_chunks(const Context &c, int ncells)
 {
-    const Dims &d = c.d;
     const int tiles = (ncells + PT_BM - 1) / PT_BM;
-    const int cells_pad = tiles * PT_BM;
     const int sms = std::max(1, c.sm_count);
-    int nchunks = (int)std::min<int64_t>(std::max(1, (4 * sms + tiles - 1) / tiles), d.ns);
-    while (nchunks > 1 && (size_t)nchunks * d.n_pnt * cells_pad * sizeof(float) > ((size_t)16 << 30)) nchunks--;
-    return nchunks;
+    return (int)std::min<int64_t>(std::max(1, (4 * sms + 8 * tiles - 1) / (8 * tiles)), c.d.nxyz);
+}
+
+// Cell tiles whose units run together: the accumulators they share (8 bytes
+// per node and cell) stay within ~32 MB, far inside L2
+int pt_tile_group(const Context &c, int tiles)
+{
+    const size_t per_tile = (size_t)c.d.n_pnt * PT_BM * sizeof(long long);
+    return std::max(1, std::min(tiles, (int)(((size_t)32 << 20) / per_tile)));
 }
 
 }  // namespace
 
 // The pair-product gain with the contraction on the tensor cores for one or
 // more grids (each with its own context, cells and output) in one launch:
-// each grid's walk over s is split into work-balanced chunks, and every
-// (grid, 128-cell tile, chunk) unit writes its own partial sums, so the
-// results do not depend on how the units are spread over the CTAs and equal
-// those of separate launches bit for bit.  The units are ordered by their
-// work, largest first (within a grid chunk-major, tiles fastest, so that the
-// CTAs in flight share weight rows in L2), and pulled from a device counter
-// by one persistent CTA per SM as each finishes its previous unit.  The unit list is uploaded once per launch shape and cached on the
-// first job's context (a replayed graph reads it without a host copy); a
-// pipeline time-out is recorded on that context.  Then the chunk partials of
-// every grid are added in chunk order.
+// each grid's walk over s is split into work-balanced D ranges, each run in
+// the eight octants, and every (grid, 128-cell tile, D range, octant) unit
+// adds its group sums into the grid's fixed-point accumulator, so the results
+// do not depend on how the units are spread over the CTAs and equal those of
+// separate launches bit for bit.  The
+// units are ordered by their work, largest first; within a grid by groups of
+// cell tiles whose accumulators fit L2 together, then by D range, octant and
+// tile (so that the CTAs in flight share weight rows in L2).  One
+// persistent CTA per SM pulls them from a device counter as it finishes its
+// previous unit.  The unit list is uploaded once per launch shape and cached
+// on the first job's context (a replayed graph reads it without a host copy);
+// a pipeline time-out is recorded on that context.  Before the launch a small
+// kernel sets every cell's scale; after it the sums are converted to FP32.
 int launch_pair_tc(const PtJob *jobs, int njobs, cudaStream_t st)
 {
     if (njobs < 1 || njobs > kPtMaxGrids) return set_error(GD_ERR_UNSUPPORTED, "pair tensor-core launch: 1-4 grids");
@@ -688,21 +855,25 @@ int launch_pair_tc(const PtJob *jobs, int njobs, cudaStream_t st)
         const int tiles = (jobs[j].ncells + PT_BM - 1) / PT_BM;
         cells_pad[j] = tiles * PT_BM;
         chunks[j] = pt_chunks(c, jobs[j].ncells);
-        unit_cost[j] = (double)c.s_work_prefix[d.ns] / chunks[j];
+        unit_cost[j] = (double)c.s_work_prefix[d.ns] / (8.0 * chunks[j]);
         const int *d_bounds = nullptr;
-        int rc = gain_bounds_device(c, chunks[j], &d_bounds);
+        int rc = pt_bounds_device(c, chunks[j], &d_bounds);
         if (rc) return rc;
-        const size_t part_bytes = (size_t)chunks[j] * d.n_pnt * cells_pad[j] * sizeof(float);
-        if ((rc = ensure_scratch(c, part_bytes))) return rc;
-        float *part = static_cast<float *>(c.scratch.ptr);
-        GD_CUDA(cudaMemsetAsync(part, 0, part_bytes, st));
+        const size_t acc_bytes = (size_t)d.n_pnt * cells_pad[j] * sizeof(long long);
+        if ((rc = ensure_scratch(c, acc_bytes + sizeof(int) * cells_pad[j]))) return rc;
+        auto *acc = static_cast<unsigned long long *>(c.scratch.ptr);
+        int *kcell = reinterpret_cast<int *>(static_cast<char *>(c.scratch.ptr) + acc_bytes);
+        GD_CUDA(cudaMemsetAsync(acc, 0, acc_bytes, st));
+        pt_scale_kernel<<<tiles * (PT_BM / 32), dim3(32, 8), 0, st>>>(jobs[j].f, jobs[j].ld, d.n_pnt, jobs[j].ncells,
+                                                                        cells_pad[j], c.pair_tc->imax1, kcell);
+        GD_CUDA(cudaGetLastError());
         const uint64_t dims[2] = {(uint64_t)PT_KC, (uint64_t)std::max<int64_t>(c.pair_tc->rows, 16)};
         const uint64_t strides[1] = {(uint64_t)PT_KC * 2};
         const uint32_t box[2] = {PT_KC, 16};
         if ((rc = encode_bf16_sw128(&maps.wh[j], c.pair_tc->wh, 2, dims, strides, box))) return rc;
         if ((rc = encode_bf16_sw128(&maps.wl[j], c.pair_tc->wl, 2, dims, strides, box))) return rc;
         L.g[j] = PtGrid{d, jobs[j].f, jobs[j].ld, jobs[j].ncells, cells_pad[j], c.d_cmap, c.d_D_item_off,
-                        c.d_D_items, c.d_D_members, c.pair_tc->wrow, d_bounds, part};
+                        c.d_D_items, c.d_D_members, c.pair_tc->wrow, d_bounds, acc, kcell};
         key += std::to_string(tiles) + "x" + std::to_string(chunks[j]) + "c" +
                std::to_string((long long)unit_cost[j]) + ";";
     }
@@ -718,9 +889,14 @@ int launch_pair_tc(const PtJob *jobs, int njobs, cudaStream_t st)
         for (int j = 0; j < njobs; j++) order[j] = j;
         std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return unit_cost[a] > unit_cost[b]; });
         std::vector<int4> units;
-        for (int j : order)
-            for (int ch = 0; ch < chunks[j]; ch++)
-                for (int t = 0; t < cells_pad[j] / PT_BM; t++) units.push_back(make_int4(j, t, ch, 0));
+        for (int j : order) {
+            const int tiles = cells_pad[j] / PT_BM, grp = pt_tile_group(*jobs[j].c, tiles);
+            for (int t0 = 0; t0 < tiles; t0 += grp)
+                for (int ch = 0; ch < chunks[j]; ch++)
+                    for (int oct = 0; oct < 8; oct++)
+                        for (int t = t0; t < std::min(tiles, t0 + grp); t++)
+                            units.push_back(make_int4(j, t, ch, oct));
+        }
         int4 *dev = nullptr;
         GD_CUDA(cudaMalloc(&dev, sizeof(int4) * units.size()));
         cudaError_t e = cudaMemcpy(dev, units.data(), sizeof(int4) * units.size(), cudaMemcpyHostToDevice);
@@ -747,9 +923,12 @@ int launch_pair_tc(const PtJob *jobs, int njobs, cudaStream_t st)
     // the kernel records a pipeline time-out instead of hanging; the call only
     // enqueues work, and gd_ctx_check reports the record
     for (int j = 0; j < njobs; j++) {
-        const int rc = reduce_gain_partials(*jobs[j].c, L.g[j].part, chunks[j], cells_pad[j], jobs[j].ncells,
-                                            jobs[j].ld, jobs[j].gain, st);
-        if (rc) return rc;
+        const Context &c = *jobs[j].c;
+        const int64_t outs = (int64_t)c.d.n_pnt * jobs[j].ncells;
+        const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>((outs + 255) / 256, (int64_t)c.sm_count * 16));
+        pt_convert_kernel<<<blocks, 256, 0, st>>>(reinterpret_cast<const long long *>(L.g[j].acc), L.g[j].kcell,
+                                                  c.d.n_pnt, cells_pad[j], jobs[j].ncells, jobs[j].ld, jobs[j].gain);
+        GD_CUDA(cudaGetLastError());
     }
     return GD_OK;
 }

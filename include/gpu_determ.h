@@ -14,8 +14,8 @@
  *    (ld >= ncells).  With R large enough to keep every node this is exactly
  *    the reference layout f[(i*ny + j)*nz + k][cell] with npx = ld.
  *  - Streams are cudaStream_t passed as gd_stream (NULL = legacy stream).
- *  - Results are bitwise reproducible run to run: no atomics, fixed-order
- *    reductions.
+ *  - Results are bitwise reproducible run to run: floating-point sums run in
+ *    a fixed order, and the one path that adds with atomics adds integers.
  *
  * Reference interfaces (savthe/gpu_determ) each entry point replaces are cited
  * as file:line.
@@ -62,6 +62,7 @@ typedef struct {
     int64_t contraction_terms; /* nonzero-weight x pair-product terms per cell-eval */
     int64_t scatter_terms;     /* (s, g, sign) output updates per cell-eval */
     int64_t cmatrix_tiles;     /* stored 256 x 64 tiles of the collision matrices (0 without) */
+    int64_t cmatrix_slices;    /* 256 x 16 slices of those tiles with a nonzero entry: the MMA K steps issued */
 } gd_info;
 
 /* Library version (major*10000 + minor*100 + patch). */
@@ -210,9 +211,10 @@ int gd_cmatrix_check(gd_cmatrix *cm, gd_stream stream);
  * GD_GAIN_PAIR (default, FP32 pair-product kernel), GD_GAIN_CMATRIX_BF16 or
  * GD_GAIN_CMATRIX_BF16X3 (builds the context's collision matrices), or
  * GD_GAIN_PAIR_TC (the pair-product formulation with its weight contraction on
- * the tensor cores, pair products and weights split into BF16 hi + lo; builds
- * a per-class-box weight table of a few GB at 24^3 instead of n^3 matrices,
- * so it serves the grids whose collision matrices do not fit). */
+ * the tensor cores, pair products and weights split into BF16 hi + lo, each
+ * cell's outputs summed in 64-bit fixed point scaled by a bound on its gain;
+ * builds a per-class-box weight table of a few GB at 24^3 instead of n^3
+ * matrices, so it serves the grids whose collision matrices do not fit). */
 enum { GD_GAIN_PAIR = 0, GD_GAIN_CMATRIX_BF16 = 1, GD_GAIN_CMATRIX_BF16X3 = 2, GD_GAIN_PAIR_TC = 3 };
 int gd_ctx_set_gain_path(gd_ctx *ctx, int path);
 
