@@ -79,13 +79,13 @@ struct PtGrid {
     const int4 *D_items;
     const uint32_t *D_members;
     const int *wrow;        // [nxyz] first weight row of each D
-    const int *s_bounds;    // [ranges + 1] bounds of the D ranges
+    const int *s_bounds;    // [chunks + 1] bounds of the walk's chunks
     unsigned long long *acc;  // [n_pnt][cells_pad] fixed-point gain (two's complement)
     const int *kcell;       // [cells_pad] scale exponent k of each cell
 };
 
 // A launch: up to kPtMaxGrids grids and the device list of work units
-// {grid, 128-cell tile, D range, octant} that the persistent CTAs pull, one at a
+// {grid, 128-cell tile, chunk of the walk, 0} that the persistent CTAs pull, one at a
 // time, from a device counter.
 struct PtLaunch {
     PtGrid g[kPtMaxGrids];
@@ -110,17 +110,16 @@ struct Unit {
     int npass;
 };
 
-// The walk visits the pair sums octant by octant: a unit covers a range of
-// class boxes D (linear order, Dz fastest) in one octant r, whose pair sum
-// has axis a equal to D_a (bit a of r clear) or to its reflection
-// 2 n_a - 2 - D_a (bit a set).  A reflection of D_a = n_a - 1 is that value
-// itself, so such positions repeat octant 0's and are empty.  Along a range
-// consecutive pair sums are neighbours (their gathers of f overlap), and the
-// eight octants' units of one D range are handed out one after another, so
-// the CTAs running them read each box's weight rows at about the same time:
-// from DRAM about once per launch instead of once per pair sum.
-__device__ __forceinline__ int walk_D(const Dims &d, int Did, int r, int &sx, int &sy, int &sz)
+// The walk visits the pair sums class box by class box: position
+// p = 8 D + r, D = (Dx ny + Dy) nz + Dz, holds the pair sum whose axis a is
+// D_a (bit a of r clear) or its reflection 2 n_a - 2 - D_a (bit a set).  A
+// reflection of D_a = n_a - 1 is that value itself, so such positions repeat
+// an earlier one and are empty.  The (up to) eight pair sums of one D read the
+// same weight rows one after another, so the rows come from DRAM about once
+// per launch instead of once per pair sum.
+__device__ __forceinline__ int walk_D(const Dims &d, int p, int &sx, int &sy, int &sz)
 {
+    const int Did = p >> 3, r = p & 7;
     const int Dz = Did % d.nz, Dy = (Did / d.nz) % d.ny, Dx = Did / d.nyz;
     if (((r & 1) && Dx == d.nx - 1) || ((r & 2) && Dy == d.ny - 1) || ((r & 4) && Dz == d.nz - 1)) return -1;
     sx = (r & 1) ? 2 * d.nx - 2 - Dx : Dx;
@@ -129,10 +128,10 @@ __device__ __forceinline__ int walk_D(const Dims &d, int Did, int r, int &sx, in
     return Did;
 }
 
-__device__ __forceinline__ void unit_of(const PtGrid &a, int sl, int oct, int q, Unit &u)
+__device__ __forceinline__ void unit_of(const PtGrid &a, int sl, int q, Unit &u)
 {
     const Dims &d = a.d;
-    const int Did = walk_D(d, sl, oct, u.sx, u.sy, u.sz);  // the caller skips empty positions
+    const int Did = walk_D(d, sl, u.sx, u.sy, u.sz);  // the caller skips empty positions
     const int Dz = Did % d.nz, Dy = (Did / d.nz) % d.ny, Dx = Did / d.nyz;
     u.ex = (Dx >> 1) + 1;
     u.ey = (Dy >> 1) + 1;
@@ -151,11 +150,11 @@ __device__ __forceinline__ void unit_of(const PtGrid &a, int sl, int oct, int q,
     u.wrow = __ldg(a.wrow + Did);
 }
 
-__device__ __forceinline__ int npass_of(const PtGrid &a, int sl, int oct)
+__device__ __forceinline__ int npass_of(const PtGrid &a, int sl)
 {
     const Dims &d = a.d;
     int sx, sy, sz;
-    const int Did = walk_D(d, sl, oct, sx, sy, sz);
+    const int Did = walk_D(d, sl, sx, sy, sz);
     if (Did < 0) return 0;
     const int m = __ldg(a.D_item_off + Did + 1) - __ldg(a.D_item_off + Did);
     return (m + PT_NMAX - 1) / PT_NMAX;
@@ -225,7 +224,7 @@ __global__ void __launch_bounds__(kPtThreads, 1)
         const int4 un_ = L.units[ui_];
         const PtGrid &a = L.g[un_.x];
         const Dims &d = a.d;
-        const int m_tile = un_.y, chunk = un_.z, oct = un_.w;
+        const int m_tile = un_.y, chunk = un_.z;
         const int s_begin = __ldg(a.s_bounds + chunk), s_end = __ldg(a.s_bounds + chunk + 1);
 
     if (warp == 0) {
@@ -234,10 +233,10 @@ __global__ void __launch_bounds__(kPtThreads, 1)
             {
             const CUtensorMap *tmWh = &maps.wh[un_.x], *tmWl = &maps.wl[un_.x];
             for (int sl = s_begin; ok && sl < s_end; sl++) {
-                const int np = npass_of(a, sl, oct);
+                const int np = npass_of(a, sl);
                 for (int q = 0; ok && q < np; q++) {
                     Unit u;
-                    unit_of(a, sl, oct, q, u);
+                    unit_of(a, sl, q, u);
                     for (int ch = 0; ch < u.nch; ch++, ck++) {
                         const int st = ck & 1;
                         if (!mbar_wait(smem_u32(&empty_bar[st]), ((uint32_t)(ck >> 1) & 1u) ^ 1u, L.err)) {
@@ -263,10 +262,10 @@ __global__ void __launch_bounds__(kPtThreads, 1)
         if (lane == 0 && ok) {
             {
             for (int sl = s_begin; ok && sl < s_end; sl++) {
-                const int np = npass_of(a, sl, oct);
+                const int np = npass_of(a, sl);
                 for (int q = 0; ok && q < np; q++, uc++) {
                     Unit u;
-                    unit_of(a, sl, oct, q, u);
+                    unit_of(a, sl, q, u);
                     const int buf = uc & 1;
                     if (!mbar_wait(smem_u32(&acce_bar[buf]), ((uint32_t)(uc >> 1) & 1u) ^ 1u, L.err)) {
                         ok = false;
@@ -321,10 +320,10 @@ __global__ void __launch_bounds__(kPtThreads, 1)
         const int k1 = kc == kBadScale ? 0 : kc / 2, k2 = kc == kBadScale ? 0 : kc - kc / 2;
         const float s1 = __int_as_float((127 + k1) << 23), s2 = __int_as_float((127 + k2) << 23);
         for (int sl = s_begin; ok && sl < s_end; sl++) {
-            const int np = npass_of(a, sl, oct);
+            const int np = npass_of(a, sl);
             for (int q = 0; ok && q < np; q++, uc++) {
                 Unit u;
-                unit_of(a, sl, oct, q, u);
+                unit_of(a, sl, q, u);
                 const int buf = uc & 1;
                 if (lane == 0 && !mbar_wait(smem_u32(&accf_bar[buf]), (uint32_t)(uc >> 1) & 1u, L.err)) epi_fail = 1;
                 // the epilogue warps take each unit together, so that the
@@ -389,10 +388,10 @@ __global__ void __launch_bounds__(kPtThreads, 1)
         const float *fcol = a.f + (live ? cell : 0);
         const int ldf = a.ld, nyz = d.nyz, nz = d.nz;  // in registers for the gather loop
         for (int sl = s_begin; ok && sl < s_end; sl++) {
-            const int np = npass_of(a, sl, oct);
+            const int np = npass_of(a, sl);
             for (int q = 0; ok && q < np; q++) {
                 Unit u;
-                unit_of(a, sl, oct, q, u);
+                unit_of(a, sl, q, u);
                 for (int ch = 0; ch < u.nch; ch++, ck++) {
                     const int st = ck & 1;
                     if (st != grp) continue;
@@ -567,8 +566,8 @@ struct PairTc {
     int64_t rows = 0;
     int max_items = 0;
     double imax1 = 0.0;   // largest gain of f = 1 (sets the cells' fixed-point scales)
-    std::vector<int64_t> walk_prefix;          // [nxyz + 1] cumulative work over the class boxes D
-    std::map<int, int *> bounds_dev;           // D-range bounds, per range count
+    std::vector<int64_t> walk_prefix;          // [8 nxyz + 1] cumulative work along the walk
+    std::map<int, int *> bounds_dev;           // chunk bounds on the walk, per chunk count
 };
 
 namespace {
@@ -737,23 +736,28 @@ int pair_tc_build(Context &c)
         return set_error(GD_ERR_CUDA, "pair weight table: unit gain not finite");
     }
     pt->imax1 = m1;
-    // work of one octant's pass over the class boxes D (the pair sum s = D of
-    // octant 0 stands for all eight, whose work is the same)
-    pt->walk_prefix.assign((size_t)d.nxyz + 1, 0);
+    // work along the walk (class box by class box, the reflections of each
+    // box's pair sum in turn; repeated reflections are empty)
+    pt->walk_prefix.assign((size_t)8 * d.nxyz + 1, 0);
     int64_t acc = 0;
     for (int Did = 0; Did < d.nxyz; Did++) {
         const int Dz = Did % d.nz, Dy = (Did / d.nz) % d.ny, Dx = Did / d.nyz;
-        const int64_t sl = ((int64_t)Dx * d.sy + Dy) * d.sz + Dz;
-        pt->walk_prefix[Did] = acc;
-        acc += c.s_work_prefix[sl + 1] - c.s_work_prefix[sl];
+        for (int r = 0; r < 8; r++) {
+            pt->walk_prefix[(size_t)8 * Did + r] = acc;
+            if (((r & 1) && Dx == d.nx - 1) || ((r & 2) && Dy == d.ny - 1) || ((r & 4) && Dz == d.nz - 1)) continue;
+            const int sx = (r & 1) ? 2 * d.nx - 2 - Dx : Dx, sy = (r & 2) ? 2 * d.ny - 2 - Dy : Dy,
+                      sz = (r & 4) ? 2 * d.nz - 2 - Dz : Dz;
+            const int64_t sl = ((int64_t)sx * d.sy + sy) * d.sz + sz;
+            acc += c.s_work_prefix[sl + 1] - c.s_work_prefix[sl];
+        }
     }
-    pt->walk_prefix[d.nxyz] = acc;
+    pt->walk_prefix[(size_t)8 * d.nxyz] = acc;
     return GD_OK;
 }
 
 namespace {
 
-// Work-balanced D-range bounds, uploaded once per range count.
+// Work-balanced chunk bounds on the walk, uploaded once per chunk count.
 int pt_bounds_device(Context &c, int nchunks, const int **out)
 {
     PairTc &pt = *c.pair_tc;
@@ -800,13 +804,16 @@ int pair_tc_take_timeout(Context &c, cudaStream_t st, bool *timed_out)
 
 namespace {
 
-// D ranges of one grid's walk for ncells cells (each run in all eight
-// octants): about four waves of one CTA per SM
+// Chunks of one grid's walk for ncells cells: about sixteen waves of one CTA
+// per SM.  The work estimate of a box is rough, and a chunk of the walk holds
+// few boxes, so units of equal estimated work end unevenly; sixteen waves
+// keep the tail short (20^3, 4096 cells: 468 ms against 481 ms with four;
+// 24^3, 1024 cells: 392 against 454 ms).
 int pt_chunks(const Context &c, int ncells)
 {
     const int tiles = (ncells + PT_BM - 1) / PT_BM;
     const int sms = std::max(1, c.sm_count);
-    return (int)std::min<int64_t>(std::max(1, (4 * sms + 8 * tiles - 1) / (8 * tiles)), c.d.nxyz);
+    return (int)std::min<int64_t>(std::max(1, (16 * sms + tiles - 1) / tiles), c.d.ns);
 }
 
 // Cell tiles whose units run together: the accumulators they share (8 bytes
@@ -821,14 +828,13 @@ int pt_tile_group(const Context &c, int tiles)
 
 // The pair-product gain with the contraction on the tensor cores for one or
 // more grids (each with its own context, cells and output) in one launch:
-// each grid's walk over s is split into work-balanced D ranges, each run in
-// the eight octants, and every (grid, 128-cell tile, D range, octant) unit
-// adds its group sums into the grid's fixed-point accumulator, so the results
-// do not depend on how the units are spread over the CTAs and equal those of
-// separate launches bit for bit.  The
+// each grid's walk over s is split into work-balanced chunks, and every
+// (grid, 128-cell tile, chunk) unit adds its group sums into the grid's
+// fixed-point accumulator, so the results do not depend on how the units are
+// spread over the CTAs and equal those of separate launches bit for bit.  The
 // units are ordered by their work, largest first; within a grid by groups of
-// cell tiles whose accumulators fit L2 together, then by D range, octant and
-// tile (so that the CTAs in flight share weight rows in L2).  One
+// cell tiles whose accumulators fit L2 together, chunk-major inside a group
+// (tiles fastest, so that the CTAs in flight share weight rows in L2).  One
 // persistent CTA per SM pulls them from a device counter as it finishes its
 // previous unit.  The unit list is uploaded once per launch shape and cached
 // on the first job's context (a replayed graph reads it without a host copy);
@@ -855,7 +861,7 @@ int launch_pair_tc(const PtJob *jobs, int njobs, cudaStream_t st)
         const int tiles = (jobs[j].ncells + PT_BM - 1) / PT_BM;
         cells_pad[j] = tiles * PT_BM;
         chunks[j] = pt_chunks(c, jobs[j].ncells);
-        unit_cost[j] = (double)c.s_work_prefix[d.ns] / (8.0 * chunks[j]);
+        unit_cost[j] = (double)c.s_work_prefix[d.ns] / chunks[j];
         const int *d_bounds = nullptr;
         int rc = pt_bounds_device(c, chunks[j], &d_bounds);
         if (rc) return rc;
@@ -893,9 +899,7 @@ int launch_pair_tc(const PtJob *jobs, int njobs, cudaStream_t st)
             const int tiles = cells_pad[j] / PT_BM, grp = pt_tile_group(*jobs[j].c, tiles);
             for (int t0 = 0; t0 < tiles; t0 += grp)
                 for (int ch = 0; ch < chunks[j]; ch++)
-                    for (int oct = 0; oct < 8; oct++)
-                        for (int t = t0; t < std::min(tiles, t0 + grp); t++)
-                            units.push_back(make_int4(j, t, ch, oct));
+                    for (int t = t0; t < std::min(tiles, t0 + grp); t++) units.push_back(make_int4(j, t, ch, 0));
         }
         int4 *dev = nullptr;
         GD_CUDA(cudaMalloc(&dev, sizeof(int4) * units.size()));
