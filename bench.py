@@ -380,6 +380,9 @@ def run_ours(args):
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
                     "ms_per_step": ms_e2e / args.steps},
             "clocks": clk.summary(), "roofline": roof,
+            "peaks": {"bf16_tflops": peak["bf16"], "bf16_source": peak["bf16_source"],
+                      "fp32_fma_tflops": peak["fp32"], "fp64_fma_tflops": peak["fp64"],
+                      "fma_source": peak["fma_source"]},
             "plain": {"value": plain_value, "unit": UNIT, "ms_per_step": ms_plain / args.steps,
                       "gain": args.gain, "clocks": clk_plain.summary(),
                       "accuracy": cell_stats(gd, ctx, q_plain, q_ref, nc)}}
@@ -573,17 +576,19 @@ def gain_roofline(name, ctx, f0, nc, stream, flush, peak, reps):
         # triangle; issued: their 256 x 16 slices with a nonzero entry (one MMA
         # K step each; the all-zero slices are skipped)
         inf = ctx._info()
-        tiles, slices = inf["cmatrix_tiles"], inf["cmatrix_slices"]
+        tiles = inf["cmatrix_tiles"]
+        # one BF16 pass issues whole tiles (4 K steps each)
+        slices = inf["cmatrix_slices"] if name == "bf16x3" else 4 * tiles
         flop = 2.0 * ((nc + 127) // 128 * 128) * 256 * 16 * slices * (3 if name == "bf16x3" else 1)
         kernel, work = "cmatrix_gain_kernel (tcgen05)", \
             "MACs x 2 of the 128x256x16 MMA K steps issued (nonzero slices of the stored tiles of the block upper triangle of each symmetric G_i; x3 for bf16x3)"
         bound, pk, src = "tensor", peak["bf16"], peak["bf16_source"]
-        # DRAM bytes per launch: the collision matrices stream through once.  An
-        # ncu capture of the same kernel (CTA pairs, one pass) on 14^3 / 4096
-        # cells read and wrote 2.847 GB for 2.773 GB of stored matrix tiles
-        # (ratio 1.027); scaled here by the matrix bytes.
+        # DRAM bytes per launch: the collision matrices stream through about
+        # once.  An ncu capture of the BF16x3 kernel (CTA pairs) on 14^3 / 4096
+        # cells read and wrote 7.141 GB for 5.636 GB of stored matrix tiles
+        # (ratio 1.267); scaled here by the matrix bytes.
         g_bytes = tiles * 256 * 64 * 2 * (2 if name == "bf16x3" else 1)
-        traffic = 1.027 * g_bytes
+        traffic = 1.267 * g_bytes
         traffic_src = "ncu dram__bytes_read+write of a 14^3/4096-cell launch, scaled by collision-matrix bytes"
     ach = flop / g_avg / 1e12
     out = {"bound": bound, "kernel": kernel, "achieved": ach, "peak": pk, "unit": "TFLOP/s",

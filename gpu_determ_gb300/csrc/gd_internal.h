@@ -220,16 +220,15 @@ int ensure_scratch(Context &c, size_t bytes);
 // gd_step's nu / gain / Q buffers for the ones passed as NULL (gd_capi.cu)
 int step_buffers(Context &c, int ld, cudaStream_t st, float **nu, float **gain, double **q);
 
-// tensor-core GEMM (gd_mlp.cu): C[M][N] = (accumulate ? C : 0) + A B^T, A [M][K]
-// and B [N][K] K-major BF16 (K a multiple of 64), C FP32 with ldc % 4 == 0 and
-// 16-byte aligned rows.
-// stall_polls > 0 is the failure-detection test hook of gd_ctx_inject_timeout
-// (every CTA's bounded wait on a barrier nothing arrives at runs out).
-// k_chunk > 0 (a multiple of 64) splits K into launches of at most k_chunk,
-// whose FP32 results are added in order: the tensor cores then accumulate at
-// most k_chunk products per FP32 sum.
-int gemm_bf16_nt_f32(const void *A, int M, const void *B, int N, int K, float *C, int ldc, bool accumulate, int *err,
-                     cudaStream_t st, int stall_polls = 0, int k_chunk = 0);
+// tensor-core GEMM (gd_mlp.cu), one launch: C[M][N] = A_hi B_hi^T + A_hi B_lo^T
+// + A_lo B_hi^T, A [M][K] and B [N][K] K-major BF16 (K a multiple of 64), C
+// FP32 with ldc % 4 == 0 and 16-byte aligned rows.  The tensor cores sum at
+// most k_chunk (a multiple of 64) products per FP32 accumulation; the chunks
+// are added in FP32, in chunk order.  stall_polls > 0 is the
+// failure-detection test hook of gd_ctx_inject_timeout (every CTA's bounded
+// wait on a barrier nothing arrives at runs out).
+int gemm_bf16x3_nt_f32(const void *Ah, const void *Al, int M, const void *Bh, const void *Bl, int N, int K, float *C,
+                       int ldc, int *err, cudaStream_t st, int stall_polls, int k_chunk);
 // loss on the tensor cores when the context uses collision matrices
 // (gd_cmatrix.cu); GD_ERR_UNSUPPORTED when the layout does not allow it.
 int cmatrix_loss(gd_cmatrix *cm, const float *f, int ncells, int ld, float *nu, cudaStream_t st);

@@ -217,6 +217,179 @@ __global__ void __launch_bounds__(kGThreads, 1)
     }
 }
 
+// C[M][N] = A_hi B_hi^T + A_hi B_lo^T + A_lo B_hi^T (FP32) for K-major BF16
+// operands: the FP32-equivalent product of two BF16 hi/lo splits, in one
+// launch.  The tensor cores' FP32 accumulation loses bits over long sums, so
+// the K range runs in chunks of kchunk 64-column steps: each chunk goes into
+// one of two tensor-memory accumulators, and the epilogue adds the chunks, in
+// chunk order, into FP32 sums it holds in registers (one row and 128 columns
+// per thread).  One 128 x 128 tile per CTA; warp 0 issues TMA, warp 1 the
+// MMAs (three per 16-column K step), warps 2..5 the epilogue.  Every wait is
+// bounded.
+constexpr int XM = 128, XN = 128, XS = 3;
+constexpr uint32_t kXA = XM * GK * 2, kXB = XN * GK * 2, kXStage = 2 * kXA + 2 * kXB;  // 64 KB
+constexpr uint32_t kXIdesc = umma_idesc_bf16(XM, XN);
+constexpr size_t kX3Smem = XS * kXStage + 1024;
+
+struct Gemm3Args {
+    int M, N, K, kchunk;  // K and kchunk in elements (multiples of 64)
+    float *c;
+    int ldc;
+    int *err;
+    int stall_polls;  // failure-detection test hook, as in GemmArgs
+};
+
+__global__ void __launch_bounds__(kGThreads, 1)
+    gemm3_nt_kernel(const __grid_constant__ CUtensorMap tAh, const __grid_constant__ CUtensorMap tAl,
+                    const __grid_constant__ CUtensorMap tBh, const __grid_constant__ CUtensorMap tBl, Gemm3Args p)
+{
+    extern __shared__ __align__(1024) unsigned char dsmem[];
+    unsigned char *base = reinterpret_cast<unsigned char *>(
+        (reinterpret_cast<uintptr_t>(dsmem) + 1023) & ~static_cast<uintptr_t>(1023));
+    __shared__ __align__(8) uint64_t full_bar[XS], empty_bar[XS], accf_bar[2], acce_bar[2], stall_bar;
+    __shared__ uint32_t tmem_holder;
+    __shared__ int abort_flag;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int m0 = blockIdx.x * XM, n0 = blockIdx.y * XN;
+    const int num_k = p.K / GK, kcs = p.kchunk / GK;
+    const int nchunks = (num_k + kcs - 1) / kcs;
+
+    if (threadIdx.x == 0) abort_flag = *(volatile int *)p.err;
+    __syncthreads();
+    if (abort_flag) return;
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < XS; s++) {
+            mbar_init(smem_u32(&full_bar[s]), 1);
+            mbar_init(smem_u32(&empty_bar[s]), 1);
+        }
+        for (int b = 0; b < 2; b++) {
+            mbar_init(smem_u32(&accf_bar[b]), 1);
+            mbar_init(smem_u32(&acce_bar[b]), 4);  // the four epilogue warps
+        }
+        mbar_init(smem_u32(&stall_bar), 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 1) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_holder)),
+                     "r"(2 * XN)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    }
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = tmem_holder;
+
+    if (p.stall_polls > 0) {
+        // test hook: a bounded wait that must run out before anything is issued
+        if (threadIdx.x == 32) mbar_wait_limit(smem_u32(&stall_bar), 0u, p.err, (uint32_t)p.stall_polls);
+        __syncthreads();
+        if (threadIdx.x == 0) abort_flag = *(volatile int *)p.err;
+        __syncthreads();
+    }
+
+    if (abort_flag) {
+        // every thread skips the work alike and meets the barrier below
+    } else if (warp == 0) {
+        if (lane == 0) {
+            for (int k = 0; k < num_k; k++) {
+                const int s = k % XS;
+                const uint32_t ph = (uint32_t)(k / XS) & 1u;
+                if (!mbar_wait(smem_u32(&empty_bar[s]), ph ^ 1u, p.err)) break;
+                unsigned char *st = base + (size_t)s * kXStage;
+                const uint32_t fb = smem_u32(&full_bar[s]);
+                mbar_expect_tx(fb, kXStage);
+                tma_load_2d(smem_u32(st), &tAh, k * GK, m0, fb);
+                tma_load_2d(smem_u32(st + kXA), &tAl, k * GK, m0, fb);
+                tma_load_2d(smem_u32(st + 2 * kXA), &tBh, k * GK, n0, fb);
+                tma_load_2d(smem_u32(st + 2 * kXA + kXB), &tBl, k * GK, n0, fb);
+            }
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {
+            bool ok = true;
+            int k = 0;
+            for (int c = 0; ok && c < nchunks; c++) {
+                const int buf = c & 1;
+                if (!mbar_wait(smem_u32(&acce_bar[buf]), ((uint32_t)(c >> 1) & 1u) ^ 1u, p.err)) {
+                    ok = false;
+                    break;
+                }
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                const uint32_t d_tmem = tmem + (uint32_t)(buf * XN);
+                const int kend = min(num_k, k + kcs);
+                for (const int kbeg = k; k < kend; k++) {
+                    const int s = k % XS;
+                    if (!mbar_wait(smem_u32(&full_bar[s]), (uint32_t)(k / XS) & 1u, p.err)) {
+                        ok = false;
+                        break;
+                    }
+                    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                    const uint32_t st = smem_u32(base + (size_t)s * kXStage);
+                    const uint32_t aH = st, aL = st + kXA, bH = st + 2 * kXA, bL = st + 2 * kXA + kXB;
+#pragma unroll
+                    for (int kk = 0; kk < GK / 16; kk++) {
+                        const uint32_t off = (uint32_t)kk * 32u;
+                        umma_bf16(d_tmem, umma_desc(aH + off), umma_desc(bH + off), kXIdesc,
+                                  (k > kbeg || kk > 0) ? 1u : 0u);
+                        umma_bf16(d_tmem, umma_desc(aH + off), umma_desc(bL + off), kXIdesc, 1u);
+                        umma_bf16(d_tmem, umma_desc(aL + off), umma_desc(bH + off), kXIdesc, 1u);
+                    }
+                    umma_commit(smem_u32(&empty_bar[s]));
+                }
+                if (ok) umma_commit(smem_u32(&accf_bar[buf]));
+            }
+        }
+    } else {
+        const int quad = warp & 3;
+        const int m = m0 + quad * 32 + lane;
+        float sum[XN];
+#pragma unroll
+        for (int j = 0; j < XN; j++) sum[j] = 0.f;
+        bool ok = true;
+        for (int c = 0; ok && c < nchunks; c++) {
+            const int buf = c & 1;
+            bool w = true;
+            if (lane == 0) w = mbar_wait(smem_u32(&accf_bar[buf]), (uint32_t)(c >> 1) & 1u, p.err);
+            if (__shfl_sync(0xffffffffu, w ? 1 : 0, 0) == 0) {
+                ok = false;
+                break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const uint32_t taddr = tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(buf * XN);
+#pragma unroll
+            for (int c0 = 0; c0 < XN; c0 += 32) {
+                float v[32];
+                tmem_ld32(taddr + (uint32_t)c0, v);
+#pragma unroll
+                for (int j = 0; j < 32; j++) sum[c0 + j] += v[j];
+            }
+            asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+            __syncwarp();
+            if (lane == 0) mbar_arrive(smem_u32(&acce_bar[buf]));
+        }
+        if (ok && m < p.M) {
+            float *row = p.c + (size_t)m * p.ldc;
+#pragma unroll
+            for (int j = 0; j < XN; j += 4) {
+                const int n = n0 + j;
+                if (n + 4 <= p.N) {
+                    *reinterpret_cast<float4 *>(row + n) = make_float4(sum[j], sum[j + 1], sum[j + 2], sum[j + 3]);
+                } else {
+#pragma unroll
+                    for (int q = 0; q < 4; q++)
+                        if (n + q < p.N) row[n + q] = sum[j + q];
+                }
+            }
+        }
+    }
+    __syncthreads();
+    if (warp == 1) {
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * XN) : "memory");
+    }
+}
+
 // out[c][r] = in[r][c] for BF16 [R][C] (row strides ldi, ldo)
 __global__ void transpose_bf16_kernel(const bf16 *__restrict__ in, int R, int Cc, int ldi, bf16 *__restrict__ out,
                                       int ldo)
@@ -505,30 +678,27 @@ int pad64(int n) { return (n + 63) / 64 * 64; }
 
 }  // namespace
 
-// C[M][N] (FP32, row stride ldc) = (accumulate ? C : 0) + A B^T for K-major BF16
-// A [M][K] and B [N][K]; the collision-matrix path computes the loss with it.
-int gemm_bf16_nt_f32(const void *A, int M, const void *B, int N, int K, float *C, int ldc, bool accumulate, int *err,
-                     cudaStream_t st, int stall_polls, int k_chunk)
+// C[M][N] (FP32, row stride ldc) = A_hi B_hi^T + A_hi B_lo^T + A_lo B_hi^T for
+// K-major BF16 [M][K] and [N][K] operands, in one launch, the tensor cores
+// summing at most k_chunk products per FP32 accumulation (the chunks added in
+// FP32 in chunk order); the collision-matrix path computes the loss with it.
+int gemm_bf16x3_nt_f32(const void *Ah, const void *Al, int M, const void *Bh, const void *Bl, int N, int K, float *C,
+                       int ldc, int *err, cudaStream_t st, int stall_polls, int k_chunk)
 {
-    // one launch per K chunk: the tensor cores sum at most k_chunk products
-    // into one FP32 accumulator, and the chunks are added in FP32 by the
-    // epilogue (C += chunk, in chunk order)
-    const int kc = k_chunk > 0 ? k_chunk : K;
-    for (int k0 = 0; k0 < K; k0 += kc) {
-        GemmArgs a{};
-        a.M = M;
-        a.N = N;
-        a.K = std::min(kc, K - k0);
-        a.k0 = k0;
-        a.ldk = K;
-        a.err = err;
-        a.stall_polls = k0 == 0 ? stall_polls : 0;
-        a.c32 = C;
-        a.ld32 = ldc;
-        a.add = (accumulate || k0 > 0) ? C : nullptr;
-        const int rc = gemm_nt(EPI_NONE, static_cast<const bf16 *>(A), static_cast<const bf16 *>(B), a, st);
-        if (rc) return rc;
-    }
+    if (K % GK || K <= 0 || M <= 0 || N <= 0 || (ldc & 3) || k_chunk <= 0 || k_chunk % GK ||
+        (reinterpret_cast<uintptr_t>(C) & 15))
+        return set_error(GD_ERR_INVALID_ARG, "GEMM shape: K and the chunk multiples of 64, ldc a multiple of 4");
+    CUtensorMap tAh, tAl, tBh, tBl;
+    int rc = make_map(&tAh, static_cast<const bf16 *>(Ah), M, K, XM);
+    if (!rc) rc = make_map(&tAl, static_cast<const bf16 *>(Al), M, K, XM);
+    if (!rc) rc = make_map(&tBh, static_cast<const bf16 *>(Bh), N, K, XN);
+    if (!rc) rc = make_map(&tBl, static_cast<const bf16 *>(Bl), N, K, XN);
+    if (rc) return rc;
+    Gemm3Args a{M, N, K, k_chunk, C, ldc, err, stall_polls};
+    dim3 grid((M + XM - 1) / XM, (N + XN - 1) / XN);
+    GD_CUDA(cudaFuncSetAttribute(gemm3_nt_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kX3Smem));
+    gemm3_nt_kernel<<<grid, kGThreads, kX3Smem, st>>>(tAh, tAl, tBh, tBl, a);
+    GD_CUDA(cudaGetLastError());
     return GD_OK;
 }
 

@@ -804,16 +804,16 @@ int pair_tc_take_timeout(Context &c, cudaStream_t st, bool *timed_out)
 
 namespace {
 
-// Chunks of one grid's walk for ncells cells: about sixteen waves of one CTA
-// per SM.  The work estimate of a box is rough, and a chunk of the walk holds
-// few boxes, so units of equal estimated work end unevenly; sixteen waves
-// keep the tail short (20^3, 4096 cells: 468 ms against 481 ms with four;
-// 24^3, 1024 cells: 392 against 454 ms).
+// Chunks of one grid's walk for ncells cells: about 32 waves of one CTA per
+// SM.  The work estimate of a box is rough, and a chunk of the walk holds few
+// boxes, so units of equal estimated work end unevenly; many short units keep
+// the tail short (20^3, 4096 cells: 459 ms with 32 waves, 468 with 16, 481
+// with 4; 24^3, 1024 cells: 379, 392, 454 ms).
 int pt_chunks(const Context &c, int ncells)
 {
     const int tiles = (ncells + PT_BM - 1) / PT_BM;
     const int sms = std::max(1, c.sm_count);
-    return (int)std::min<int64_t>(std::max(1, (16 * sms + tiles - 1) / tiles), c.d.ns);
+    return (int)std::min<int64_t>(std::max(1, (32 * sms + tiles - 1) / tiles), c.d.ns);
 }
 
 // Cell tiles whose units run together: the accumulators they share (8 bytes

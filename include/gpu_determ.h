@@ -62,7 +62,8 @@ typedef struct {
     int64_t contraction_terms; /* nonzero-weight x pair-product terms per cell-eval */
     int64_t scatter_terms;     /* (s, g, sign) output updates per cell-eval */
     int64_t cmatrix_tiles;     /* stored 256 x 64 tiles of the collision matrices (0 without) */
-    int64_t cmatrix_slices;    /* 256 x 16 slices of those tiles with a nonzero entry: the MMA K steps issued */
+    int64_t cmatrix_slices;    /* 256 x 16 slices of those tiles with a nonzero entry: the MMA K steps
+                                  issued in GD_CMATRIX_BF16X3 mode (one BF16 pass issues whole tiles) */
 } gd_info;
 
 /* Library version (major*10000 + minor*100 + patch). */

@@ -113,3 +113,30 @@ def test_pair_tc_edge_cell_counts(cuda, gdlib, nc, ld):
     rel = float((out[:, :nc] - ref[:, :nc]).norm() / ref[:, :nc].norm())
     assert rel <= 2e-5, rel
     ctx.check()
+
+
+def test_pair_tc_fixed_point_scale_is_exact(cuda, gdlib):
+    """Each cell's outputs accumulate in 64-bit fixed point scaled by a power
+    of two set from its own max|f|: scaling a cell's f by 2^e shifts its scale
+    exponent by -2e, so its gain is the unscaled gain times 2^(2e), bit for
+    bit (while every value stays a normal float), and the other cells do not
+    change.  A cell with a non-finite f gets NaN outputs and leaves the others
+    untouched."""
+    torch = cuda
+    spec = gdlib.GridSpec(12, R=4.8)
+    ctx = gdlib.Context(spec)
+    nc = 160
+    f = torch.from_numpy(inputs.dirichlet_mixtures(spec.fill(), nc, seed=5)).cuda()
+    base = _gain(gdlib, ctx, gdlib.GAIN_PAIR_TC, f, nc, nc, torch)
+    g = f.clone()
+    g[:, 3] *= 2.0 ** 20
+    g[:, 7] *= 2.0 ** -8
+    g[5, 11] = float("nan")
+    g[9, 140] = float("inf")
+    out = _gain(gdlib, ctx, gdlib.GAIN_PAIR_TC, g, nc, nc, torch)
+    assert torch.equal(out[:, 3], base[:, 3] * 2.0 ** 40)
+    assert torch.equal(out[:, 7], base[:, 7] * 2.0 ** -16)
+    assert bool(torch.isnan(out[:, 11]).all()) and bool(torch.isnan(out[:, 140]).all())
+    keep = [c for c in range(nc) if c not in (3, 7, 11, 140)]
+    assert torch.equal(out[:, keep], base[:, keep])
+    ctx.check()
