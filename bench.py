@@ -428,13 +428,14 @@ def run_ours(args):
 def path_launches(name, ctx):
     """Kernel launches of the loss and of the gain on a gain path: the FP32
     loss kernel, or on the collision-matrix paths the BF16 conversion of f and
-    three K-chunked tensor-core GEMMs (256 columns of K per launch); the gain
-    kernel and its chunk reduction, or the conversion of f and the
-    collision-matrix kernel."""
-    if name in ("pair", "pair_tc"):
+    one tensor-core GEMM; the FP32 gain kernel and its chunk reduction, the
+    pair tensor-core kernel between its scale and conversion kernels, or the
+    conversion of f and the collision-matrix kernel."""
+    if name == "pair":
         return 1, 2
-    ns_k = (ctx.n_pnt + 63) // 64 * 64
-    return 1 + 3 * ((ns_k + 255) // 256), 2
+    if name == "pair_tc":
+        return 1, 3
+    return 2, 2
 
 
 def cell_stats(gd, ctx, q, q_ref, nc):

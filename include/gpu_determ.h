@@ -124,7 +124,7 @@ int gd_correction_basis(gd_ctx *ctx, float *basis, gd_stream stream);
  * in-sphere nodes (either output may be NULL), on the context's gain path:
  * GD_GAIN_PAIR computes both in FP32 (SIMT kernels); the collision-matrix
  * paths compute the gain on the tensor cores and, when ld is a multiple of
- * 4, the loss as three BF16 GEMMs (see gd_ctx_set_gain_path).  Replaces the
+ * 4, the loss as one BF16x3 GEMM (see gd_ctx_set_gain_path).  Replaces the
  * loss and gain stages of evolve_colisions (collision_integral.h:11-17,
  * collision_integral.cu:32-188, 587-648). */
 int gd_collision(gd_ctx *ctx, const float *f, int ncells, int ld, float *nu, float *gain,
@@ -178,8 +178,9 @@ int gd_ctx_check(gd_ctx *ctx, gd_stream stream);
  * GD_CMATRIX_BF16 rounds f and G to BF16 (relative error ~3e-4 on I);
  * GD_CMATRIX_BF16X3 splits both into BF16 hi + lo parts and sums
  * hi*hi + hi*lo + lo*hi (~4e-6).  With a context's gain path set to either
- * mode, its loss nu = B f also runs on the tensor cores (three BF16 GEMMs,
- * ~1e-5) when ld is a multiple of 4.  No reference counterpart: the reference
+ * mode, its loss nu = B f also runs on the tensor cores (B and f split into
+ * BF16 hi + lo, three products per K step in one launch, ~5e-6) when ld is
+ * a multiple of 4.  No reference counterpart: the reference
  * forms these matrices only implicitly in its gain loop
  * (collision_integral.cu:75-188). */
 typedef struct gd_cmatrix gd_cmatrix;

@@ -66,11 +66,12 @@ def test_step_with_cmatrix_gain_path(cuda, gdlib, path, tol):
 
 @pytest.mark.parametrize("n,R,ncells,ld", [(12, 4.8, 300, 300), (12, 4.8, 100, 103), (16, 4.8, 64, 64)])
 def test_tensor_core_loss(cuda, gdlib, n, R, ncells, ld):
-    """With collision matrices selected, nu = B f runs as three BF16 GEMMs
-    (hi/lo split).  The tensor cores' FP32 accumulation leaves nu slightly low
-    (mean relative bias ~8e-6 at 16^3, growing with the node count), so the
-    bound is 4e-5 per node and cell (the FP32 kernel meets 1e-5) and 2e-5 on
-    the mean; the FP64 projection restores exact conservation either way.  A
+    """With collision matrices selected, nu = B f runs on the tensor cores
+    (hi/lo split, B_hi f_hi + B_hi f_lo + B_lo f_hi in one launch, the K range
+    in chunks of 256 added in FP32).  The tensor cores' FP32 accumulation
+    leaves nu slightly low (mean relative bias ~1e-6 at 20^3), so the bound is
+    4e-5 per node and cell (the FP32 kernel meets 1e-5) and 2e-5 on the
+    mean; the FP64 projection restores exact conservation either way.  A
     leading dimension that is not a multiple of 4 falls back to the FP32 kernel
     (bitwise equal to the pair path's nu)."""
     torch = cuda
