@@ -99,12 +99,14 @@ struct CmParams {
     int ns;       // in-sphere nodes
     int ns_k;     // padded node count (multiple of BK)
     int ncells, ld;
-    const float *f;  // [ns_k][ldf] FP32 distribution in matrix order (epilogue)
+    const float *f;  // [8][ns_k][ldf] FP32 distribution in matrix order, per reflection (epilogue)
     int ldf;
     float *gain;     // [ns][ld]
     int *err;        // set to 1 when a wait times out
-    const int *node_off;     // [ns + 1] each node's range of stored tiles
-    const uint32_t *tiles;   // stored tiles, n << 16 | k, n-major then k within each node
+    const int *node_off;     // [orbits + 1] each orbit representative's range of stored tiles
+    const uint32_t *tiles;   // stored tiles (mask << 28 | n << 16 | k), n-major then k per representative
+    const int *orbit;        // [ns] node -> representative's slot << 3 | reflection
+    const int *order;        // [ns] the nodes in launch order (reflection-major)
     int m_tiles;             // cell tiles, padded to whole clusters (the grid's x extent)
     int chain;               // most stored tiles summed in one tensor-memory accumulation (even)
 };
@@ -185,9 +187,13 @@ __global__ void __launch_bounds__(kThreads, 1)
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = tmem_base_holder;
 
-    // one CTA per (cell tile, node); a pair holds adjacent cell tiles of one node
-    const int m_tile = blockIdx.x, node = blockIdx.y;
-    const int l0 = __ldg(p.node_off + node), cnt = __ldg(p.node_off + node + 1) - l0;
+    // one CTA per (cell tile, node); a pair holds adjacent cell tiles of one node.
+    // Node i = R(i0) for the representative i0 of its orbit under the lattice's
+    // reflections: G_i[a][b] = G_i0[R a][R b], so I_i(f) = I_i0(f o R), and the
+    // CTA contracts i0's stored tiles with the copy of f reflected by R.
+    const int m_tile = blockIdx.x, node = __ldg(p.order + blockIdx.y);
+    const int ob = __ldg(p.orbit + node), rep = ob >> 3, refl = ob & 7;
+    const int l0 = __ldg(p.node_off + rep), cnt = __ldg(p.node_off + rep + 1) - l0;
 
     if (warp == 0) {
         // ---- TMA producer (both CTAs; each fills its own stages) ---------------
@@ -211,10 +217,10 @@ __global__ void __launch_bounds__(kThreads, 1)
                     // this CTA's BN / CL rows of it
                     const int k = (int)tile_k(__ldg(tl + j + t));
                     unsigned char *ts = st + (size_t)t * kTileSlot;
-                    tma_load_2d(smem_u32(ts), &tmFh, k * BK, m_tile * BM, fb);
+                    tma_load_3d(smem_u32(ts), &tmFh, k * BK, m_tile * BM, refl, fb);
                     tma_load_3d(smem_u32(ts + kTileA), &tmGh, 0, (int)crank * (BN / CL), l0 + j + t, fb);
                     if (NPARTS == 2) {
-                        tma_load_2d(smem_u32(ts + kTileA + kTileBc), &tmFl, k * BK, m_tile * BM, fb);
+                        tma_load_3d(smem_u32(ts + kTileA + kTileBc), &tmFl, k * BK, m_tile * BM, refl, fb);
                         tma_load_3d(smem_u32(ts + 2 * kTileA + kTileBc), &tmGl, 0, (int)crank * (BN / CL),
                                     l0 + j + t, fb);
                     }
@@ -342,7 +348,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         // zero, so T[b] = 0 there and clamping b keeps every load in bounds
         // without a branch.  A group's values are requested as soon as the
         // previous group is folded, so they arrive while its MMAs run.
-        const float *fcell = p.f + (live ? cell : 0);
+        const float *fcell = p.f + (size_t)refl * p.ns_k * p.ldf + (live ? cell : 0);
         float fv[BN / 2];
         auto load_f = [&](int b0) {
 #pragma unroll
@@ -512,10 +518,17 @@ __global__ void assemble_b_kernel(Dims d, int ns_k, const uint32_t *__restrict__
 // rows in matrix order, fp[a][c] (leading dimension ldf), for the epilogue.
 __global__ void convert_f_kernel(const float *__restrict__ f, int ns, int ns_k, int ncells, int ld,
                                  const int *__restrict__ inv, __nv_bfloat16 *__restrict__ fh,
-                                 __nv_bfloat16 *__restrict__ fl, float *__restrict__ fp, int ldf)
+                                 __nv_bfloat16 *__restrict__ fl, float *__restrict__ fp, int ldf, int f_rows)
 {
     __shared__ float tile[32][33];
     const int a0 = blockIdx.x * 32, c0 = blockIdx.y * 32;
+    // blockIdx.z = R: the copy of f reflected by R (inv + R ns maps matrix
+    // index -> node R(inv[m])), stacked R-major
+    const int R = blockIdx.z;
+    inv += (size_t)R * ns;
+    fh += (size_t)R * f_rows * ns_k;
+    if (fl) fl += (size_t)R * f_rows * ns_k;
+    if (fp) fp += (size_t)R * ns_k * ldf;
     for (int r = threadIdx.y; r < 32; r += blockDim.y) {
         const int a = a0 + r, c = c0 + threadIdx.x;
         const float v = (a < ns && c < ncells) ? f[(size_t)__ldg(inv + a) * ld + c] : 0.f;
@@ -573,30 +586,62 @@ struct gd_cmatrix {
     int ns = 0, ns_k = 0;
     int tiles = 0;       // BN x BK tiles of one node's block upper triangle
     int cluster = 2;     // CTAs per MMA: 2 (CTA-pair MMA, M = 256 cells; the default) or 1
-    int64_t slots = 0;   // stored (not all-zero) tiles over all nodes
-    int64_t slices = 0;  // their 16-column slices with a nonzero entry (MMA K steps issued)
-    int *node_off = nullptr;    // [ns + 1] into list
-    uint32_t *list = nullptr;   // stored tiles per node, n << 16 | k
+    // matrices are stored for one representative per orbit of the nodes under
+    // the reflections of the lattice (x -> nx - 1 - x per symmetric axis)
+    int nreps = 0;       // orbit representatives (ns / 8 on a lattice symmetric in all three axes)
+    int nrefl = 1;       // reflections of f kept on the device: 8, or 1 without a symmetric axis
+    int *orbit = nullptr;  // [ns] rep slot << 3 | reflection bits (bit a: axis a mirrored)
+    int *order = nullptr;  // [ns] the gain kernel's launch order (reflection-major)
+    int64_t slots = 0;   // stored (not all-zero) tiles over the representatives
+    int64_t slices = 0;  // 16-column slices with a nonzero entry issued per launch (all nodes)
+    int *node_off = nullptr;    // [nreps + 1] into list
+    uint32_t *list = nullptr;   // stored tiles per representative, mask << 28 | n << 16 | k
     __nv_bfloat16 *gh = nullptr, *gl = nullptr;
-    __nv_bfloat16 *fh = nullptr, *fl = nullptr;  // f as [cell][matrix index] BF16 hi / lo
-    float *fp = nullptr;                         // f as [matrix index][cell] FP32 (epilogue)
+    // f per reflection R, stacked R-major: [R][cell][matrix index] BF16 hi / lo
+    // (f_cells rows per R) and [R][matrix index][cell] FP32 (epilogue)
+    __nv_bfloat16 *fh = nullptr, *fl = nullptr;
+    float *fp = nullptr;
     int f_cells = 0;
     // matrix order of the nodes: a 3-D Hilbert curve over the lattice, which
     // packs the nonzero entries of the G_i into fewer 256 x 64 tiles than
-    // the compact (i, j, k) order; inv[m] is the node at matrix index m,
-    // mnodes[m] its packed lattice coordinates
+    // the compact (i, j, k) order; inv[R ns + m] is the node R(node at matrix
+    // index m) (R = 0: the node itself), mnodes[m] its packed lattice
+    // coordinates
     int *inv = nullptr;
     uint32_t *mnodes = nullptr;
     __nv_bfloat16 *bh = nullptr, *bl = nullptr;  // loss matrix [node][ns_k] BF16 hi / lo
     int *err = nullptr;
     int stall_next = 0;  // gd_ctx_inject_timeout: polls for the next tensor-core loss GEMM
-    // stored tiles per tensor-memory accumulation of the gain, and 64-column K
-    // chunks per launch of the tensor-core loss (gd_cmatrix_set_chain)
+    // stored tiles per tensor-memory accumulation of the gain (gd_cmatrix_set_chain)
     int chain = gd::kChainUnlimited;
 };
 
 namespace gd {
 int ensure_f(gd_cmatrix *h, int ncells);
+
+// Axes along which the node set is symmetric (bit a: x_a -> n_a - 1 - x_a maps
+// every in-sphere node to an in-sphere node).  The weights depend on |g|,
+// |d| and whether s - i lies in the box, all invariant under these
+// reflections, so G_R(i)[R a][R b] = G_i[a][b] exactly.
+int lattice_reflections(const Context &c)
+{
+    const Dims &d = c.d;
+    std::vector<char> in(d.nxyz, 0);
+    for (int m = 0; m < d.n_pnt; m++) in[((size_t)c.ui[m] * d.ny + c.vi[m]) * d.nz + c.wi[m]] = 1;
+    int axes = 0;
+    const int n[3] = {d.nx, d.ny, d.nz};
+    for (int a = 0; a < 3; a++) {
+        if (n[a] & 1) continue;  // a middle plane would be its own mirror
+        bool sym = true;
+        for (int m = 0; sym && m < d.n_pnt; m++) {
+            int x[3] = {c.ui[m], c.vi[m], c.wi[m]};
+            x[a] = n[a] - 1 - x[a];
+            sym = in[((size_t)x[0] * d.ny + x[1]) * d.nz + x[2]] != 0;
+        }
+        if (sym) axes |= 1 << a;
+    }
+    return axes;
+}
 
 // Index of (x, y, z) along a 3-D Hilbert curve through the 2^bits cube
 // (Skilling's transpose algorithm: "Programming the Hilbert curve", AIP Conf.
@@ -683,17 +728,66 @@ extern "C" int gd_cmatrix_create(gd_ctx *ctx, int mode, gd_cmatrix **out)
     for (int n = 0; n < num_n; n++)
         for (int k = 0; k < k_end(n, num_k); k++) tile_nk.push_back(make_int2(n, k));
     h->tiles = (int)tile_nk.size();
-    const size_t ntri = (size_t)h->ns * h->tiles;  // triangle tiles over all nodes
+    // orbits of the nodes under the lattice's reflections: the representative
+    // of node x mirrors every symmetric axis with x_a >= n_a / 2 (n_a is even,
+    // so no node is its own mirror and every orbit has 2^axes nodes)
+    const int axes = lattice_reflections(c);
+    h->nrefl = axes ? 8 : 1;
+    const int nax[3] = {d.nx, d.ny, d.nz};
+    std::vector<int> box_map(d.nxyz, -1);
+    for (int m = 0; m < h->ns; m++) box_map[((size_t)c.ui[m] * d.ny + c.vi[m]) * d.nz + c.wi[m]] = m;
+    auto reflect = [&](int m, int R) {
+        int x[3] = {c.ui[m], c.vi[m], c.wi[m]};
+        for (int a = 0; a < 3; a++)
+            if ((R >> a) & 1) x[a] = nax[a] - 1 - x[a];
+        return box_map[((size_t)x[0] * d.ny + x[1]) * d.nz + x[2]];
+    };
+    std::vector<int> orbit(h->ns), rep_slot(h->ns, -1), order(h->ns);
+    std::vector<uint32_t> rep_nodes;
+    std::vector<int> orbit_size;
+    for (int m = 0; m < h->ns; m++) {
+        int R = 0;
+        for (int a = 0; a < 3; a++) {
+            const int xa = a == 0 ? c.ui[m] : a == 1 ? c.vi[m] : c.wi[m];
+            if (((axes >> a) & 1) && 2 * xa >= nax[a]) R |= 1 << a;
+        }
+        const int r = reflect(m, R);
+        if (rep_slot[r] < 0) {
+            rep_slot[r] = (int)rep_nodes.size();
+            rep_nodes.push_back((uint32_t)c.ui[r] | ((uint32_t)c.vi[r] << 10) | ((uint32_t)c.wi[r] << 20));
+            orbit_size.push_back(0);
+        }
+        orbit[m] = rep_slot[r] << 3 | R;
+        orbit_size[rep_slot[r]]++;
+    }
+    h->nreps = (int)rep_nodes.size();
+    // launch order: reflection-major, so that the CTAs in flight read one
+    // reflected copy of f (60 MB at 20^3 / 4096 cells, L2-resident) rather
+    // than all eight; each representative's tiles are then read once per
+    // reflection (reflection-minor order ran 13 % slower)
+    for (int m = 0; m < h->ns; m++) order[m] = m;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+        return ((orbit[a] & 7) << 24 | orbit[a] >> 3) < ((orbit[b] & 7) << 24 | orbit[b] >> 3);
+    });
+    const size_t ntri = (size_t)h->nreps * h->tiles;  // triangle tiles over the representatives
     float *w = nullptr;
     int2 *d_tiles = nullptr;
     uint8_t *d_nz = nullptr;
     int *d_slot = nullptr;
+    uint32_t *d_reps = nullptr;
     const size_t na = (size_t)d.hx * d.nx * d.hy * d.hz * d.nyz;
     const int64_t work = (int64_t)ntri * BN * (BK / 8);
     const int blocks = (int)std::min<int64_t>((work + 255) / 256, (int64_t)c.sm_count * 64);
     int rc = GD_OK;
-    cudaError_t e = cudaMalloc(&h->inv, sizeof(int) * h->ns);
+    cudaError_t e = cudaMalloc(&h->inv, sizeof(int) * h->ns * h->nrefl);
     if (e == cudaSuccess) e = cudaMalloc(&h->mnodes, sizeof(uint32_t) * h->ns);
+    if (e == cudaSuccess) e = cudaMalloc(&h->orbit, sizeof(int) * h->ns);
+    if (e == cudaSuccess) e = cudaMalloc(&h->order, sizeof(int) * h->ns);
+    if (e == cudaSuccess) e = cudaMalloc(&d_reps, sizeof(uint32_t) * h->nreps);
+    if (e == cudaSuccess) e = cudaMemcpy(h->orbit, orbit.data(), sizeof(int) * h->ns, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(h->order, order.data(), sizeof(int) * h->ns, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+        e = cudaMemcpy(d_reps, rep_nodes.data(), sizeof(uint32_t) * h->nreps, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMalloc(&h->err, sizeof(int));
     if (e == cudaSuccess) e = cudaMalloc(&w, na * sizeof(float));
     if (e == cudaSuccess) e = cudaMalloc(&d_tiles, sizeof(int2) * tile_nk.size());
@@ -704,17 +798,16 @@ extern "C" int gd_cmatrix_create(gd_ctx *ctx, int mode, gd_cmatrix **out)
     if (!rc) rc = launch_dense_tables(d, nullptr, w, nullptr);
     // the matrix order of the nodes: of the lattice's placements inside the
     // Hilbert cube, the one whose matrices store the fewest tiles, counted on
-    // a sample of output nodes (the same for every placement)
+    // a sample of representatives (the same for every placement)
     std::vector<int> inv;
     std::vector<uint32_t> mnodes;
     if (!rc) {
         const int span = (1 << hilbert_bits(d)) - std::max(d.nx, std::max(d.ny, d.nz));
-        const int nsample = std::min(h->ns, 128);
-        std::vector<uint32_t> sample(nsample), h_nodes(h->ns);
+        const int nsample = std::min(h->nreps, 128);
+        std::vector<uint32_t> sample(nsample);
         uint32_t *d_sample = nullptr;
-        e = cudaMemcpy(h_nodes.data(), c.d_nodes, sizeof(uint32_t) * h->ns, cudaMemcpyDeviceToHost);
-        for (int k = 0; k < nsample; k++) sample[k] = h_nodes[(size_t)k * h->ns / nsample];
-        if (e == cudaSuccess) e = cudaMalloc(&d_sample, sizeof(uint32_t) * nsample);
+        for (int k = 0; k < nsample; k++) sample[k] = rep_nodes[(size_t)k * h->nreps / nsample];
+        e = cudaMalloc(&d_sample, sizeof(uint32_t) * nsample);
         if (e == cudaSuccess)
             e = cudaMemcpy(d_sample, sample.data(), sizeof(uint32_t) * nsample, cudaMemcpyHostToDevice);
         const size_t nsz = (size_t)nsample * h->tiles * kSlices;
@@ -746,7 +839,13 @@ extern "C" int gd_cmatrix_create(gd_ctx *ctx, int mode, gd_cmatrix **out)
             }
         }
         cudaFree(d_sample);
-        if (e == cudaSuccess) e = cudaMemcpy(h->inv, inv.data(), sizeof(int) * h->ns, cudaMemcpyHostToDevice);
+        // inv per reflection R: the node R(inv[m]) at matrix index m
+        std::vector<int> inv_r((size_t)h->ns * h->nrefl);
+        for (int R = 0; R < h->nrefl; R++)
+            for (int m = 0; m < h->ns; m++)
+                inv_r[(size_t)R * h->ns + m] = (R & ~axes) ? inv[m] : reflect(inv[m], R);
+        if (e == cudaSuccess)
+            e = cudaMemcpy(h->inv, inv_r.data(), sizeof(int) * inv_r.size(), cudaMemcpyHostToDevice);
         if (e == cudaSuccess)
             e = cudaMemcpy(h->mnodes, mnodes.data(), sizeof(uint32_t) * h->ns, cudaMemcpyHostToDevice);
         if (e == cudaSuccess) e = cudaMemset(d_nz, 0, ntri * kSlices);
@@ -755,30 +854,31 @@ extern "C" int gd_cmatrix_create(gd_ctx *ctx, int mode, gd_cmatrix **out)
     // pass 1: which triangle tiles hold a nonzero entry
     std::vector<uint8_t> nz(ntri * kSlices);
     if (!rc) {
-        assemble_g_kernel<<<blocks, 256>>>(d, h->ns, h->tiles, d_tiles, c.d_nodes, h->mnodes, w, d_nz, nullptr,
+        assemble_g_kernel<<<blocks, 256>>>(d, h->nreps, h->tiles, d_tiles, d_reps, h->mnodes, w, d_nz, nullptr,
                                            nullptr, nullptr);
         e = cudaGetLastError();
         if (e == cudaSuccess) e = cudaMemcpy(nz.data(), d_nz, ntri * kSlices, cudaMemcpyDeviceToHost);
         if (e != cudaSuccess) rc = cuda_error(e, "collision-matrix tile scan");
     }
-    // per-node lists of the stored tiles (n-major, k ascending) and their slots
-    std::vector<int> node_off(h->ns + 1, 0), slot_of(ntri, -1);
+    // per-representative lists of the stored tiles (n-major, k ascending) and
+    // their slots; every node of an orbit issues its representative's slices
+    std::vector<int> node_off(h->nreps + 1, 0), slot_of(ntri, -1);
     std::vector<uint32_t> list;
     if (!rc) {
-        for (int i = 0; i < h->ns; i++) {
+        for (int i = 0; i < h->nreps; i++) {
             node_off[i] = (int)list.size();
             for (int t = 0; t < h->tiles; t++) {
                 uint32_t mask = 0;
                 for (int q = 0; q < kSlices; q++)
                     if (nz[((size_t)i * h->tiles + t) * kSlices + q]) mask |= 1u << q;
                 if (mask) {
-                    h->slices += __builtin_popcount(mask);
+                    h->slices += (int64_t)__builtin_popcount(mask) * orbit_size[i];
                     slot_of[(size_t)i * h->tiles + t] = (int)list.size();
                     list.push_back(mask << 28 | ((uint32_t)tile_nk[t].x << 16) | (uint32_t)tile_nk[t].y);
                 }
             }
         }
-        node_off[h->ns] = (int)list.size();
+        node_off[h->nreps] = (int)list.size();
         h->slots = (int64_t)list.size();
     }
     const size_t elems = (size_t)h->slots * BN * BK;
@@ -813,8 +913,8 @@ extern "C" int gd_cmatrix_create(gd_ctx *ctx, int mode, gd_cmatrix **out)
     }
     // pass 2: the stored tiles, and the loss matrix
     if (!rc) {
-        assemble_g_kernel<<<blocks, 256>>>(d, h->ns, h->tiles, d_tiles, c.d_nodes, h->mnodes, w, nullptr, d_slot, h->gh,
-                                           h->gl);
+        assemble_g_kernel<<<blocks, 256>>>(d, h->nreps, h->tiles, d_tiles, d_reps, h->mnodes, w, nullptr, d_slot,
+                                           h->gh, h->gl);
         e = cudaGetLastError();
         const size_t nb = (size_t)h->ns * h->ns_k;
         if (e == cudaSuccess) e = cudaMalloc(&h->bh, nb * 2);
@@ -832,6 +932,7 @@ extern "C" int gd_cmatrix_create(gd_ctx *ctx, int mode, gd_cmatrix **out)
     cudaFree(d_tiles);
     cudaFree(d_nz);
     cudaFree(d_slot);
+    cudaFree(d_reps);
     if (rc) {
         cudaFree(h->bh);
         cudaFree(h->bl);
@@ -842,6 +943,8 @@ extern "C" int gd_cmatrix_create(gd_ctx *ctx, int mode, gd_cmatrix **out)
         cudaFree(h->err);
         cudaFree(h->inv);
         cudaFree(h->mnodes);
+        cudaFree(h->orbit);
+        cudaFree(h->order);
         delete h;
         return rc;
     }
@@ -880,6 +983,8 @@ extern "C" int gd_cmatrix_destroy(gd_cmatrix *h)
     cudaFree(h->err);
     cudaFree(h->inv);
     cudaFree(h->mnodes);
+    cudaFree(h->orbit);
+    cudaFree(h->order);
     delete h;
     return GD_OK;
 }
@@ -893,27 +998,29 @@ extern "C" int gd_cmatrix_gain(gd_cmatrix *h, const float *f, int ncells, int ld
     const bool split = h->mode == GD_CMATRIX_BF16X3;
     int rc0 = gd::ensure_f(h, ncells);
     if (rc0) return rc0;
-    dim3 cb(32, 8), cg((h->ns_k + 31) / 32, (ncells + 31) / 32);
+    dim3 cb(32, 8), cg((h->ns_k + 31) / 32, (ncells + 31) / 32, h->nrefl);
     convert_f_kernel<<<cg, cb, 0, st>>>(f, h->ns, h->ns_k, ncells, ld, h->inv, h->fh, split ? h->fl : nullptr, h->fp,
-                                        h->f_cells);
+                                        h->f_cells, h->f_cells);
     GD_CUDA(cudaGetLastError());
 
     EncodeTiled enc;
     int rc = get_encoder(&enc);
     if (rc) return rc;
     CUtensorMap tFh, tFl, tGh, tGl;
-    const cuuint64_t fdims[2] = {(cuuint64_t)h->ns_k, (cuuint64_t)ncells};
-    const cuuint64_t fstr[1] = {(cuuint64_t)h->ns_k * 2};
-    const cuuint32_t fbox[2] = {BK, BM};
+    // f per reflection: [R][cell][matrix index], f_cells rows per R (cells past
+    // ncells read as zeros)
+    const cuuint64_t fdims[3] = {(cuuint64_t)h->ns_k, (cuuint64_t)ncells, (cuuint64_t)h->nrefl};
+    const cuuint64_t fstr[2] = {(cuuint64_t)h->ns_k * 2, (cuuint64_t)h->f_cells * h->ns_k * 2};
+    const cuuint32_t fbox[3] = {BK, BM, 1};
     const cuuint64_t gdims[3] = {(cuuint64_t)BK, (cuuint64_t)BN, (cuuint64_t)std::max<int64_t>(h->slots, 1)};
     const cuuint64_t gstr[2] = {(cuuint64_t)BK * 2, (cuuint64_t)BN * BK * 2};
     // with a CTA pair each CTA loads half of a G tile
     const int cl = (h->cluster == 2 && ncells > BM) ? 2 : 1;
     const cuuint32_t gbox[3] = {BK, (cuuint32_t)(BN / cl), 1};
-    if ((rc = encode(enc, &tFh, h->fh, 2, fdims, fstr, fbox))) return rc;
+    if ((rc = encode(enc, &tFh, h->fh, 3, fdims, fstr, fbox))) return rc;
     if ((rc = encode(enc, &tGh, h->gh, 3, gdims, gstr, gbox))) return rc;
     if (split) {
-        if ((rc = encode(enc, &tFl, h->fl, 2, fdims, fstr, fbox))) return rc;
+        if ((rc = encode(enc, &tFl, h->fl, 3, fdims, fstr, fbox))) return rc;
         if ((rc = encode(enc, &tGl, h->gl, 3, gdims, gstr, gbox))) return rc;
     } else {
         tFl = tFh;
@@ -921,7 +1028,8 @@ extern "C" int gd_cmatrix_gain(gd_cmatrix *h, const float *f, int ncells, int ld
     }
     // cell tiles padded to whole clusters: a tile past ncells reads zeros and stores nothing
     const int m_tiles = ((ncells + BM - 1) / BM + cl - 1) / cl * cl;
-    CmParams prm{h->ns, h->ns_k, ncells, ld, h->fp, h->f_cells, gain, h->err, h->node_off, h->list, m_tiles, h->chain};
+    CmParams prm{h->ns,     h->ns_k,  ncells,   ld,       h->fp,    h->f_cells, gain,
+                 h->err,    h->node_off, h->list, h->orbit, h->order, m_tiles,  h->chain};
     // one CTA per (cell tile, node), cell tiles fastest so that the CTAs in flight
     // share a few nodes' matrix tiles in L2 (a persistent grid of one CTA per SM
     // taking the tiles round-robin measured 3-4 % slower at 20^3 / 4096 cells)
@@ -1001,22 +1109,23 @@ int ensure_f(gd_cmatrix *h, int ncells)
     h->fh = h->fl = nullptr;
     h->fp = nullptr;
     h->f_cells = 0;
-    GD_CUDA(cudaMalloc(&h->fh, (size_t)ncells * h->ns_k * 2));
-    GD_CUDA(cudaMalloc(&h->fl, (size_t)ncells * h->ns_k * 2));
-    GD_CUDA(cudaMalloc(&h->fp, (size_t)ncells * h->ns_k * 4));
+    const size_t per = (size_t)ncells * h->ns_k * h->nrefl;  // one copy of f per reflection
+    GD_CUDA(cudaMalloc(&h->fh, per * 2));
+    GD_CUDA(cudaMalloc(&h->fl, per * 2));
+    GD_CUDA(cudaMalloc(&h->fp, per * 4));
     h->f_cells = ncells;
     return GD_OK;
 }
 
-// nu = B f as three tensor-core GEMMs, B_hi f_hi + B_hi f_lo + B_lo f_hi
-// (the BF16 split keeps ~16 significant bits of both factors).
+// nu = B f on the tensor cores, B_hi f_hi + B_hi f_lo + B_lo f_hi in one
+// launch (the BF16 split keeps ~16 significant bits of both factors).
 int cmatrix_loss(gd_cmatrix *h, const float *f, int ncells, int ld, float *nu, cudaStream_t st)
 {
     if (!h->bh || (ld & 3) || (reinterpret_cast<uintptr_t>(nu) & 15)) return GD_ERR_UNSUPPORTED;
     int rc = ensure_f(h, ncells);
     if (rc) return rc;
-    dim3 cb(32, 8), cg((h->ns_k + 31) / 32, (ncells + 31) / 32);
-    convert_f_kernel<<<cg, cb, 0, st>>>(f, h->ns, h->ns_k, ncells, ld, h->inv, h->fh, h->fl, nullptr, 0);
+    dim3 cb(32, 8), cg((h->ns_k + 31) / 32, (ncells + 31) / 32, 1);  // f itself (R = 0)
+    convert_f_kernel<<<cg, cb, 0, st>>>(f, h->ns, h->ns_k, ncells, ld, h->inv, h->fh, h->fl, nullptr, 0, h->f_cells);
     GD_CUDA(cudaGetLastError());
     const int stall = h->stall_next;  // a pending time-out injection fires here, once
     h->stall_next = 0;
@@ -1035,7 +1144,10 @@ double cmatrix_bytes_bound(const Context &c, int mode)
     const int num_n = (ns + BN - 1) / BN, num_k = ns_k / BK;
     int64_t tiles = 0;
     for (int n = 0; n < num_n; n++) tiles += k_end(n, num_k);
-    return (double)tiles * ns * BN * BK * 2.0 * (mode == GD_CMATRIX_BF16X3 ? 2.0 : 1.0);
+    // matrices of one representative per orbit of the reflections
+    const int axes = lattice_reflections(c);
+    const double reps = (double)ns / (double)(1 << __builtin_popcount(axes));
+    return (double)tiles * reps * BN * BK * 2.0 * (mode == GD_CMATRIX_BF16X3 ? 2.0 : 1.0);
 }
 
 int encode_bf16_sw128(CUtensorMap *m, void *ptr, int rank, const uint64_t *dims, const uint64_t *strides,
