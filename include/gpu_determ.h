@@ -173,8 +173,11 @@ int gd_ctx_check(gd_ctx *ctx, gd_stream stream);
  * collision matrices G_i assembled on the GPU from the analytic weights and
  * contracted on the tcgen05 tensor cores with FP32 accumulation.  G_i is
  * symmetric, so only the 256 x 64 tiles of its block upper triangle that hold
- * a nonzero entry are stored (off-diagonal entries doubled): 1.39 M tiles,
- * 45.5 GB in BF16 at 20^3 (R = 4.8), twice that for GD_CMATRIX_BF16X3.
+ * a nonzero entry are stored (off-diagonal entries doubled), and only for one
+ * node per orbit of the lattice's reflections (x_a -> n_a - 1 - x_a on each
+ * axis along which the node set is symmetric): node R(i) uses G_i with f
+ * reflected by R.  At 20^3 (R = 4.8) that is ~5 GB in BF16, twice that for
+ * GD_CMATRIX_BF16X3 (8x less than one matrix per node).
  * GD_CMATRIX_BF16 rounds f and G to BF16 (relative error ~3e-4 on I);
  * GD_CMATRIX_BF16X3 splits both into BF16 hi + lo parts and sums
  * hi*hi + hi*lo + lo*hi (~4e-6).  With a context's gain path set to either
