@@ -577,18 +577,20 @@ def gain_roofline(name, ctx, f0, nc, stream, flush, peak, reps):
         # triangle; issued: their 256 x 16 slices with a nonzero entry (one MMA
         # K step each; the all-zero slices are skipped)
         inf = ctx._info()
-        tiles = inf["cmatrix_tiles"]
-        # one BF16 pass issues whole tiles (4 K steps each)
-        slices = inf["cmatrix_slices"] if name == "bf16x3" else 4 * tiles
+        tiles = inf["cmatrix_tiles"]  # stored (one matrix per orbit of the lattice's reflections)
+        # issued over every node; one BF16 pass issues whole tiles (4 K steps each)
+        slices = inf["cmatrix_slices"] if name == "bf16x3" else 4 * inf["cmatrix_node_tiles"]
         flop = 2.0 * ((nc + 127) // 128 * 128) * 256 * 16 * slices * (3 if name == "bf16x3" else 1)
         kernel, work = "cmatrix_gain_kernel (tcgen05)", \
             "MACs x 2 of the 128x256x16 MMA K steps issued (nonzero slices of the stored tiles of the block upper triangle of each symmetric G_i; x3 for bf16x3)"
         bound, pk, src = "tensor", peak["bf16"], peak["bf16_source"]
-        # DRAM bytes per launch: the collision matrices stream through about
-        # once.  An ncu capture of the BF16x3 kernel (CTA pairs) on 14^3 / 4096
-        # cells read and wrote 7.141 GB for 5.636 GB of stored matrix tiles
-        # (ratio 1.267); scaled here by the matrix bytes.
-        g_bytes = tiles * 256 * 64 * 2 * (2 if name == "bf16x3" else 1)
+        # DRAM bytes per launch: every node's matrix tiles stream through about
+        # once (a representative's tiles once per reflection: the launch runs
+        # reflection-major).  An ncu capture of the BF16x3 kernel (CTA pairs,
+        # one matrix per node) on 14^3 / 4096 cells read and wrote 7.141 GB for
+        # 5.636 GB of matrix tiles (ratio 1.267); scaled here by the tile bytes
+        # the nodes stream.
+        g_bytes = inf["cmatrix_node_tiles"] * 256 * 64 * 2 * (2 if name == "bf16x3" else 1)
         traffic = 1.267 * g_bytes
         traffic_src = "ncu dram__bytes_read+write of a 14^3/4096-cell launch, scaled by collision-matrix bytes"
     ach = flop / g_avg / 1e12

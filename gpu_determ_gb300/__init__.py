@@ -62,7 +62,7 @@ class _Info(C.Structure):
                 ("nonzero_weights", C.c_int64), ("table_a_elems", C.c_int64),
                 ("pair_products", C.c_int64), ("contraction_terms", C.c_int64),
                 ("scatter_terms", C.c_int64), ("cmatrix_tiles", C.c_int64),
-                ("cmatrix_slices", C.c_int64)]
+                ("cmatrix_slices", C.c_int64), ("cmatrix_node_tiles", C.c_int64)]
 
 
 class _PairSizes(C.Structure):

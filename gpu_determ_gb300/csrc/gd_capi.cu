@@ -497,6 +497,7 @@ int gd_ctx_info(const gd_ctx *ctx, gd_info *out)
     out->scatter_terms = ctx->c.scatter_terms;
     out->cmatrix_tiles = gd::cmatrix_stored_tiles(ctx->c.cmatrix);
     out->cmatrix_slices = gd::cmatrix_issued_slices(ctx->c.cmatrix);
+    out->cmatrix_node_tiles = gd::cmatrix_node_tiles(ctx->c.cmatrix);
     return GD_OK;
 }
 

@@ -593,7 +593,8 @@ struct gd_cmatrix {
     int *orbit = nullptr;  // [ns] rep slot << 3 | reflection bits (bit a: axis a mirrored)
     int *order = nullptr;  // [ns] the gain kernel's launch order (reflection-major)
     int64_t slots = 0;   // stored (not all-zero) tiles over the representatives
-    int64_t slices = 0;  // 16-column slices with a nonzero entry issued per launch (all nodes)
+    int64_t slices = 0;  // 16-column slices with a nonzero entry issued per cell tile (all nodes)
+    int64_t node_tiles = 0;  // stored tiles issued per cell tile (all nodes)
     int *node_off = nullptr;    // [nreps + 1] into list
     uint32_t *list = nullptr;   // stored tiles per representative, mask << 28 | n << 16 | k
     __nv_bfloat16 *gh = nullptr, *gl = nullptr;
@@ -873,6 +874,7 @@ extern "C" int gd_cmatrix_create(gd_ctx *ctx, int mode, gd_cmatrix **out)
                     if (nz[((size_t)i * h->tiles + t) * kSlices + q]) mask |= 1u << q;
                 if (mask) {
                     h->slices += (int64_t)__builtin_popcount(mask) * orbit_size[i];
+                    h->node_tiles += orbit_size[i];
                     slot_of[(size_t)i * h->tiles + t] = (int)list.size();
                     list.push_back(mask << 28 | ((uint32_t)tile_nk[t].x << 16) | (uint32_t)tile_nk[t].y);
                 }
@@ -1137,6 +1139,7 @@ int cmatrix_loss(gd_cmatrix *h, const float *f, int ncells, int ld, float *nu, c
 
 int64_t cmatrix_stored_tiles(const gd_cmatrix *cm) { return cm ? cm->slots : 0; }
 int64_t cmatrix_issued_slices(const gd_cmatrix *cm) { return cm ? cm->slices : 0; }
+int64_t cmatrix_node_tiles(const gd_cmatrix *cm) { return cm ? cm->node_tiles : 0; }
 
 double cmatrix_bytes_bound(const Context &c, int mode)
 {

@@ -238,6 +238,7 @@ int run_loss_path(Context &c, const float *f, int ncells, int ld, float *nu, cud
 // stored tiles of a context's collision matrices (0 for NULL)
 int64_t cmatrix_stored_tiles(const gd_cmatrix *cm);
 int64_t cmatrix_issued_slices(const gd_cmatrix *cm);
+int64_t cmatrix_node_tiles(const gd_cmatrix *cm);
 // upper bound of the collision matrices' bytes (every triangle tile stored)
 double cmatrix_bytes_bound(const Context &c, int mode);
 

@@ -62,8 +62,10 @@ typedef struct {
     int64_t contraction_terms; /* nonzero-weight x pair-product terms per cell-eval */
     int64_t scatter_terms;     /* (s, g, sign) output updates per cell-eval */
     int64_t cmatrix_tiles;     /* stored 256 x 64 tiles of the collision matrices (0 without) */
-    int64_t cmatrix_slices;    /* 256 x 16 slices of those tiles with a nonzero entry: the MMA K steps
-                                  issued in GD_CMATRIX_BF16X3 mode (one BF16 pass issues whole tiles) */
+    int64_t cmatrix_slices;    /* 256 x 16 slices with a nonzero entry over every node's matrix: the MMA
+                                  K steps one cell tile issues in GD_CMATRIX_BF16X3 mode */
+    int64_t cmatrix_node_tiles; /* tiles over every node's matrix (a node uses the stored tiles of its
+                                   orbit's representative): what one BF16 pass issues per cell tile */
 } gd_info;
 
 /* Library version (major*10000 + minor*100 + patch). */
@@ -175,8 +177,8 @@ int gd_ctx_check(gd_ctx *ctx, gd_stream stream);
  * symmetric, so only the 256 x 64 tiles of its block upper triangle that hold
  * a nonzero entry are stored (off-diagonal entries doubled), and only for one
  * node per orbit of the lattice's reflections (x_a -> n_a - 1 - x_a on each
- * axis along which the node set is symmetric): node R(i) uses G_i with f
- * reflected by R.  At 20^3 (R = 4.8) that is ~5 GB in BF16, twice that for
+ * axis; the node set is symmetric since the sphere is centred in the box and
+ * n_a is even): node R(i) uses G_i with f reflected by R.  At 20^3 (R = 4.8) that is ~5 GB in BF16, twice that for
  * GD_CMATRIX_BF16X3 (8x less than one matrix per node).
  * GD_CMATRIX_BF16 rounds f and G to BF16 (relative error ~3e-4 on I);
  * GD_CMATRIX_BF16X3 splits both into BF16 hi + lo parts and sums

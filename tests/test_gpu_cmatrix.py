@@ -36,6 +36,30 @@ def test_cmatrix_gain_matches_oracle(cuda, gdlib, n, R, ncells, ld):
         cm.close()
 
 
+@pytest.mark.parametrize("dims,R", [((12, 10, 8), 4.2), ((8, 12, 10), 16.5)])
+def test_cmatrix_orbits_on_non_cubic_lattices(cuda, gdlib, dims, R):
+    """Matrices are stored for one node per orbit of the lattice's three
+    reflections, and node R(i) contracts the matrices of i with f reflected by
+    R; on lattices with different extents per axis (the sphere cutting some
+    of them) the result still matches the FP64 oracle."""
+    torch = cuda
+    nx, ny, nz = dims
+    spec = gdlib.GridSpec(nx, ny, nz, R=R)
+    ctx = gdlib.Context(spec)
+    nc = 96
+    f = inputs.mixtures(spec.fill(), nc, seed=31)
+    ft = torch.from_numpy(f).cuda()
+    o = Oracle(nx, ny, nz, R=R)
+    ref = o.gain_f64(o.to_box(f))
+    cm = gdlib.CollisionMatrix(ctx, gdlib.CMATRIX_BF16X3)
+    out = torch.empty_like(ft)
+    cm.gain(ft, nc, nc, out)
+    torch.cuda.synchronize()
+    rel = np.linalg.norm(out.cpu().numpy() - ref) / np.linalg.norm(ref)
+    assert rel <= 2e-5, rel
+    cm.close()
+
+
 @pytest.mark.parametrize("path,tol", [(2, 1e-4), (1, 2e-2)])
 def test_step_with_cmatrix_gain_path(cuda, gdlib, path, tol):
     """gd_step with the tensor-core gain: the FP64 projection still conserves
