@@ -31,6 +31,7 @@ GAIN_CMATRIX_BF16X3 = 2
 GAIN_PAIR_TC = 3
 BATCH_STREAMS = 0
 BATCH_FUSED_PAIR_TC = 1
+BATCH_FUSED_CMATRIX = 2
 MLP_SCALE_INPUT = 1
 MLP_SCALE_OUTPUT = 2
 MLP_LOSS_MSE = 4
@@ -522,8 +523,10 @@ class Batch:
         _check(lib().gd_batch_step(self._h, int(bool(use_graph)), _stream(stream)))
 
     def set_mode(self, mode: int):
-        """BATCH_STREAMS (per-group steps on forked streams) or
-        BATCH_FUSED_PAIR_TC (every group's gain in one persistent launch)."""
+        """BATCH_STREAMS (per-group steps on forked streams),
+        BATCH_FUSED_PAIR_TC (every group's gain in one persistent launch of the
+        pair-product kernel) or BATCH_FUSED_CMATRIX (every group's gain in one
+        launch of the collision-matrix kernel)."""
         _check(lib().gd_batch_set_mode(self._h, int(mode)))
 
     def check(self):

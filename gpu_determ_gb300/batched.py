@@ -1,7 +1,8 @@
 """Batched cells on uneven velocity grids, stepped as one CUDA graph.
 
     python -m gpu_determ_gb300.batched [--cells 4096] [--grids 12 16 20 24] [--steps 50]
-                                       [--radius 4.8] [--mach 3] [--no-graph] [--no-autotune] [--fused]
+                                       [--radius 4.8] [--mach 3] [--no-graph] [--no-autotune]
+                                       [--fused {cmatrix,pair_tc}]
 
 The cells sample a Mach-3 normal shock (inputs.shock_profile: tanh blend of
 the Rankine-Hugoniot upstream and downstream Maxwellians, gamma = 5/3,
@@ -9,7 +10,10 @@ upstream n = 1, T = 1) and are dealt round-robin to the grids, so every grid
 holds a full sampling of the profile.  Each grid is a context whose gain
 launch the autotuner picks on its own cells; one gd_batch holds all groups,
 and each step (collision, FP64 projection, Courant relaxation per grid) is
-one CUDA graph launch after the first two.  Reported: cells*steps/s over the
+one CUDA graph launch after the first two.  With --fused, every grid's gain
+runs in ONE launch per step: the collision-matrix kernel over all grids'
+(cell tile, node) pairs (cmatrix), or the persistent pair-product kernel over
+all grids' (cell tile, s-chunk) units (pair_tc).  Reported: cells*steps/s over the
 timed steps (CUDA events on the launching stream), per-grid moment drift
 between the first and last step, the autotuner's choices.
 """
@@ -21,17 +25,19 @@ import sys
 
 import numpy as np
 
-from . import (BATCH_FUSED_PAIR_TC, DT_COURANT, GAIN_CMATRIX_BF16X3, GAIN_PAIR, GAIN_PAIR_TC, Batch, Context, GridSpec,
+from . import (BATCH_FUSED_CMATRIX, BATCH_FUSED_PAIR_TC, DT_COURANT, GAIN_CMATRIX_BF16X3, GAIN_PAIR, GAIN_PAIR_TC, Batch, Context, GridSpec,
                inputs)
 
 
 def build(cells: int = 4096, grids=(12, 16, 20, 24), radius: float = 4.8, mach: float = 3.0,
           courant: float = 0.5, autotune: bool = True, mem_budget: float = 120e9, device: int = 0,
-          fused: bool = False):
+          fused: str | None = None):
     """Contexts, device arrays and the batch; returns a dict of them.  With
-    fused, every grid runs the pair products with the contraction on the
-    tensor cores and the batch computes all gains in one persistent launch
-    (BATCH_FUSED_PAIR_TC) instead of autotuned per-grid launches."""
+    fused = "cmatrix", every grid uses BF16x3 collision matrices and the batch
+    computes all gains in one launch of the collision-matrix kernel
+    (BATCH_FUSED_CMATRIX); with fused = "pair_tc", every grid runs the pair
+    products with the contraction on the tensor cores in one persistent launch
+    (BATCH_FUSED_PAIR_TC); otherwise each grid's gain path is autotuned."""
     import torch
     dev = torch.device("cuda", device)
     groups = []
@@ -45,7 +51,9 @@ def build(cells: int = 4096, grids=(12, 16, 20, 24), radius: float = 4.8, mach: 
         f = torch.from_numpy(np.ascontiguousarray(f_all[:, mine])).to(dev)
         nc = len(mine)
         tune = None
-        if fused:
+        if fused == "cmatrix":
+            ctx.set_gain_path(GAIN_CMATRIX_BF16X3)
+        elif fused == "pair_tc":
             ctx.set_gain_path(GAIN_PAIR_TC)
         elif autotune:
             tune = ctx.autotune(f, nc, nc,
@@ -57,7 +65,7 @@ def build(cells: int = 4096, grids=(12, 16, 20, 24), radius: float = 4.8, mach: 
         groups.append({"grid": n, "n_pnt": ctx.n_pnt, "cells": nc, "ctx": ctx, "f": f, "m5": m5, "time": t,
                        "autotune": tune})
     if fused:
-        b.set_mode(BATCH_FUSED_PAIR_TC)
+        b.set_mode(BATCH_FUSED_CMATRIX if fused == "cmatrix" else BATCH_FUSED_PAIR_TC)
     return {"batch": b, "groups": groups, "device": dev, "fused": fused}
 
 
@@ -105,8 +113,9 @@ def main(argv=None):
     p.add_argument("--no-graph", action="store_true")
     p.add_argument("--no-autotune", action="store_true")
     p.add_argument("--compare-eager", action="store_true", help="also time the same steps without the graph")
-    p.add_argument("--fused", action="store_true",
-                   help="every grid's gain in one persistent launch (pair products, contraction on tensor cores)")
+    p.add_argument("--fused", nargs="?", const="cmatrix", choices=["cmatrix", "pair_tc"],
+                   help="every grid's gain in one launch: collision matrices (default) or the persistent "
+                        "pair-product kernel")
     a = p.parse_args(argv)
     state = build(a.cells, a.grids, a.radius, a.mach, autotune=not a.no_autotune, fused=a.fused)
     res = run(state, a.steps, use_graph=not a.no_graph)

@@ -70,11 +70,13 @@ int enqueue_steps(gd_batch *b)
     return GD_OK;
 }
 
-// GD_BATCH_FUSED_PAIR_TC: every group's loss, then ONE persistent launch of
-// the pair-product gain (contraction on the tensor cores) for all groups,
-// then every group's projection and relaxation, all on the batch stream.
-// Each group's results equal gd_step on its context's GD_GAIN_PAIR_TC path
-// bit for bit (the same kernels, chunks and unit partials).
+// The fused modes: every group's loss, then ONE launch of the gain for all
+// groups (GD_BATCH_FUSED_PAIR_TC: the persistent pair-product kernel with its
+// contraction on the tensor cores; GD_BATCH_FUSED_CMATRIX: the collision-
+// matrix kernel over every grid's nodes), then every group's projection and
+// relaxation, all on the batch stream.  Each group's results equal gd_step on
+// its context's gain path bit for bit (the same per-unit work: integer sums
+// on the pair path, the same CTA pairs on the matrix path).
 int enqueue_fused(gd_batch *b)
 {
     using namespace gd;
@@ -82,6 +84,7 @@ int enqueue_fused(gd_batch *b)
     std::vector<float *> nu(ng), gain(ng);
     std::vector<double *> q(ng);
     std::vector<PtJob> jobs(ng);
+    std::vector<CmJob> cjobs(ng);
     for (size_t k = 0; k < ng; k++) {
         const gd_batch::Group &g = b->groups[k];
         Context &c = g.ctx->c;
@@ -91,8 +94,10 @@ int enqueue_fused(gd_batch *b)
         if (!rc) rc = run_loss_path(c, g.f, g.ncells, g.ld, nu[k], b->main);
         if (rc) return rc;
         jobs[k] = PtJob{&c, g.f, g.ncells, g.ld, gain[k]};
+        cjobs[k] = CmJob{c.cmatrix, g.f, g.ncells, g.ld, gain[k]};
     }
-    int rc = launch_pair_tc(jobs.data(), (int)ng, b->main);
+    int rc = b->mode == GD_BATCH_FUSED_CMATRIX ? launch_cmatrix(cjobs.data(), (int)ng, b->main)
+                                               : launch_pair_tc(jobs.data(), (int)ng, b->main);
     if (rc) return rc;
     for (size_t k = 0; k < ng; k++) {
         const gd_batch::Group &g = b->groups[k];
@@ -106,14 +111,19 @@ int enqueue_fused(gd_batch *b)
     return GD_OK;
 }
 
-int check_fused(const gd_batch *b)
+int check_fused(const gd_batch *b, int mode)
 {
     using namespace gd;
     if (b->groups.size() > 4) return set_error(GD_ERR_UNSUPPORTED, "fused batch: at most 4 groups");
     for (size_t k = 0; k < b->groups.size(); k++) {
         const Context &c = b->groups[k].ctx->c;
-        if (c.gain_path != GD_GAIN_PAIR_TC || !c.pair_tc)
+        if (mode == GD_BATCH_FUSED_PAIR_TC && (c.gain_path != GD_GAIN_PAIR_TC || !c.pair_tc))
             return set_error(GD_ERR_UNSUPPORTED, "fused batch: every group's context needs gain path GD_GAIN_PAIR_TC");
+        if (mode == GD_BATCH_FUSED_CMATRIX &&
+            (c.gain_path != b->groups[0].ctx->c.gain_path || !c.cmatrix ||
+             (c.gain_path != GD_GAIN_CMATRIX_BF16 && c.gain_path != GD_GAIN_CMATRIX_BF16X3)))
+            return set_error(GD_ERR_UNSUPPORTED,
+                             "fused batch: every group's context needs the same collision-matrix gain path");
         for (size_t j = 0; j < k; j++)
             if (b->groups[j].ctx == b->groups[k].ctx)
                 return set_error(GD_ERR_UNSUPPORTED, "fused batch: one group per context");
@@ -127,10 +137,10 @@ extern "C" int gd_batch_set_mode(gd_batch *b, int mode)
 {
     using namespace gd;
     if (!b) return set_error(GD_ERR_INVALID_ARG, "NULL argument");
-    if (mode != GD_BATCH_STREAMS && mode != GD_BATCH_FUSED_PAIR_TC)
+    if (mode != GD_BATCH_STREAMS && mode != GD_BATCH_FUSED_PAIR_TC && mode != GD_BATCH_FUSED_CMATRIX)
         return set_error(GD_ERR_INVALID_ARG, "unknown batch mode");
-    if (mode == GD_BATCH_FUSED_PAIR_TC) {
-        const int rc = check_fused(b);
+    if (mode != GD_BATCH_STREAMS) {
+        const int rc = check_fused(b, mode);
         if (rc) return rc;
     }
     b->mode = mode;
@@ -213,8 +223,8 @@ extern "C" int gd_batch_step(gd_batch *b, int use_graph, gd_stream stream)
     GD_CUDA(cudaEventRecord(b->joined, user));
     GD_CUDA(cudaStreamWaitEvent(b->main, b->joined, 0));
     int rc = GD_OK;
-    if (b->mode == GD_BATCH_FUSED_PAIR_TC && (rc = check_fused(b))) return rc;
-    auto enqueue = [&]() { return b->mode == GD_BATCH_FUSED_PAIR_TC ? enqueue_fused(b) : enqueue_steps(b); };
+    if (b->mode != GD_BATCH_STREAMS && (rc = check_fused(b, b->mode))) return rc;
+    auto enqueue = [&]() { return b->mode != GD_BATCH_STREAMS ? enqueue_fused(b) : enqueue_steps(b); };
     if (!use_graph || b->steps == 0) {
         rc = enqueue();
     } else {

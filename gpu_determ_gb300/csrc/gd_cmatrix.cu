@@ -107,8 +107,23 @@ struct CmParams {
     const uint32_t *tiles;   // stored tiles (mask << 28 | n << 16 | k), n-major then k per representative
     const int *orbit;        // [ns] node -> representative's slot << 3 | reflection
     const int *order;        // [ns] the nodes in launch order (reflection-major)
-    int m_tiles;             // cell tiles, padded to whole clusters (the grid's x extent)
+    int m_tiles;             // cell tiles, padded to whole clusters
     int chain;               // most stored tiles summed in one tensor-memory accumulation (even)
+};
+
+// One launch serves up to kCmMaxGrids velocity grids (each with its own
+// matrices, f and gain): blockIdx.y in [ystart[j], ystart[j + 1]) is node
+// blockIdx.y - ystart[j] (in launch order) of grid j, blockIdx.x its cell
+// tile (CTAs past the grid's m_tiles leave at once, pairs together).
+constexpr int kCmMaxGrids = 4;
+struct CmLaunch {
+    CmParams g[kCmMaxGrids];
+    int ystart[kCmMaxGrids + 1];
+    int ngrids;
+};
+// the grids' tensor maps: f (hi, lo; one copy per reflection) and G (hi, lo)
+struct CmMaps {
+    CUtensorMap fh[kCmMaxGrids], fl[kCmMaxGrids], gh[kCmMaxGrids], gl[kCmMaxGrids];
 };
 
 // G_i is symmetric in (a, b), so only its block upper triangle is stored and
@@ -128,12 +143,22 @@ __host__ __device__ __forceinline__ int k_end(int n, int num_k)
 // CTA issues the MMAs, and each CTA's tensor memory receives its own cells'
 // rows.  A CTA then brings 32 KB per tile into its shared memory instead of
 // 48 KB, and a G tile crosses L2 once per pair.
-template <int NPASS, int CL>
+template <int NPASS, int CL, bool MULTI>
 __global__ void __launch_bounds__(kThreads, 1)
-    cmatrix_gain_kernel(const __grid_constant__ CUtensorMap tmFh, const __grid_constant__ CUtensorMap tmFl,
-                        const __grid_constant__ CUtensorMap tmGh, const __grid_constant__ CUtensorMap tmGl,
-                        CmParams p)
+    cmatrix_gain_kernel(const __grid_constant__ CmMaps maps, const __grid_constant__ CmLaunch L)
 {
+    // MULTI: several grids in the launch (the fused batch); a single grid
+    // reads its parameters at constant offsets (selecting them by a runtime
+    // index costs registers, and the kernel is at its register limit)
+    int gj = 0;
+    if (MULTI)
+        while (gj + 1 < L.ngrids && (int)blockIdx.y >= L.ystart[gj + 1]) gj++;
+    const CmParams &p = L.g[MULTI ? gj : 0];
+    // cell tiles past this grid's extent (m_tiles is a multiple of CL, so the
+    // two CTAs of a pair leave together, before any barrier)
+    if ((int)blockIdx.x >= p.m_tiles) return;
+    const int mj = MULTI ? gj : 0;
+    const CUtensorMap &tmFh = maps.fh[mj], &tmFl = maps.fl[mj], &tmGh = maps.gh[mj], &tmGl = maps.gl[mj];
     constexpr int NPARTS = NPASS == 1 ? 1 : 2;
     constexpr bool PAIR = CL == 2;
     constexpr uint32_t kTileBc = kTileB / CL;  // this CTA's rows of a G tile
@@ -191,7 +216,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     // Node i = R(i0) for the representative i0 of its orbit under the lattice's
     // reflections: G_i[a][b] = G_i0[R a][R b], so I_i(f) = I_i0(f o R), and the
     // CTA contracts i0's stored tiles with the copy of f reflected by R.
-    const int m_tile = blockIdx.x, node = __ldg(p.order + blockIdx.y);
+    const int m_tile = blockIdx.x, node = __ldg(p.order + (blockIdx.y - (MULTI ? L.ystart[gj] : 0)));
     const int ob = __ldg(p.orbit + node), rep = ob >> 3, refl = ob & 7;
     const int l0 = __ldg(p.node_off + rep), cnt = __ldg(p.node_off + rep + 1) - l0;
 
@@ -991,56 +1016,81 @@ extern "C" int gd_cmatrix_destroy(gd_cmatrix *h)
     return GD_OK;
 }
 
-extern "C" int gd_cmatrix_gain(gd_cmatrix *h, const float *f, int ncells, int ld, float *gain, gd_stream stream)
-{
-    using namespace gd;
-    if (!h || !f || !gain) return set_error(GD_ERR_INVALID_ARG, "NULL argument");
-    if (ncells < 1 || ld < ncells) return set_error(GD_ERR_INVALID_ARG, "need 1 <= ncells <= ld");
-    cudaStream_t st = (cudaStream_t)stream;
-    const bool split = h->mode == GD_CMATRIX_BF16X3;
-    int rc0 = gd::ensure_f(h, ncells);
-    if (rc0) return rc0;
-    dim3 cb(32, 8), cg((h->ns_k + 31) / 32, (ncells + 31) / 32, h->nrefl);
-    convert_f_kernel<<<cg, cb, 0, st>>>(f, h->ns, h->ns_k, ncells, ld, h->inv, h->fh, split ? h->fl : nullptr, h->fp,
-                                        h->f_cells, h->f_cells);
-    GD_CUDA(cudaGetLastError());
+namespace gd {
 
+// The collision-matrix gain of one or more grids (at most kCmMaxGrids, one
+// mode) in one launch: per grid the reflected copies of f, its tensor maps
+// and parameters; the grids' nodes stacked along the grid's y extent.  Each
+// grid's result equals its own launch's bit for bit (every CTA does the same
+// work either way).
+int launch_cmatrix(const CmJob *jobs, int njobs, cudaStream_t st)
+{
+    if (njobs < 1 || njobs > kCmMaxGrids) return set_error(GD_ERR_UNSUPPORTED, "collision-matrix launch: 1-4 grids");
+    const bool split = jobs[0].cm->mode == GD_CMATRIX_BF16X3;
+    // a CTA pair per MMA when every grid allows it (cluster 2, more than one cell tile)
+    int cl = 2;
+    for (int j = 0; j < njobs; j++) {
+        const CmJob &jb = jobs[j];
+        if (!jb.cm || !jb.f || !jb.gain) return set_error(GD_ERR_INVALID_ARG, "NULL argument");
+        if (jb.ncells < 1 || jb.ld < jb.ncells) return set_error(GD_ERR_INVALID_ARG, "need 1 <= ncells <= ld");
+        if ((jb.cm->mode == GD_CMATRIX_BF16X3) != split)
+            return set_error(GD_ERR_UNSUPPORTED, "collision-matrix launch: one mode for every grid");
+        for (int k = 0; k < j; k++)
+            if (jobs[k].cm == jb.cm) return set_error(GD_ERR_UNSUPPORTED, "one launch serves distinct matrices");
+        if (jb.cm->cluster != 2 || jb.ncells <= BM) cl = 1;
+    }
     EncodeTiled enc;
     int rc = get_encoder(&enc);
     if (rc) return rc;
-    CUtensorMap tFh, tFl, tGh, tGl;
-    // f per reflection: [R][cell][matrix index], f_cells rows per R (cells past
-    // ncells read as zeros)
-    const cuuint64_t fdims[3] = {(cuuint64_t)h->ns_k, (cuuint64_t)ncells, (cuuint64_t)h->nrefl};
-    const cuuint64_t fstr[2] = {(cuuint64_t)h->ns_k * 2, (cuuint64_t)h->f_cells * h->ns_k * 2};
-    const cuuint32_t fbox[3] = {BK, BM, 1};
-    const cuuint64_t gdims[3] = {(cuuint64_t)BK, (cuuint64_t)BN, (cuuint64_t)std::max<int64_t>(h->slots, 1)};
-    const cuuint64_t gstr[2] = {(cuuint64_t)BK * 2, (cuuint64_t)BN * BK * 2};
-    // with a CTA pair each CTA loads half of a G tile
-    const int cl = (h->cluster == 2 && ncells > BM) ? 2 : 1;
-    const cuuint32_t gbox[3] = {BK, (cuuint32_t)(BN / cl), 1};
-    if ((rc = encode(enc, &tFh, h->fh, 3, fdims, fstr, fbox))) return rc;
-    if ((rc = encode(enc, &tGh, h->gh, 3, gdims, gstr, gbox))) return rc;
-    if (split) {
-        if ((rc = encode(enc, &tFl, h->fl, 3, fdims, fstr, fbox))) return rc;
-        if ((rc = encode(enc, &tGl, h->gl, 3, gdims, gstr, gbox))) return rc;
-    } else {
-        tFl = tFh;
-        tGl = tGh;
+    CmMaps maps{};
+    CmLaunch L{};
+    L.ngrids = njobs;
+    int mx = 0;
+    for (int j = 0; j < njobs; j++) {
+        const CmJob &jb = jobs[j];
+        gd_cmatrix *h = jb.cm;
+        if ((rc = ensure_f(h, jb.ncells))) return rc;
+        dim3 cb(32, 8), cg((h->ns_k + 31) / 32, (jb.ncells + 31) / 32, h->nrefl);
+        convert_f_kernel<<<cg, cb, 0, st>>>(jb.f, h->ns, h->ns_k, jb.ncells, jb.ld, h->inv, h->fh,
+                                            split ? h->fl : nullptr, h->fp, h->f_cells, h->f_cells);
+        GD_CUDA(cudaGetLastError());
+        // f per reflection: [R][cell][matrix index], f_cells rows per R (cells
+        // past ncells read as zeros)
+        const cuuint64_t fdims[3] = {(cuuint64_t)h->ns_k, (cuuint64_t)jb.ncells, (cuuint64_t)h->nrefl};
+        const cuuint64_t fstr[2] = {(cuuint64_t)h->ns_k * 2, (cuuint64_t)h->f_cells * h->ns_k * 2};
+        const cuuint32_t fbox[3] = {BK, BM, 1};
+        const cuuint64_t gdims[3] = {(cuuint64_t)BK, (cuuint64_t)BN, (cuuint64_t)std::max<int64_t>(h->slots, 1)};
+        const cuuint64_t gstr[2] = {(cuuint64_t)BK * 2, (cuuint64_t)BN * BK * 2};
+        // with a CTA pair each CTA loads half of a G tile
+        const cuuint32_t gbox[3] = {BK, (cuuint32_t)(BN / cl), 1};
+        if ((rc = encode(enc, &maps.fh[j], h->fh, 3, fdims, fstr, fbox))) return rc;
+        if ((rc = encode(enc, &maps.gh[j], h->gh, 3, gdims, gstr, gbox))) return rc;
+        if (split) {
+            if ((rc = encode(enc, &maps.fl[j], h->fl, 3, fdims, fstr, fbox))) return rc;
+            if ((rc = encode(enc, &maps.gl[j], h->gl, 3, gdims, gstr, gbox))) return rc;
+        } else {
+            maps.fl[j] = maps.fh[j];
+            maps.gl[j] = maps.gh[j];
+        }
+        // cell tiles padded to whole clusters: a tile past ncells reads zeros and stores nothing
+        const int m_tiles = ((jb.ncells + BM - 1) / BM + cl - 1) / cl * cl;
+        L.g[j] = CmParams{h->ns,     h->ns_k,     jb.ncells, jb.ld,    h->fp,    h->f_cells, jb.gain,
+                          h->err,    h->node_off, h->list,   h->orbit, h->order, m_tiles,    h->chain};
+        L.ystart[j + 1] = L.ystart[j] + h->ns;
+        mx = std::max(mx, m_tiles);
     }
-    // cell tiles padded to whole clusters: a tile past ncells reads zeros and stores nothing
-    const int m_tiles = ((ncells + BM - 1) / BM + cl - 1) / cl * cl;
-    CmParams prm{h->ns,     h->ns_k,  ncells,   ld,       h->fp,    h->f_cells, gain,
-                 h->err,    h->node_off, h->list, h->orbit, h->order, m_tiles,  h->chain};
     // one CTA per (cell tile, node), cell tiles fastest so that the CTAs in flight
     // share a few nodes' matrix tiles in L2 (a persistent grid of one CTA per SM
     // taking the tiles round-robin measured 3-4 % slower at 20^3 / 4096 cells)
-    dim3 grid((unsigned)m_tiles, (unsigned)h->ns);
+    if (L.ystart[njobs] > 65535) return set_error(GD_ERR_UNSUPPORTED, "collision-matrix launch: too many nodes");
+    dim3 grid((unsigned)mx, (unsigned)L.ystart[njobs]);
     const int npass = split ? 3 : 1;
     const size_t smem = (size_t)cm_stages(npass, cl) * cm_stage_bytes(npass, cl) + 1024;
-    void (*kern)(const CUtensorMap, const CUtensorMap, const CUtensorMap, const CUtensorMap, CmParams) =
-        split ? (cl == 2 ? cmatrix_gain_kernel<3, 2> : cmatrix_gain_kernel<3, 1>)
-              : (cl == 2 ? cmatrix_gain_kernel<1, 2> : cmatrix_gain_kernel<1, 1>);
+    void (*kern)(const CmMaps, const CmLaunch) =
+        njobs == 1 ? (split ? (cl == 2 ? cmatrix_gain_kernel<3, 2, false> : cmatrix_gain_kernel<3, 1, false>)
+                            : (cl == 2 ? cmatrix_gain_kernel<1, 2, false> : cmatrix_gain_kernel<1, 1, false>))
+                   : (split ? (cl == 2 ? cmatrix_gain_kernel<3, 2, true> : cmatrix_gain_kernel<3, 1, true>)
+                            : (cl == 2 ? cmatrix_gain_kernel<1, 2, true> : cmatrix_gain_kernel<1, 1, true>));
     GD_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = grid;
@@ -1054,11 +1104,22 @@ extern "C" int gd_cmatrix_gain(gd_cmatrix *h, const float *f, int ncells, int ld
     attr[0].val.clusterDim.z = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    GD_CUDA(cudaLaunchKernelEx(&cfg, kern, tFh, tFl, tGh, tGl, prm));
+    GD_CUDA(cudaLaunchKernelEx(&cfg, kern, maps, L));
     GD_CUDA(cudaGetLastError());
-    // the kernel records a pipeline time-out in h->err instead of hanging; the
-    // call only enqueues work, and gd_cmatrix_check / gd_ctx_check report it
+    // the kernel records a pipeline time-out in each grid's err instead of
+    // hanging; the call only enqueues work, and gd_cmatrix_check /
+    // gd_ctx_check report it
     return GD_OK;
+}
+
+}  // namespace gd
+
+extern "C" int gd_cmatrix_gain(gd_cmatrix *h, const float *f, int ncells, int ld, float *gain, gd_stream stream)
+{
+    using namespace gd;
+    if (!h || !f || !gain) return set_error(GD_ERR_INVALID_ARG, "NULL argument");
+    const CmJob job{h, f, ncells, ld, gain};
+    return launch_cmatrix(&job, 1, (cudaStream_t)stream);
 }
 
 extern "C" int gd_ctx_inject_timeout(gd_ctx *ctx, int polls)

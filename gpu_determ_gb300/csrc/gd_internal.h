@@ -204,6 +204,15 @@ struct PtJob {
     float *gain;
 };
 int launch_pair_tc(const PtJob *jobs, int njobs, cudaStream_t st);
+// the collision-matrix gain of 1-4 grids (one gd_cmatrix each, one mode) in
+// one launch (gd_cmatrix.cu); results equal separate launches bit for bit
+struct CmJob {
+    gd_cmatrix *cm;
+    const float *f;
+    int ncells, ld;
+    float *gain;
+};
+int launch_cmatrix(const CmJob *jobs, int njobs, cudaStream_t st);
 // reads (synchronising st) and clears the pipeline time-out record of the
 // pair tensor-core kernel; *timed_out receives whether it was set
 int pair_tc_take_timeout(Context &c, cudaStream_t st, bool *timed_out);

@@ -279,8 +279,12 @@ int gd_batch_step(gd_batch *b, int use_graph, gd_stream stream);
  * 128-cell tile, s-chunk) units, each group's loss, projection and
  * relaxation around it on the batch stream; results equal gd_step on each
  * group's context bit for bit.  A pipeline time-out of the fused launch is
- * recorded on the first group's context. */
-enum { GD_BATCH_STREAMS = 0, GD_BATCH_FUSED_PAIR_TC = 1 };
+ * recorded on the first group's context.  GD_BATCH_FUSED_CMATRIX: the same
+ * with the gains of all groups (at most 4, on distinct contexts whose gain
+ * path is the same collision-matrix mode) in one launch of the
+ * collision-matrix kernel over every grid's (cell tile, node) pairs; results
+ * equal gd_step bit for bit, time-outs are recorded per context. */
+enum { GD_BATCH_STREAMS = 0, GD_BATCH_FUSED_PAIR_TC = 1, GD_BATCH_FUSED_CMATRIX = 2 };
 int gd_batch_set_mode(gd_batch *b, int mode);
 int gd_batch_check(gd_batch *b);
 int gd_batch_info(const gd_batch *b, int *groups, int *streams, int *graph_nodes, int64_t *steps);

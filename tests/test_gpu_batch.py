@@ -95,13 +95,15 @@ def test_autotune_picks_a_measured_candidate(gdlib, cuda):
     assert r2["path"] == "pair" and len(r2["candidates"]) == 3
 
 
-def test_fused_batch_one_launch_matches_single_steps(gdlib, cuda):
-    """GD_BATCH_FUSED_PAIR_TC: the gains of uneven grids (8^3, 12^3, 16^3 with
-    200-300 cells, so some grids have more than one 128-cell tile) come from
-    one persistent launch over a device list of (grid, cell tile, s-chunk)
-    units; each grid's distribution and time after a few steps, eager and
-    replayed from the graph, equal gd_step on its own context (pair products
-    with the contraction on the tensor cores) bit for bit."""
+@pytest.mark.parametrize("mode", ["pair_tc", "cmatrix"])
+def test_fused_batch_one_launch_matches_single_steps(gdlib, cuda, mode):
+    """The gains of uneven grids (8^3, 12^3, 16^3 with 130-300 cells, so some
+    grids have more than one 128-cell tile) come from one launch per step:
+    GD_BATCH_FUSED_PAIR_TC, the persistent pair-product kernel over a device
+    list of (grid, cell tile, s-chunk) units; GD_BATCH_FUSED_CMATRIX, the
+    BF16x3 collision-matrix kernel over every grid's (cell tile, node) pairs.
+    Each grid's distribution and time after a few steps, eager and replayed
+    from the graph, equal gd_step on its own context bit for bit."""
     torch = cuda
     from gpu_determ_gb300 import inputs
     specs = [(8, 200, 11), (12, 300, 12), (16, 130, 13)]
@@ -109,7 +111,7 @@ def test_fused_batch_one_launch_matches_single_steps(gdlib, cuda):
     for n, cells, seed in specs:
         spec = gdlib.GridSpec(n, R=4.8)
         ctx = gdlib.Context(spec)
-        ctx.set_gain_path(gdlib.GAIN_PAIR_TC)
+        ctx.set_gain_path(gdlib.GAIN_PAIR_TC if mode == "pair_tc" else gdlib.GAIN_CMATRIX_BF16X3)
         groups.append((ctx, inputs.shock_profile(spec.fill(), cells) if n != 12 else
                        inputs.mixtures(spec.fill(), cells, seed=seed), cells))
     f_ref, t_ref = _run_single(gdlib, torch, groups)
@@ -122,7 +124,7 @@ def test_fused_batch_one_launch_matches_single_steps(gdlib, cuda):
             b.add(ctx, f, cells, cells, gdlib.DT_COURANT, 0.5, time=t)
             fs.append(f)
             ts.append(t)
-        b.set_mode(gdlib.BATCH_FUSED_PAIR_TC)
+        b.set_mode(gdlib.BATCH_FUSED_PAIR_TC if mode == "pair_tc" else gdlib.BATCH_FUSED_CMATRIX)
         for _ in range(STEPS):
             b.step(use_graph)
         b.check()
@@ -144,7 +146,8 @@ def test_fused_batch_rejects_other_gain_paths(gdlib, cuda):
     f = torch.from_numpy(inputs.mixtures(spec.fill(), 32, seed=1)).cuda()
     b = gdlib.Batch()
     b.add(ctx, f, 32, 32, gdlib.DT_COURANT, 0.5)
-    with pytest.raises(gdlib.GDError) as e:
-        b.set_mode(gdlib.BATCH_FUSED_PAIR_TC)     # the context is on the FP32 pair kernel
-    assert e.value.code == 4
+    for mode in (gdlib.BATCH_FUSED_PAIR_TC, gdlib.BATCH_FUSED_CMATRIX):
+        with pytest.raises(gdlib.GDError) as e:
+            b.set_mode(mode)                      # the context is on the FP32 pair kernel
+        assert e.value.code == 4
     b.close()
