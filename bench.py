@@ -586,13 +586,12 @@ def gain_roofline(name, ctx, f0, nc, stream, flush, peak, reps):
         bound, pk, src = "tensor", peak["bf16"], peak["bf16_source"]
         # DRAM bytes per launch: every node's matrix tiles stream through about
         # once (a representative's tiles once per reflection: the launch runs
-        # reflection-major).  An ncu capture of the BF16x3 kernel (CTA pairs,
-        # one matrix per node) on 14^3 / 4096 cells read and wrote 7.141 GB for
-        # 5.636 GB of matrix tiles (ratio 1.267); scaled here by the tile bytes
-        # the nodes stream.
+        # reflection-major).  An ncu capture of the BF16x3 kernel (CTA pairs) on
+        # 14^3 / 4096 cells read and wrote 7.806 GB for 5.820 GB of tiles the
+        # nodes stream (ratio 1.341); scaled here by the 20^3 launch's tiles.
         g_bytes = inf["cmatrix_node_tiles"] * 256 * 64 * 2 * (2 if name == "bf16x3" else 1)
-        traffic = 1.267 * g_bytes
-        traffic_src = "ncu dram__bytes_read+write of a 14^3/4096-cell launch, scaled by collision-matrix bytes"
+        traffic = 1.341 * g_bytes
+        traffic_src = "ncu dram__bytes_read+write of a 14^3/4096-cell launch, scaled by the matrix tile bytes the nodes stream"
     ach = flop / g_avg / 1e12
     out = {"bound": bound, "kernel": kernel, "achieved": ach, "peak": pk, "unit": "TFLOP/s",
            "frac": ach / pk, "peak_source": src, "work": work,
