@@ -1029,6 +1029,7 @@ int launch_cmatrix(const CmJob *jobs, int njobs, cudaStream_t st)
     const bool split = jobs[0].cm->mode == GD_CMATRIX_BF16X3;
     // a CTA pair per MMA when every grid allows it (cluster 2, more than one cell tile)
     int cl = 2;
+    int64_t total_nodes = 0;
     for (int j = 0; j < njobs; j++) {
         const CmJob &jb = jobs[j];
         if (!jb.cm || !jb.f || !jb.gain) return set_error(GD_ERR_INVALID_ARG, "NULL argument");
@@ -1038,7 +1039,9 @@ int launch_cmatrix(const CmJob *jobs, int njobs, cudaStream_t st)
         for (int k = 0; k < j; k++)
             if (jobs[k].cm == jb.cm) return set_error(GD_ERR_UNSUPPORTED, "one launch serves distinct matrices");
         if (jb.cm->cluster != 2 || jb.ncells <= BM) cl = 1;
+        total_nodes += jb.cm->ns;
     }
+    if (total_nodes > 65535) return set_error(GD_ERR_UNSUPPORTED, "collision-matrix launch: too many nodes");
     EncodeTiled enc;
     int rc = get_encoder(&enc);
     if (rc) return rc;
@@ -1082,7 +1085,6 @@ int launch_cmatrix(const CmJob *jobs, int njobs, cudaStream_t st)
     // one CTA per (cell tile, node), cell tiles fastest so that the CTAs in flight
     // share a few nodes' matrix tiles in L2 (a persistent grid of one CTA per SM
     // taking the tiles round-robin measured 3-4 % slower at 20^3 / 4096 cells)
-    if (L.ystart[njobs] > 65535) return set_error(GD_ERR_UNSUPPORTED, "collision-matrix launch: too many nodes");
     dim3 grid((unsigned)mx, (unsigned)L.ystart[njobs]);
     const int npass = split ? 3 : 1;
     const size_t smem = (size_t)cm_stages(npass, cl) * cm_stage_bytes(npass, cl) + 1024;
