@@ -48,9 +48,6 @@ struct GemmArgs {
     bf16 *c16;          // [M][ld16] or null
     int ld32, ld16;
     int *err;
-    // K range of this launch: columns [k0, k0 + K) of A and B, whose rows
-    // hold ldk elements (ldk = 0: K, the whole rows)
-    int k0, ldk;
     // failure-detection test hook: > 0 makes every CTA wait this many polls on
     // a barrier that nothing arrives at (before any copy or MMA is issued),
     // record the time-out, free its tensor memory and return
@@ -137,8 +134,8 @@ __global__ void __launch_bounds__(kGThreads, 1)
                 unsigned char *st = base + (size_t)s * kStageBytes;
                 const uint32_t fb = smem_u32(&full_bar[s]);
                 mbar_expect_tx(fb, kStageBytes);
-                tma_load_2d(smem_u32(st), &tA, p.k0 + k * GK, m0, fb);
-                tma_load_2d(smem_u32(st + kA), &tB, p.k0 + k * GK, n0, fb);
+                tma_load_2d(smem_u32(st), &tA, k * GK, m0, fb);
+                tma_load_2d(smem_u32(st + kA), &tB, k * GK, n0, fb);
             }
         }
     } else if (warp == 1) {
@@ -638,15 +635,11 @@ int make_map(CUtensorMap *m, const bf16 *ptr, int rows, int K, int box_rows)
 // output strides ld32, ld16 multiples of 4.
 int gemm_nt(int epi, const bf16 *A, const bf16 *B, const GemmArgs &a, cudaStream_t st)
 {
-    const int ldk = a.ldk ? a.ldk : a.K;
-    if (a.K % GK || a.K <= 0 || a.M <= 0 || a.N <= 0 || (a.ld32 & 3) || (a.ld16 & 3) || a.k0 % GK || a.k0 < 0 ||
-        ldk % GK || a.k0 + a.K > ldk)
-        return set_error(GD_ERR_INVALID_ARG,
-                         "GEMM shape: K, k0 and the row length multiples of 64, k0 + K within the rows, strides "
-                         "multiples of 4");
+    if (a.K % GK || a.K <= 0 || a.M <= 0 || a.N <= 0 || (a.ld32 & 3) || (a.ld16 & 3))
+        return set_error(GD_ERR_INVALID_ARG, "GEMM shape: K a multiple of 64, strides multiples of 4");
     CUtensorMap tA, tB;
-    int rc = make_map(&tA, A, a.M, ldk, GM);
-    if (!rc) rc = make_map(&tB, B, a.N, ldk, GN);
+    int rc = make_map(&tA, A, a.M, a.K, GM);
+    if (!rc) rc = make_map(&tB, B, a.N, a.K, GN);
     if (rc) return rc;
     dim3 grid((a.M + GM - 1) / GM, (a.N + GN - 1) / GN);
     switch (epi) {
