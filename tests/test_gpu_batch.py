@@ -151,3 +151,24 @@ def test_fused_batch_rejects_other_gain_paths(gdlib, cuda):
             b.set_mode(mode)                      # the context is on the FP32 pair kernel
         assert e.value.code == 4
     b.close()
+
+
+def test_fused_cmatrix_batch_needs_one_matrix_mode(gdlib, cuda):
+    """One launch of the collision-matrix kernel serves one mode: groups on
+    BF16x3 and on one BF16 pass cannot be fused (GD_ERR_UNSUPPORTED, before
+    anything is enqueued)."""
+    torch = cuda
+    from gpu_determ_gb300 import inputs
+    b = gdlib.Batch()
+    ctxs = []
+    for n, path in ((8, gdlib.GAIN_CMATRIX_BF16X3), (12, gdlib.GAIN_CMATRIX_BF16)):
+        spec = gdlib.GridSpec(n, R=4.8)
+        ctx = gdlib.Context(spec)
+        ctx.set_gain_path(path)
+        f = torch.from_numpy(inputs.mixtures(spec.fill(), 64, seed=n)).cuda()
+        b.add(ctx, f, 64, 64, gdlib.DT_COURANT, 0.5)
+        ctxs.append(ctx)
+    with pytest.raises(gdlib.GDError) as e:
+        b.set_mode(gdlib.BATCH_FUSED_CMATRIX)
+    assert e.value.code == 4
+    b.close()
