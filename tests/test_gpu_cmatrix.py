@@ -218,3 +218,32 @@ def test_c2_batch_against_fp64_oracle(cuda, gdlib):
         if path != gdlib.GAIN_CMATRIX_BF16:
             assert cell_q.max() <= 1e-3, (path, report[path])
     print("C2 16^3,", nc, "cells: path -> (gain rel-L2, Q rel-L2, Q per-cell median, p99, max) vs FP64:", report)
+
+
+def test_orbit_storage_reflection_identity_is_bitwise(cuda, gdlib):
+    """Node R(i) contracts the matrices of its orbit's representative with f
+    reflected by R, so the gain of f at R(i) and the gain of f o R at i run
+    the same MMAs on the same operands: equal bit for bit, for every node and
+    all eight reflections of the lattice."""
+    torch = cuda
+    n = 12
+    spec = gdlib.GridSpec(n, R=4.8)
+    g = spec.fill()
+    ui, vi, wi = g["ui"], g["vi"], g["wi"]
+    box = {(int(a), int(b), int(c)): m for m, (a, b, c) in enumerate(zip(ui, vi, wi))}
+    ctx = gdlib.Context(spec)
+    cm = gdlib.CollisionMatrix(ctx, gdlib.CMATRIX_BF16X3)
+    nc = 140
+    f = inputs.mixtures(g, nc, seed=77)
+    base = torch.empty((len(ui), nc), dtype=torch.float32, device="cuda")
+    cm.gain(torch.from_numpy(f).cuda(), nc, nc, base)
+    torch.cuda.synchronize()
+    base = base.cpu().numpy()
+    for R in range(1, 8):
+        perm = np.array([box[((n - 1 - a) if R & 1 else a, (n - 1 - b) if R & 2 else b, (n - 1 - c) if R & 4 else c)]
+                         for a, b, c in zip(ui, vi, wi)])
+        out = torch.empty((len(ui), nc), dtype=torch.float32, device="cuda")
+        cm.gain(torch.from_numpy(np.ascontiguousarray(f[perm])).cuda(), nc, nc, out)  # (f o R)[m] = f[R m]
+        torch.cuda.synchronize()
+        assert np.array_equal(out.cpu().numpy(), base[perm]), R
+    cm.close()
