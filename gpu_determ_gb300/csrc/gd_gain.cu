@@ -119,7 +119,7 @@ __global__ void __launch_bounds__(kThreads, 1) gain_pair_kernel(GainArgs a)
                 const int k4 = cmap[A + l1z0], k5 = cmap[B + lz0], k6 = cmap[Cc + lz0], k7 = cmap[Dd + l1z0];
                 const int j0 = cmap[A + lz1], j1 = cmap[B + l1z1], j2 = cmap[Cc + l1z1], j3 = cmap[Dd + lz1];
                 const int j4 = cmap[A + l1z1], j5 = cmap[B + lz1], j6 = cmap[Cc + lz1], j7 = cmap[Dd + l1z1];
-#define GD_F(k) (((k) >= 0 && live) ? __ldg(fcol + (size_t)(k) * ld) : 0.f)
+#define GD_F(k) (((k) >= 0 && live) ? __ldg(fcol + (k) * ld) : 0.f)  // 32-bit offsets: n_pnt ld < 2^31
                 const float f0 = GD_F(k0), f1 = GD_F(k1), f2 = GD_F(k2), f3 = GD_F(k3);
                 const float f4 = GD_F(k4), f5 = GD_F(k5), f6 = GD_F(k6), f7 = GD_F(k7);
                 const float h0 = GD_F(j0), h1 = GD_F(j1), h2 = GD_F(j2), h3 = GD_F(j3);
@@ -205,11 +205,11 @@ __global__ void __launch_bounds__(kThreads, 1) gain_pair_kernel(GainArgs a)
                     const bool hx = sg & 1, hy = (sg >> 1) & 1, hz = (sg >> 2) & 1;
                     const bool dup = (hx && gx == 0) || (hy && gy == 0) || (hz && gz == 0);
                     tgt[sg] = dup ? -1 : cmap[(hx ? X1 : X0) + (hy ? Y1 : Y0) + (hz ? Z1 : Z0)];
-                    old[sg] = tgt[sg] >= 0 ? part[(size_t)tgt[sg] * a.cells_pad] : 0.f;
+                    old[sg] = tgt[sg] >= 0 ? part[tgt[sg] * a.cells_pad] : 0.f;
                 }
 #pragma unroll
                 for (int sg = 0; sg < 8; sg++)
-                    if (tgt[sg] >= 0) part[(size_t)tgt[sg] * a.cells_pad] = old[sg] + acc;
+                    if (tgt[sg] >= 0) part[tgt[sg] * a.cells_pad] = old[sg] + acc;
             }
         }
         __syncthreads();
@@ -378,6 +378,9 @@ int launch_gain_pair(Context &c, const float *f, int ncells, int ld, float *gain
     const Dims &d = c.d;
     const int nblk = (ncells + cb - 1) / cb;
     const int cells_pad = nblk * cb;
+    // the kernel forms node x stride offsets in 32 bits
+    if ((int64_t)d.n_pnt * std::max(ld, cells_pad) >= ((int64_t)1 << 31))
+        return set_error(GD_ERR_UNSUPPORTED, "pair gain: n_pnt * ld must stay below 2^31");
     GD_CUDA(cudaMemsetAsync(part, 0, (size_t)nchunks * d.n_pnt * cells_pad * sizeof(float), st));
     GainArgs a{d, f, ld, ncells, cells_pad, c.d_cmap, c.d_grp_row_off, c.d_grp_rows, c.d_D_item_off,
                c.d_D_items, c.d_D_members, d_bounds, part, c.gain_cmap_smem ? 1 : 0};
