@@ -221,7 +221,8 @@ int gd_cmatrix_check(gd_cmatrix *cm, gd_stream stream);
  * the tensor cores, pair products and weights split into BF16 hi + lo, each
  * cell's outputs summed in 64-bit fixed point scaled by a bound on its gain;
  * builds a per-class-box weight table of a few GB at 24^3 instead of n^3
- * matrices, so it serves the grids whose collision matrices do not fit). */
+ * matrices, so it serves the grids whose collision matrices do not fit).
+ * The two pair paths need n_pnt * ld < 2^31 (GD_ERR_UNSUPPORTED otherwise). */
 enum { GD_GAIN_PAIR = 0, GD_GAIN_CMATRIX_BF16 = 1, GD_GAIN_CMATRIX_BF16X3 = 2, GD_GAIN_PAIR_TC = 3 };
 int gd_ctx_set_gain_path(gd_ctx *ctx, int path);
 
