@@ -160,14 +160,6 @@ __device__ __forceinline__ int npass_of(const PtGrid &a, int sl)
     return (m + PT_NMAX - 1) / PT_NMAX;
 }
 
-// Two BF16 values in one word, the first at the lower address.
-__device__ __forceinline__ uint32_t pack_bf16(float first, float second)
-{
-    const uint32_t a = (uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(first));
-    const uint32_t b = (uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(second));
-    return a | (b << 16);
-}
-
 template <bool CMAP_SMEM>
 __global__ void __launch_bounds__(kPtThreads, 1)
     pair_tc_kernel(const __grid_constant__ PtMaps maps, const __grid_constant__ PtLaunch L)
@@ -446,21 +438,19 @@ __global__ void __launch_bounds__(kPtThreads, 1)
                                 if (k < u.K) set_run();
                             }
                         }
-                        uint4 hv, lv;
-                        float hf[8], lf[8];
+                        // BF16 hi / lo of each pair of products, two per conversion
+                        // (the first at the lower address; p - hi is exact in FP32)
+                        uint32_t hw[4], lw[4];
 #pragma unroll
-                        for (int t = 0; t < 8; t++) {
-                            hf[t] = __bfloat162float(__float2bfloat16_rn(pv[t]));
-                            lf[t] = pv[t] - hf[t];
+                        for (int q = 0; q < 4; q++) {
+                            const __nv_bfloat162 h2 = __floats2bfloat162_rn(pv[2 * q], pv[2 * q + 1]);
+                            const __nv_bfloat162 l2 = __floats2bfloat162_rn(pv[2 * q] - __low2float(h2),
+                                                                            pv[2 * q + 1] - __high2float(h2));
+                            hw[q] = *reinterpret_cast<const uint32_t *>(&h2);
+                            lw[q] = *reinterpret_cast<const uint32_t *>(&l2);
                         }
-                        hv.x = pack_bf16(hf[0], hf[1]);
-                        hv.y = pack_bf16(hf[2], hf[3]);
-                        hv.z = pack_bf16(hf[4], hf[5]);
-                        hv.w = pack_bf16(hf[6], hf[7]);
-                        lv.x = pack_bf16(lf[0], lf[1]);
-                        lv.y = pack_bf16(lf[2], lf[3]);
-                        lv.z = pack_bf16(lf[4], lf[5]);
-                        lv.w = pack_bf16(lf[6], lf[7]);
+                        const uint4 hv = make_uint4(hw[0], hw[1], hw[2], hw[3]);
+                        const uint4 lv = make_uint4(lw[0], lw[1], lw[2], lw[3]);
                         // 16-byte chunk j of this row, 128-byte swizzle
                         const uint32_t co = (((uint32_t)j ^ swz) & 7u) * 16u;
                         *reinterpret_cast<uint4 *>(pH + co) = hv;
