@@ -7,13 +7,16 @@
 //   G_i[a][b] = m(d) * w(|2i - s|, |d|) * [s - i in the box],
 //   m(d) = (d_x == 0 ? 1 : 1/2) * (d_y == 0 ? 2 : 1) * (d_z == 0 ? 2 : 1),
 // with w the analytic weight table (compute_matrix.cu:505-562).  G is stored
-// dense in BF16 (optionally as hi + lo parts), G[i][b][a] with a contiguous.
+// in BF16 (optionally as hi + lo parts) as the 256 x 64 tiles of its block
+// upper triangle that hold a nonzero entry, with the nodes in a Hilbert-curve
+// matrix order, and only for one node per orbit of the lattice's reflections
+// (node R(i) uses G_i with f reflected by R).
 //
 // Contraction: for output node i and 128 cells c,
 //   D[c][b] = sum_a F[c][a] G_i[a][b]   (tcgen05.mma, BF16 x BF16 -> FP32 in TMEM)
 //   I[i][c] = sum_b D[c][b] f[b][c]      (epilogue, FP32)
 // One CTA per (128-cell tile, i), by default two CTAs per cluster running each
-// MMA as a CTA pair (M = 256 cells).  Warp 0 issues TMA loads of F (cells x
+// MMA as a CTA pair (M = 256 cells); one launch may serve several grids.  Warp 0 issues TMA loads of F (cells x
 // 64 a) and of G_i (256 b x 64 a, or this CTA's half of it) into a ring of
 // shared-memory stages (128-byte swizzle); warp 1 issues the MMAs (N = 256,
 // K = 16) into one of two TMEM accumulators, or relays its CTA's landed
