@@ -16,7 +16,8 @@
 // (relative error ~1e-6 against the FP32 kernel).  Boxes with more than 256
 // groups run as several passes of at most 256 groups, each forming P again.
 //
-// One CTA per (128-cell tile, chunk of s), warp-specialized:
+// One persistent CTA per SM takes (grid, 128-cell tile, chunk of the walk over
+// s) units from a device list, warp-specialized:
 //   warps 14..21 pair products of one 64-offset chunk for the 128 cells (thread
 //                = cell, eight gathers of f per product, the FP32 products of
 //                the FP32 kernel), split into BF16 hi/lo and written to shared
