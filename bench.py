@@ -427,14 +427,14 @@ def run_ours(args):
 
 def path_launches(name, ctx):
     """Kernel launches of the loss and of the gain on a gain path: the FP32
-    loss kernel, or on the collision-matrix paths the BF16 conversion of f and
-    one tensor-core GEMM; the FP32 gain kernel and its chunk reduction, the
+    loss kernel, or on the tensor-core paths the BF16 conversion of f and one
+    tensor-core GEMM; the FP32 gain kernel and its chunk reduction, the
     pair tensor-core kernel between its scale and conversion kernels, or the
     conversion of f and the collision-matrix kernel."""
     if name == "pair":
         return 1, 2
     if name == "pair_tc":
-        return 1, 3
+        return 2, 3
     return 2, 2
 
 

@@ -468,6 +468,8 @@ int gd_ctx_set_gain_path(gd_ctx *ctx, int path)
     c.gain_path = GD_GAIN_PAIR;
     if (path == GD_GAIN_PAIR_TC) {
         int rc = gd::pair_tc_build(c);
+        // the loss on the tensor cores too (the loss matrix alone)
+        if (!rc && (rc = gd::cmatrix_create_loss_only(ctx, &c.cmatrix))) gd::pair_tc_free(c);
         if (rc) return rc;
     } else if (path != GD_GAIN_PAIR) {
         const int mode = path == GD_GAIN_CMATRIX_BF16 ? GD_CMATRIX_BF16 : GD_CMATRIX_BF16X3;

@@ -241,6 +241,9 @@ int gemm_bf16x3_nt_f32(const void *Ah, const void *Al, int M, const void *Bh, co
 // loss on the tensor cores when the context uses collision matrices
 // (gd_cmatrix.cu); GD_ERR_UNSUPPORTED when the layout does not allow it.
 int cmatrix_loss(gd_cmatrix *cm, const float *f, int ncells, int ld, float *nu, cudaStream_t st);
+// the loss matrix alone, for contexts on the pair path with its contraction on
+// the tensor cores (gd_cmatrix.cu)
+int cmatrix_create_loss_only(gd_ctx *ctx, gd_cmatrix **out);
 // loss for the context's gain path: tensor cores with collision matrices (when
 // the layout allows), else the FP32 kernel
 int run_loss_path(Context &c, const float *f, int ncells, int ld, float *nu, cudaStream_t st);
