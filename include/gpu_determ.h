@@ -124,9 +124,10 @@ int gd_correction_basis(gd_ctx *ctx, float *basis, gd_stream stream);
 /* ---- collision operator ------------------------------------------------ */
 /* Loss frequency nu[i][c] = sum_j b(|i-j|) f[j][c] and gain I[i][c] over the
  * in-sphere nodes (either output may be NULL), on the context's gain path:
- * GD_GAIN_PAIR computes both in FP32 (SIMT kernels); the collision-matrix
- * paths compute the gain on the tensor cores and, when ld is a multiple of
- * 4, the loss as one BF16x3 GEMM (see gd_ctx_set_gain_path).  Replaces the
+ * GD_GAIN_PAIR computes both in FP32 (SIMT kernels); the tensor-core paths
+ * (collision matrices, GD_GAIN_PAIR_TC) compute the gain on the tensor cores
+ * and, when ld is a multiple of 4, the loss as one BF16x3 GEMM (see
+ * gd_ctx_set_gain_path).  Replaces the
  * loss and gain stages of evolve_colisions (collision_integral.h:11-17,
  * collision_integral.cu:32-188, 587-648). */
 int gd_collision(gd_ctx *ctx, const float *f, int ncells, int ld, float *nu, float *gain,
@@ -178,16 +179,16 @@ int gd_ctx_check(gd_ctx *ctx, gd_stream stream);
  * a nonzero entry are stored (off-diagonal entries doubled), and only for one
  * node per orbit of the lattice's reflections (x_a -> n_a - 1 - x_a on each
  * axis; the node set is symmetric since the sphere is centred in the box and
- * n_a is even): node R(i) uses G_i with f reflected by R.  At 20^3 (R = 4.8) that is ~5 GB in BF16, twice that for
- * GD_CMATRIX_BF16X3 (8x less than one matrix per node).
- * GD_CMATRIX_BF16 rounds f and G to BF16 (relative error ~3e-4 on I);
- * GD_CMATRIX_BF16X3 splits both into BF16 hi + lo parts and sums
- * hi*hi + hi*lo + lo*hi (~4e-6).  With a context's gain path set to either
- * mode, its loss nu = B f also runs on the tensor cores (B and f split into
- * BF16 hi + lo, three products per K step in one launch, ~5e-6) when ld is
- * a multiple of 4.  No reference counterpart: the reference
- * forms these matrices only implicitly in its gain loop
- * (collision_integral.cu:75-188). */
+ * n_a is even): node R(i) uses G_i with f reflected by R.  At 20^3
+ * (R = 4.8) that is ~5 GB in BF16, twice that for GD_CMATRIX_BF16X3 (8x less
+ * than one matrix per node).  GD_CMATRIX_BF16 rounds f and G to BF16
+ * (relative error ~3e-4 on I); GD_CMATRIX_BF16X3 splits both into BF16 hi +
+ * lo parts and sums hi*hi + hi*lo + lo*hi (~4e-6).  With a context's gain
+ * path set to either mode (or to GD_GAIN_PAIR_TC), its loss nu = B f also
+ * runs on the tensor cores (B and f split into BF16 hi + lo, three products
+ * per K step in one launch, ~5e-6) when ld is a multiple of 4.  No reference
+ * counterpart: the reference forms these matrices only implicitly in its
+ * gain loop (collision_integral.cu:75-188). */
 typedef struct gd_cmatrix gd_cmatrix;
 enum { GD_CMATRIX_BF16 = 0, GD_CMATRIX_BF16X3 = 1 };
 int gd_cmatrix_create(gd_ctx *ctx, int mode, gd_cmatrix **out);
