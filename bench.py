@@ -75,6 +75,11 @@ def parse():
     p.add_argument("--train-steps", type=int, default=6000)
     p.add_argument("--fp64-cells", type=int, default=32,
                    help="cells of the timed batch checked against the oracle's FP64 path (in the CPU-baseline leg)")
+    p.add_argument("--kernels", action="store_true",
+                   help="time the step's loss, projection and relaxation kernels one by one against their "
+                        "rooflines (one JSON line) instead of the step")
+    p.add_argument("--once", action="store_true",
+                   help="with --kernels: launch each kernel once, untimed (the command an ncu capture runs)")
     return p.parse_args()
 
 
@@ -644,9 +649,116 @@ def alternatives(args, ctx, f0, nc, stream, flush, peak, q_ref):
     return out
 
 
+def run_kernels(args):
+    """The step's kernels besides the gain, one by one on the bench workload:
+    CUDA events on the launching stream, the 256 MiB L2 flush before each
+    launch, best of --steps after --warmup.  Each is set against what bounds
+    it: HBM bytes (MEASURED_PEAKS.json), or the FP32 / FP64 FMA or BF16 tensor
+    throughput.  GB300's FP64 rate is 1/64 of its FP32 rate, and float <-> double
+    conversions issue on the same pipe, so the FP64 projection and relaxation
+    are bound by it rather than by HBM."""
+    import torch
+    import gpu_determ_gb300 as gd
+    from gpu_determ_gb300 import inputs
+
+    torch.cuda.set_device(0)
+    spec = gd.GridSpec(args.grid, R=args.radius)
+    t0 = time.perf_counter()
+    ctx = gd.Context(spec)
+    torch.cuda.synchronize()
+    build_s = {"context": time.perf_counter() - t0}
+    n, nc = ctx.n_pnt, args.cells
+    f = torch.from_numpy(inputs.dirichlet_mixtures(spec.fill(), nc, seed=args.seed + 17)).cuda()
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    nu, gain, nuc = (torch.empty_like(f) for _ in range(3))
+    q = torch.empty(f.shape, dtype=torch.float64, device="cuda")
+    fr = f.clone()
+    tm, dt = torch.zeros(1, device="cuda"), torch.zeros(1, device="cuda")
+    stream = torch.cuda.current_stream()
+    ms = {}
+
+    def run(name, fn):
+        fn()
+        torch.cuda.synchronize()
+        if args.once:
+            return
+        for _ in range(args.warmup):
+            fn()
+        best = float("inf")
+        for _ in range(max(1, args.steps)):
+            flush.fill_(1)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            best = min(best, e0.elapsed_time(e1))
+        ms[name] = best
+
+    run("loss_fp32", lambda: ctx.collision(f, nc, nc, nu, None))
+    if args.gain != "pair":
+        t0 = time.perf_counter()
+        ctx.set_gain_path(GAIN_PATHS[args.gain])
+        torch.cuda.synchronize()
+        build_s["gain_path"] = time.perf_counter() - t0
+        run("loss_tc", lambda: ctx.collision(f, nc, nc, nu, None))
+    ctx.collision(f, nc, nc, nu, gain)
+    run("project", lambda: ctx.project(f, nu, gain, nc, nc, nuc, q, None))
+    run("relax_fixed", lambda: ctx.relax(fr, nuc, gain, nc, nc, gd.DT_FIXED, 1e-4, tm, dt))
+    run("relax_courant", lambda: ctx.relax(fr, nuc, gain, nc, nc, gd.DT_COURANT, args.courant, tm, dt))
+    ctx.check()
+    line = {"mode": "kernels", "once": bool(args.once), "build_s": build_s,
+            "config": {"grid": args.grid, "radius": args.radius, "nodes": n, "cells": nc, "gain": args.gain,
+                       "l2": "256 MiB buffer written before each timed launch"}}
+    if args.once:
+        print(json.dumps(line))
+        return
+    pk = peaks(gd, 0)
+    try:
+        with open(PEAKS_FILE) as fh:
+            hbm, hbm_src = float(json.load(fh)["hbm_gbs"]), "measured copy (MEASURED_PEAKS.json)"
+    except Exception:
+        hbm, hbm_src = 6800.0, "fallback copy bandwidth"
+    cells = float(n) * nc
+
+    def entry(t, flop=None, fpeak=None, nbytes=None, work=""):
+        e = {"ms": t, "work": work}
+        if flop is not None:
+            e.update({"tflops": flop / t / 1e9, "flop_peak_tflops": fpeak, "flop_frac": flop / t / 1e9 / fpeak})
+        if nbytes is not None:
+            e.update({"gbs": nbytes / t / 1e6, "hbm_peak_gbs": hbm, "hbm_frac": nbytes / t / 1e6 / hbm})
+        return e
+
+    k = {}
+    k["loss_kernel (FP32)"] = entry(ms["loss_fp32"], flop=2.0 * n * n * nc, fpeak=pk["fp32"],
+                                    work="2 n^2 FLOP per cell (one FMA per partner), vs the FP32 FMA peak")
+    if "loss_tc" in ms:
+        rows, cols, kk = -(-n // 128) * 128, -(-nc // 128) * 128, -(-n // 64) * 64
+        k["convert + gemm3_nt_kernel (loss on tensor cores)"] = entry(
+            ms["loss_tc"], flop=3 * 2.0 * rows * cols * kk, fpeak=pk["bf16"],
+            nbytes=4.0 * n * kk + 4.0 * kk * nc + 4.0 * cells + 4.0 * cells,
+            work="3 BF16 MMA products per K step over the padded tiles, vs the BF16 peak; bytes: B and f "
+                 "as BF16 hi/lo, f read and nu written in FP32")
+    k["project_kernel (FP64)"] = entry(ms["project"], flop=65.0 * cells, fpeak=pk["fp64"], nbytes=24.0 * cells,
+                                       work="65 FP64 FLOP per node and cell (53 for the 25 sums, 12 for nu' and "
+                                            "Q) and 7 conversions; bytes: f, nu, I read, nu' and FP64 Q written")
+    k["relax_kernel (FP64, fixed dt)"] = entry(ms["relax_fixed"], flop=4.0 * cells, fpeak=pk["fp64"],
+                                               nbytes=16.0 * cells,
+                                               work="f + dt (I - f nu') in FP64: 4 FLOP and 4 conversions; bytes: f, nu', "
+                                                    "I read, f written")
+    k["max_kernel + dt_kernel (Courant dt)"] = entry(max(ms["relax_courant"] - ms["relax_fixed"], 1e-6),
+                                                     nbytes=4.0 * cells, work="nu' read once")
+    line.update({"kernels": k, "peaks": {"hbm_gbs": hbm, "hbm_source": hbm_src, "fp32_tflops": pk["fp32"],
+                                         "fp64_tflops": pk["fp64"], "bf16_tflops": pk["bf16"],
+                                         "fma_source": pk["fma_source"], "bf16_source": pk["bf16_source"]}})
+    print(json.dumps(line))
+
+
 def main():
     args = parse()
-    if args.impl == "reference":
+    if args.kernels:
+        run_kernels(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_ours(args)

@@ -349,7 +349,7 @@ static int create_context(Context &c, const gd_grid_spec &spec, int device)
     GD_CUDA(cudaMalloc(&c.d_nodes, sizeof(uint32_t) * d.n_pnt));
     GD_CUDA(cudaMalloc(&c.d_phi, sizeof(double) * 5 * d.n_pnt));
     GD_CUDA(cudaMalloc(&c.d_b, sizeof(float) * d.nxyz));
-    GD_CUDA(cudaMalloc(&c.d_reduce, sizeof(float) * 512));
+    GD_CUDA(cudaMalloc(&c.d_reduce, sizeof(float) * kReduceFloats));
     GD_CUDA(cudaMalloc(&c.d_status, sizeof(unsigned int) * 2));
     {
         const unsigned int clear[2] = {0u, 0xffffffffu};

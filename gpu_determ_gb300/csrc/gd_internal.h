@@ -55,6 +55,9 @@ struct Scratch {
     size_t bytes = 0;
 };
 
+// Floats of a context's reduction buffer (block maxima of nu', then dt).
+constexpr int kReduceFloats = 2048;
+
 struct Context {
     gd_grid_spec spec{};
     Dims d{};
@@ -109,7 +112,7 @@ struct Context {
     // launch shape (device array, count), uploaded once
     std::map<std::string, std::pair<int4 *, int>> pt_units_dev;
     int gain_waves = 2;         // gain launch: at least this many CTAs per SM (autotuned)
-    float *d_reduce = nullptr;  // small device scalars (max nu, dt)
+    float *d_reduce = nullptr;  // [kReduceFloats]: block maxima of nu', then dt
     unsigned int *d_status = nullptr;  // numeric status of projections: flags, first failing cell
     int sm_count = 0;
 };

@@ -159,19 +159,27 @@ __global__ void __launch_bounds__(kWarps * 32) project_kernel(ProjArgs a)
 }
 
 // Per-block maximum of nu' (non-negative); a second launch with one block
-// reduces the block maxima.  The maximum does not depend on the order.
+// reduces the block maxima.  Block b takes the rows b, b + gridDim.x, ..., its
+// threads the cells of each row (32-bit indices, four loads in flight per
+// thread).  The maximum does not depend on the order.
 __global__ void max_kernel(const float *__restrict__ v, int n_pnt, int ncells, int ld,
                            float *__restrict__ out)
 {
     __shared__ float sm[256];
-    float m = 0.f;
-    const int64_t total = (int64_t)n_pnt * ncells;
-    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total;
-         t += (int64_t)gridDim.x * blockDim.x) {
-        const int node = (int)(t / ncells), c = (int)(t % ncells);
-        m = fmaxf(m, v[(size_t)node * ld + c]);
+    float m0 = 0.f, m1 = 0.f, m2 = 0.f, m3 = 0.f;
+    const int step = blockDim.x;
+    for (int node = blockIdx.x; node < n_pnt; node += gridDim.x) {
+        const float *row = v + (size_t)node * ld;
+        int c = threadIdx.x;
+        for (; c + 3 * step < ncells; c += 4 * step) {
+            m0 = fmaxf(m0, __ldg(row + c));
+            m1 = fmaxf(m1, __ldg(row + c + step));
+            m2 = fmaxf(m2, __ldg(row + c + 2 * step));
+            m3 = fmaxf(m3, __ldg(row + c + 3 * step));
+        }
+        for (; c < ncells; c += step) m0 = fmaxf(m0, __ldg(row + c));
     }
-    sm[threadIdx.x] = m;
+    sm[threadIdx.x] = fmaxf(fmaxf(m0, m1), fmaxf(m2, m3));
     __syncthreads();
     for (int s = 128; s > 0; s >>= 1) {
         if (threadIdx.x < s) sm[threadIdx.x] = fmaxf(sm[threadIdx.x], sm[threadIdx.x + s]);
@@ -187,32 +195,37 @@ __global__ void dt_kernel(const float *__restrict__ blockmax, int nb, int mode, 
                           float *__restrict__ dt_out, float *__restrict__ time_dev,
                           float *__restrict__ dt_user)
 {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    if (blockIdx.x != 0 || threadIdx.x >= 32) return;
     float dt = param;
     if (mode == GD_DT_COURANT) {
+        // one warp: lanes take strided block maxima, then a shuffle maximum
         float m = 0.f;
-        for (int k = 0; k < nb; k++) m = fmaxf(m, blockmax[k]);
+        for (int k = threadIdx.x; k < nb; k += 32) m = fmaxf(m, blockmax[k]);
+        for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
         dt = m > 0.f ? param / m : 1.0e10f;
     }
+    if (threadIdx.x != 0) return;
     *dt_out = dt;
     if (dt_user) *dt_user = dt;
     if (time_dev) *time_dev += dt;
 }
 
 // f <- f + dt (I - f nu')  (evolve_f, collision_integral.cu:809-833), in FP64.
+// Block b takes the rows b, b + gridDim.x, ..., its threads the cells of each
+// row (32-bit indices).
 __global__ void relax_kernel(float *__restrict__ f, const float *__restrict__ nu,
                              const float *__restrict__ gain, const double *__restrict__ q, int n_pnt,
                              int ncells, int ld, const float *__restrict__ dt_dev)
 {
     const double dt = *dt_dev;
-    const int64_t total = (int64_t)n_pnt * ncells;
-    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total;
-         t += (int64_t)gridDim.x * blockDim.x) {
-        const int node = (int)(t / ncells), c = (int)(t % ncells);
-        const size_t o = (size_t)node * ld + c;
-        const double fv = f[o];
-        const double qv = q ? q[o] : (double)gain[o] - fv * (double)nu[o];
-        f[o] = (float)(fv + dt * qv);
+    for (int node = blockIdx.x; node < n_pnt; node += gridDim.x) {
+        const size_t r = (size_t)node * ld;
+        for (int c = threadIdx.x; c < ncells; c += blockDim.x) {
+            const size_t o = r + c;
+            const double fv = f[o];
+            const double qv = q ? q[o] : (double)gain[o] - fv * (double)nu[o];
+            f[o] = (float)(fv + dt * qv);
+        }
     }
 }
 
@@ -280,8 +293,9 @@ int run_relax_q(Context &c, float *f, const float *nu_corr, const float *gain, c
                 int ncells, int ld, int mode, float param, float *time_dev, float *dt_dev,
                 cudaStream_t st)
 {
-    const int nb = 256;
-    float *blockmax = c.d_reduce;      // [nb]
+    // blocks of the maximum: a few per SM, within the reduction buffer
+    const int nb = std::max(1, std::min(std::min(4 * c.sm_count, kReduceFloats - 1), c.d.n_pnt));
+    float *blockmax = c.d_reduce;        // [nb]
     float *dt_scalar = c.d_reduce + nb;  // [1]
     if (mode == GD_DT_COURANT) {
         max_kernel<<<nb, 256, 0, st>>>(nu_corr, c.d.n_pnt, ncells, ld, blockmax);
@@ -289,8 +303,7 @@ int run_relax_q(Context &c, float *f, const float *nu_corr, const float *gain, c
     }
     dt_kernel<<<1, 32, 0, st>>>(blockmax, nb, mode, param, dt_scalar, time_dev, dt_dev);
     GD_CUDA(cudaGetLastError());
-    const int64_t total = (int64_t)c.d.n_pnt * ncells;
-    const int blocks = (int)std::min<int64_t>((total + 255) / 256, (int64_t)c.sm_count * 16);
+    const int blocks = std::min(c.d.n_pnt, c.sm_count * 16);
     relax_kernel<<<std::max(blocks, 1), 256, 0, st>>>(f, nu_corr, gain, q, c.d.n_pnt, ncells, ld, dt_scalar);
     GD_CUDA(cudaGetLastError());
     return GD_OK;
