@@ -250,7 +250,7 @@ int gd_compact_to_box(gd_ctx *ctx, const float *compact, int ncells, int ld, flo
  * fewer chunks and the sums, ordered differently, agree within FP32
  * rounding.  The first call on a device looks the array's address up, which
  * may also load the library's device code on that device and so reserve the
- * 64 MiB there (the driver's allocation, not a cudaMalloc): a caller that
+ * 64 MiB there (the CUDA driver's allocation, not a cudaMalloc): a caller that
  * wants no allocation at all inside its hot loop makes one warm-up call at
  * start-up, before any stream capture.  All calls share the array: calls
  * that overlap on the GPU race, so order them. */
