@@ -201,6 +201,20 @@ class Oracle:
         sing = lib().or_project(self._c, f, nu, gain, nc, nu_c, q, x)
         return nu_c, q, x, sing
 
+    def project_f64(self, f, nu, gain):
+        """The conservation projection with FP64 nu and gain (no FP32 rounding
+        of its inputs), in numpy: A X = B with A_kl = sum_i f nu phi_k phi_l,
+        B_k = sum_i (I - f nu) phi_k, nu' = nu (1 + X.phi), Q = I - f nu'
+        (the intended per-cell system of collision_integral.cu:217-526 over
+        the basis of velocity.cu:17-50).  Returns Q, [n_pnt][cells] float64."""
+        phi = self.phi()
+        f64 = np.asarray(f, np.float64)
+        fnu = f64 * nu
+        A = np.einsum("ic,ik,il->ckl", fnu, phi, phi)
+        B = np.einsum("ic,ik->ck", gain - fnu, phi)
+        X = np.linalg.solve(A, B[..., None])[..., 0]
+        return gain - f64 * nu * (1.0 + phi @ X.T)
+
     def moments(self, f):
         f = np.ascontiguousarray(f, np.float64)
         m = np.zeros((f.shape[1], 5), np.float64)

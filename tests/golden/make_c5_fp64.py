@@ -9,9 +9,7 @@ Maxwellians M(1, u_c, T_c) of inputs.cavity_field for the 16 384-cell batch
 (seed 0), cells 0, 5461, 10922 and 16383 (a corner, two interior cells and the
 opposite corner of the 128 x 128 cell grid).  For each: the oracle's FP64 loss
 nu and gain I (collision_integral.cu:32-72, 75-188 restated in oracle.c), then
-the conservation projection in FP64 numpy (A X = B with
-A_kl = sum f nu phi_k phi_l, B_k = sum (I - f nu) phi_k, nu' = nu (1 + X.phi),
-Q = I - f nu').
+the conservation projection in FP64 (Oracle.project_f64).
 
 Outputs (npz): f [n][4] float32 (the inputs, so the test does not regenerate
 them), q [n][4] float64, gain [n][4] float64, cells [4] int64.
@@ -34,16 +32,6 @@ CELLS = (0, 5461, 10922, 16383)
 BATCH = 16384
 
 
-def fp64_projection(o, f, nu, gain):
-    phi = o.phi()
-    f64 = f.astype(np.float64)
-    fnu = f64 * nu
-    A = np.einsum("ic,ik,il->ckl", fnu, phi, phi)
-    B = np.einsum("ic,ik->ck", gain - fnu, phi)
-    X = np.linalg.solve(A, B[..., None])[..., 0]
-    return gain - f64 * nu * (1.0 + phi @ X.T)
-
-
 def main():
     o = Oracle(32, R=5.5)
     g = {"u": o.u, "v": o.v, "w": o.w, "ui": o.ui, "vi": o.vi, "wi": o.wi}
@@ -56,7 +44,7 @@ def main():
     fb = o.to_box(f)
     nu = o.loss_f64(fb)
     gain = o.gain_f64(fb)
-    q = fp64_projection(o, f, nu, gain)
+    q = o.project_f64(f, nu, gain)
     out = os.path.join(HERE, "c5_fp64_cells.npz")
     np.savez_compressed(out, f=f, q=q, gain=gain, cells=np.asarray(CELLS, np.int64))
     print("wrote", out, "n_pnt", o.n_pnt)
