@@ -133,3 +133,23 @@ def test_oracle_projection_conserves():
     mom = phi.T @ q
     scale = np.abs(phi).T @ np.abs(gain.astype(np.float64))
     assert np.all(np.abs(mom) <= 1e-12 * scale)
+
+
+def test_oracle_fp64_projection_conserves_and_agrees():
+    """The all-FP64 projection (FP64 nu and gain, numpy solve) conserves the
+    five moments and agrees with the C projection, which rounds nu and gain
+    to FP32 first, to that rounding."""
+    o = Oracle(8, R=16.5)
+    rng = np.random.default_rng(2)
+    f = np.stack([pyoracle.maxwellian(o, 1.0, rng.normal(0, 0.5, 3), 1.0) +
+                  pyoracle.maxwellian(o, 0.5, rng.normal(0, 0.5, 3), 0.7) for _ in range(3)], axis=1)
+    f = f.astype(np.float32)
+    fb = o.to_box(f)
+    nu, gain = o.loss_f64(fb), o.gain_f64(fb)
+    q64 = o.project_f64(f, nu, gain)
+    phi = o.phi()
+    scale = np.abs(phi).T @ np.abs(gain)
+    assert np.all(np.abs(phi.T @ q64) <= 1e-12 * scale)
+    _, q32in, _, sing = o.project(f, nu.astype(np.float32), gain.astype(np.float32))
+    assert sing == 0
+    assert np.linalg.norm(q64 - q32in) <= 1e-4 * np.linalg.norm(q64)
